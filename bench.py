@@ -1,0 +1,408 @@
+#!/usr/bin/env python3
+"""Benchmark of the LSD-SLAM hot path on GB300: batched SE3 trackFrame of frame pairs at 640x480.
+
+One step = one batch of 64 independent synthetic frame pairs at 640x480 (5 pyramid levels, ~60k
+semi-dense keyframe points each) pushed through the whole device path: both image pyramids, the
+keyframe depth pyramid and point compaction, and the persistent cluster tracker running every
+pair's coarse-to-fine LM loop to convergence.  value = pairs tracked per second with the inputs
+resident in HBM; e2e = the same through the public C-ABI call with pinned host buffers (upload,
+run, read back poses and stats every step).  Also reported: the plain one-pair-per-call form
+(lsdg_track_se3), the mixed-size batch (20 x 320x240, 32 x 640x480, 12 x 1280x960), the
+tracker's roofline, the CPU restatement on the host cores, and accuracy against ground truth.
+
+--impl reference times the CPU restatement of the same path (the reference's own lsd-slam code
+is an unvendored import and cannot be built), all host threads, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lsd-slam-pangolin-gui_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)
+
+import numpy as np  # noqa: E402
+
+METRIC = "tracked frame pairs/s @640x480"
+UNIT = "pairs/s"
+N_PAIRS = 64
+W, H = 640, 480
+MIXED = [(320, 240)] * 20 + [(640, 480)] * 32 + [(1280, 960)] * 12
+
+
+def _gen(seed, w, h):
+    import synth
+    return synth.tracking_pair(seed, w, h)
+
+
+def gen_pairs(specs, workers):
+    ctx = mp.get_context("spawn")  # never fork a process that may touch CUDA
+    with ctx.Pool(max(1, min(workers, len(specs)))) as pool:
+        return pool.starmap(_gen, specs)
+
+
+# ----------------------------------------------------------------------------------------------
+# clocks
+# ----------------------------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t0 = self.t1 = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "50", "-i", str(self.device)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+
+    def mark(self, t0, t1):
+        self.t0, self.t1 = t0, t1
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out = ""
+        sm, mx, reasons = [], None, set()
+        for ln in out.splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in (("hw_slowdown", f[5]), ("hw_thermal_slowdown", f[6]), ("sw_thermal_slowdown", f[7]),
+                            ("sw_power_cap", f[8])):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        loaded = [s for s in sm if s > 0.5 * (mx or max(sm))] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm), "window": "soak + timed region"}
+
+
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic(workload_key: str):
+    """dram bytes per launch of the tracker kernel from a committed ncu summary, if present."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    pat = re.compile(r"traffic_bytes_per_launch\[" + re.escape(workload_key) + r"\]\s*:\s*([0-9.eE+]+)")
+    for fn in sorted(os.listdir(d)):
+        if fn.endswith((".md", ".txt")):
+            m = pat.search(open(os.path.join(d, fn)).read())
+            if m:
+                return float(m.group(1))
+    return None
+
+
+# ----------------------------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    import lsdg
+    import synth
+
+    workers = os.cpu_count() or 8
+    # all host-side generation happens before the first CUDA call
+    pairs = gen_pairs([(1000 * rank + i, W, H) for i in range(N_PAIRS)], workers)
+    mixed = gen_pairs([(5000 + 1000 * rank + i, w, h) for i, (w, h) in enumerate(MIXED)], workers) if not args.quick else []
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    ctx = lsdg.Context(device=local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream_ptr())
+
+    def pinned(a):
+        t = torch.empty(a.size, dtype=torch.float32).pin_memory()
+        t.numpy()[:] = a.ravel()
+        return t.numpy()
+
+    ri, rd, rv, ni = [pinned(x) for x in lsdg.pack_pairs(pairs)]
+    init = np.stack([np.eye(3, 4)] * N_PAIRS)
+    batch = lsdg.Batch(ctx, [p.w for p in pairs], [p.h for p in pairs], [p.intr for p in pairs])
+    batch.load(ri, rd, rv, ni, init)
+    batch.run()  # autotune + graph capture
+    out, stats = batch.read()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    clocks = Clocks(local_rank)
+    clocks.start()
+    # warm-up: W steps, then a ~1.5 s soak so clocks settle and the sampler sees the load
+    for _ in range(max(3, args.warmup)):
+        batch.run()
+    ctx.sync()
+    t_soak = time.time()
+    while time.time() - t_soak < 1.5:
+        batch.run()
+        ctx.sync()
+
+    # ---- value: inputs resident in HBM ----
+    barrier()
+    n_launch0 = ctx.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tw0 = time.time()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run()
+    e1.record(stream)
+    e1.synchronize()
+    tw1 = time.time()
+    barrier()
+    dev_ms = max_over_ranks(e0.elapsed_time(e1))
+    launches = ctx.launch_count() - n_launch0
+    ms_per_step = dev_ms / args.steps
+    value = N_PAIRS * world * args.steps / (dev_ms / 1e3)
+
+    # ---- e2e: public call with pinned host buffers, copies in the timed region ----
+    barrier()
+    t0 = time.time()
+    for _ in range(args.steps):
+        out_e, stats_e = batch.track(ri, rd, rv, ni, init)
+    barrier()
+    e2e_s = max_over_ranks(time.time() - t0)
+    clocks.mark(tw0, tw1)
+    clk = clocks.stop()
+    e2e_value = N_PAIRS * world * args.steps / e2e_s
+    h2d = 4 * ri.nbytes + init.nbytes
+    d2h = out_e.nbytes + N_PAIRS * 280
+
+    # ---- roofline of the tracker kernel (events recorded inside the captured graph) ----
+    tr, bd = [], []
+    for _ in range(5):
+        batch.run()
+        b_ms, t_ms = batch.timing()
+        tr.append(t_ms)
+        bd.append(b_ms)
+    passes, pass_bytes, unique_bytes = batch.work()
+    track_ms = statistics.median(tr)
+    build_ms = statistics.median(bd)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = pass_bytes / (track_ms / 1e3) / 1e9
+    traffic = profiled_traffic("64x640x480")
+
+    # accuracy vs ground truth (the synthetic motion)
+    errs = [synth.pose_error(out_e[i], pairs[i].frame_to_ref) for i in range(N_PAIRS)]
+    lost = sum(1 for s in stats_e if s.status != 0)
+
+    # ---- plain: one pair per lsdg_track_se3 call on resident frames ----
+    frames = []
+    for p in pairs[:16]:
+        kf = lsdg.Frame(ctx, p.w, p.h, p.intr).upload(p.ref_image).set_depth(p.ref_idepth, p.ref_idepth_var)
+        fr = lsdg.Frame(ctx, p.w, p.h, p.intr).upload(p.new_image)
+        frames.append((kf, fr))
+    tracker = lsdg.SE3Tracker(ctx)
+    tracker.trackFrame(*frames[0])  # autotune the one-pair shape
+    barrier()
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tp = time.time()
+    pe0.record(stream)
+    for rep in range(2):
+        for kf, fr in frames:
+            tracker.trackFrame(kf, fr)
+    pe1.record(stream)
+    pe1.synchronize()
+    plain_wall = time.time() - tp
+    plain_value = 2 * len(frames) / plain_wall
+    plain_dev = 2 * len(frames) / (pe0.elapsed_time(pe1) / 1e3)
+    del frames
+
+    # ---- mixed-size batch (20 x 320x240, 32 x 640x480, 12 x 1280x960) ----
+    mixed_res = None
+    if mixed:
+        mb = lsdg.Batch(ctx, [p.w for p in mixed], [p.h for p in mixed], [p.intr for p in mixed])
+        mb.load(*[np.ascontiguousarray(x) for x in lsdg.pack_pairs(mixed)], np.stack([np.eye(3, 4)] * len(mixed)))
+        mb.run()
+        for _ in range(3):
+            mb.run()
+        ctx.sync()
+        me0, me1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        me0.record(stream)
+        k_mixed = max(5, args.steps)
+        for _ in range(k_mixed):
+            mb.run()
+        me1.record(stream)
+        me1.synchronize()
+        mo, ms_ = mb.read()
+        m_ms = me0.elapsed_time(me1) / k_mixed
+        merr = [synth.pose_error(mo[i], mixed[i].frame_to_ref) for i in range(len(mixed))]
+        mixed_res = {"pairs": len(mixed), "ms_per_batch": m_ms, "pairs_per_s": len(mixed) / (m_ms / 1e3),
+                     "shape": mb.shape(), "max_gt_rot_err_rad": max(e[0] for e in merr),
+                     "lost": sum(1 for s in ms_ if s.status != 0)}
+        mb.close()
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded textured-plane scenes, sigma=2 noise, semi-dense keyframe depth)",
+        "config": {"workload": f"batched SE3 trackFrame, {N_PAIRS} pairs 640x480 per GPU, 5 levels",
+                   "pairs_per_step_per_gpu": N_PAIRS, "width": W, "height": H, "levels": 5,
+                   "points_level0_mean": float(np.mean([s.n_points for s in stats])),
+                   "l2": "inputs larger than L2: %.0f MB of level-0 inputs + %.0f MB pyramids resident per GPU"
+                         % (4 * ri.nbytes / 1e6, 2 * N_PAIRS * 409200 * 20 / 1e6),
+                   "parallelism": f"pair sharding, {world} rank(s), no collective on the data path",
+                   "tile_shape": batch.shape()},
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "api": "lsdg_batch_track_se3 (pinned host buffers)"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": "track_se3_kernel",
+                     "note": "achieved = algorithmic bytes of all LM residual passes (points 20 B + frame level "
+                             "12 B/px + sums, per pass) / tracker kernel time; re-reads across passes are L2 "
+                             "hits, so this is an L2-side figure against the HBM peak (%s)" % peak_kind,
+                     "first_touch_GBps": unique_bytes / (track_ms / 1e3) / 1e9,
+                     "tracker_ms": track_ms, "build_ms": build_ms, "passes_per_step": passes},
+        "plain": {"pairs_per_s": plain_value, "pairs_per_s_device": plain_dev, "api": "lsdg_track_se3, one pair per call",
+                  "batched_over_plain": value / plain_value},
+        "mixed_batch": mixed_res,
+        "accuracy": {"max_gt_rot_err_rad": max(e[0] for e in errs), "max_gt_trans_err_m": max(e[1] for e in errs),
+                     "lost": lost},
+    }
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline(pairs, args)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    batch.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(pairs, args, min_seconds=10.0):
+    """The float CPU restatement of the same path on the host cores (pairs spread over threads)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lsdo
+    import synth
+
+    cores = os.cpu_count() or 1
+    n = 0
+    t0 = time.time()
+    reps = 0
+    while True:
+        out, stats = lsdo.track_batch(pairs, threads=cores)
+        n += len(pairs)
+        reps += 1
+        if time.time() - t0 >= min_seconds or args.quick:
+            break
+    dt = time.time() - t0
+    # FP64 restatement on a sample, for the accuracy report
+    errs = []
+    for p in pairs[:4]:
+        _, Td, _ = lsdo.track_se3(p, double=True)
+        errs.append(synth.pose_error(out[pairs.index(p)], Td))
+    return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{reps} x the {len(pairs)}-pair 640x480 batch (float CPU restatement, pairs over {cores} threads)",
+            "float_vs_fp64_max_rot_err_rad": max(e[0] for e in errs)}
+
+
+# ----------------------------------------------------------------------------------------------
+# reference arm
+# ----------------------------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lsdo
+
+    workers = os.cpu_count() or 8
+    pairs = gen_pairs([(i, W, H) for i in range(N_PAIRS)], workers)
+    cores = workers
+    # bound the run: a step is the full 64-pair batch unless K steps would exceed ~150 s
+    t0 = time.time()
+    lsdo.track_batch(pairs[:cores], threads=cores)
+    est_pair = (time.time() - t0) / max(1, min(cores, len(pairs))) * cores  # seconds per pair per thread
+    per_step = len(pairs)
+    while per_step > cores and (args.steps + args.warmup) * per_step * est_pair / cores > 150:
+        per_step //= 2
+    sample = pairs[:per_step]
+    for _ in range(args.warmup):
+        lsdo.track_batch(sample, threads=cores)
+    t0 = time.time()
+    for _ in range(args.steps):
+        lsdo.track_batch(sample, threads=cores)
+    dt = time.time() - t0
+    value = per_step * args.steps / dt
+    res = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"SE3 trackFrame on CPU, {per_step} pairs 640x480 per step, 5 levels"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": f"{per_step} pairs per step of the 64-pair 640x480 workload; the reference's own "
+                                      "lsd-slam CPU code is an unvendored import (fips.yml:2-4), so this is the "
+                                      "project's float C++ restatement"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(res), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--quick", action="store_true", help="skip the mixed batch; one CPU-baseline pass")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

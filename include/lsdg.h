@@ -1,0 +1,267 @@
+/*
+ * lsdg.h -- C-ABI of the GB300-native LSD-SLAM per-pixel hot path.
+ *
+ * Two parts, both computed by hand-written CUDA kernels for sm_103a on one GPU:
+ *   - direct image alignment: the per-point warp, photometric residual, Jacobian and
+ *     Huber-weighted normal equations inside a Levenberg-Marquardt loop over the image
+ *     pyramid (SE3Tracker::trackFrame, Sim3Tracker::trackFrameSim3, calculateWarpUpdate);
+ *   - the semi-dense inverse-depth filter (DepthMap::updateKeyframe -> observeDepth,
+ *     DepthMap::createKeyFrame -> propagateDepth, regularizeDepthMap).
+ *
+ * Where the reference meets this path: lib/App/InputThread.cpp:71 hands every undistorted
+ * 8-bit frame to SlamSystem::nextImage, whose tracking / mapping / constraint-search threads call
+ * the four methods above (they live in the lsd-slam fips import, fips.yml:2-4).  The results
+ * leave through OutputIOWrapper (lib/Pangolin_IOWrapper/PangolinOutputIOWrapper.cpp:42-97), which
+ * reads per pyramid level row-major float arrays idepth(lvl), idepthVar(lvl), image(lvl) with
+ * idepth <= 0 meaning "no depth" (lib/Pangolin_IOWrapper/Keyframe.h:95).  lsdg_frame_get_depth and
+ * lsdg_depth_get return exactly that layout.
+ *
+ * Conventions
+ *   - images: row-major float32, pixel centres at integer coordinates; width and height must be
+ *     multiples of 2^(levels-1).
+ *   - pinhole back-projection X = (x - cx) / fx * z (Keyframe.h:86-89,134-136), z = 1 / idepth.
+ *   - pyramid level l+1 is the 2x2 mean of level l; fx_{l+1} = fx_l / 2,
+ *     cx_{l+1} = (cx_l + 0.5) / 2 - 0.5.
+ *   - a pose is 12 doubles, row-major [R | t] (3x4).  "a_to_b" maps a point in camera a's
+ *     coordinates into camera b's.  A Sim3 pose is 13 doubles: [R | t] followed by the scale s
+ *     (x_b = s R x_a + t).
+ *   - every call returns lsdg_status; lsdg_last_error gives a message.  Nothing aborts and no
+ *     C++ exception crosses this boundary.  Host pointers are caller-owned and only read or
+ *     written during the call.  All device memory is owned by the context.
+ *   - calls on one context run in order on the context's CUDA stream and are synchronous unless
+ *     documented otherwise.  Use one context per calling thread (the reference runs tracking,
+ *     mapping and constraint search on separate threads).
+ *
+ * There is no CPU fallback: every compute entry point launches CUDA kernels and fails with
+ * LSDG_CUDA_ERROR when no usable GPU is present.
+ */
+#ifndef LSDG_H_
+#define LSDG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define LSDG_API __attribute__((visibility("default")))
+#else
+#define LSDG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LSDG_MAX_LEVELS 6
+#define LSDG_NE_SIZE 32      /* normal-equation record, see lsdg_se3_normal_equations */
+#define LSDG_NE_SIZE_SIM3 40 /* Sim3 record, see lsdg_sim3_normal_equations */
+
+typedef enum lsdg_status {
+  LSDG_OK = 0,
+  LSDG_INVALID_ARG = 1,
+  LSDG_TRACKING_LOST = 2, /* the pose is still written; quality numbers are in the stats */
+  LSDG_DIVERGED = 3,
+  LSDG_TIMEOUT = 4, /* a bounded device-side wait ran out; the context stays usable */
+  LSDG_CUDA_ERROR = 5,
+  LSDG_OUT_OF_MEMORY = 6,
+  LSDG_NOT_SUPPORTED = 7
+} lsdg_status;
+
+typedef struct lsdg_intrinsics {
+  float fx, fy, cx, cy; /* level 0 */
+} lsdg_intrinsics;
+
+/* Tuning table shared by the kernels and the CPU oracle.  The upstream constants are not
+ * available (the lsd-slam import is not vendored), so this table is the project's own; each
+ * value's meaning is documented here and lsdg_default_params fills it. */
+typedef struct lsdg_params {
+  int32_t levels; /* pyramid levels, 1..LSDG_MAX_LEVELS (default 5) */
+
+  /* ---- direct alignment (SE3 and Sim3) ---- */
+  int32_t max_iterations[LSDG_MAX_LEVELS]; /* LM iterations per level, index = level */
+  float photometric_variance; /* sigma_I^2 of a residual (intensity units^2) */
+  float huber_delta;          /* Huber threshold on the variance-normalised residual */
+  float min_z;                /* warped points with z <= min_z are not used (m) */
+  float lm_lambda_initial;    /* LM damping at the start of each level: A_ii = H_ii (1 + lambda) */
+  float lm_lambda_up;         /* lambda *= up after a rejected step */
+  float lm_lambda_down;       /* lambda *= down after an accepted step */
+  float convergence_eps;      /* a level ends when an accepted step lowers the mean energy by
+                                 less than this fraction */
+  float step_eps;             /* a level ends when max |delta| falls below this */
+  float min_good_ratio;       /* inliers / used points below which tracking is lost */
+  float min_usage;            /* used points / keyframe points below which tracking is lost */
+  float sim3_depth_variance;  /* floor of the inverse-depth residual variance (Sim3) */
+  float sim3_depth_weight;    /* weight of the inverse-depth residual relative to photometric */
+
+  /* ---- depth filter: observeDepth ---- */
+  float min_grad;          /* keyframe gradient magnitude needed to observe a pixel */
+  float min_idepth;        /* search range limits (1/m) */
+  float max_idepth;
+  float epipolar_var;      /* sigma_l^2: variance of the epipolar line position (px^2) */
+  float image_var;         /* sigma_i^2: image noise variance for the photometric disparity error */
+  float min_grad_along_epl2; /* minimum squared cosine between gradient and epipolar line */
+  float max_ssd;           /* mean squared difference per sample above which a match fails */
+  float unique_ratio;      /* the best SSD must be below second-best / unique_ratio */
+  float search_sigmas;     /* search +- this many standard deviations around a hypothesis */
+  float max_search_len;    /* longest epipolar segment searched (px) */
+  float min_search_len;    /* shortest epipolar segment searched (px) */
+  float fuse_chi2;         /* (d_obs - d)^2 / (var + var_obs) above this: inconsistent */
+  float min_epl_length;    /* full-range epipolar segment shorter than this (px): no baseline, skip */
+  int32_t validity_init;   /* validity of a new hypothesis */
+  int32_t validity_max;
+  int32_t validity_penalty; /* subtracted on an inconsistent observation */
+  int32_t blacklist_limit; /* pixels with this many failed matches are no longer observed */
+
+  /* ---- propagateDepth ---- */
+  float prediction_var;    /* added to the propagated variance (1/m^2) */
+  float propagate_max_photo_diff; /* |I_new - I_old| above this drops a propagated hypothesis */
+
+  /* ---- regularizeDepthMap + hole filling ---- */
+  int32_t reg_radius;       /* window half-size */
+  float reg_chi2;           /* neighbour compatible if (d_n - d)^2 <= reg_chi2 (var_n + var) */
+  int32_t reg_min_support;  /* a hypothesis with fewer compatible neighbours is removed */
+  int32_t fill_min_support; /* a hole with at least this many valid neighbours is filled */
+  float fill_var_factor;    /* variance of a filled pixel = factor * neighbours' harmonic mean */
+
+  int32_t reserved[8];
+} lsdg_params;
+
+typedef struct lsdg_track_stats {
+  int32_t status;                       /* lsdg_status of this alignment */
+  int32_t passes[LSDG_MAX_LEVELS];      /* residual passes run per level (1 + iterations) */
+  int32_t total_passes;
+  int32_t n_points;                     /* keyframe points at level 0 */
+  int32_t n_valid;                      /* points that warped into the image (last pass, level 0) */
+  int32_t n_good;                       /* inliers (|r / sigma| <= huber_delta) */
+  float mean_energy;                    /* mean Huber energy of the last accepted pass */
+  float good_ratio;                     /* n_good / n_valid */
+  float usage;                          /* n_valid / n_points */
+  double hessian[28];                   /* upper triangle of J^T W J at the result (21 SE3, 28 Sim3) */
+} lsdg_track_stats;
+
+typedef struct lsdg_ctx lsdg_ctx;
+typedef struct lsdg_frame lsdg_frame;
+typedef struct lsdg_batch lsdg_batch;
+typedef struct lsdg_depthmap lsdg_depthmap;
+
+/* ------------------------------------------------------------------------------------------ */
+/* Context                                                                                     */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Fill the default tuning table (host only, needs no GPU). */
+LSDG_API void lsdg_default_params(lsdg_params* params);
+
+/* ABI version of this header (host only). */
+LSDG_API int32_t lsdg_abi_version(void);
+
+/* Create a context on CUDA device `device` with its own stream.  params may be NULL (defaults). */
+LSDG_API lsdg_status lsdg_create(lsdg_ctx** out, const lsdg_params* params, int device);
+LSDG_API lsdg_status lsdg_destroy(lsdg_ctx* ctx);
+LSDG_API lsdg_status lsdg_set_params(lsdg_ctx* ctx, const lsdg_params* params);
+LSDG_API const char* lsdg_last_error(const lsdg_ctx* ctx);
+/* The context's cudaStream_t (for callers that time or order work around the library). */
+LSDG_API void* lsdg_stream(lsdg_ctx* ctx);
+LSDG_API lsdg_status lsdg_sync(lsdg_ctx* ctx);
+/* Number of kernel launches this context has issued so far (all entry points). */
+LSDG_API int64_t lsdg_launch_count(const lsdg_ctx* ctx);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Frames (upstream Frame: intensity + gradient pyramid, optional keyframe depth)              */
+/* ------------------------------------------------------------------------------------------ */
+
+LSDG_API lsdg_status lsdg_frame_create(lsdg_ctx* ctx, int width, int height, const lsdg_intrinsics* intr,
+                              lsdg_frame** out);
+LSDG_API lsdg_status lsdg_frame_destroy(lsdg_ctx* ctx, lsdg_frame* frame);
+/* Upload a float32 image (host) and build the {I, gx, gy} pyramid on the device. */
+LSDG_API lsdg_status lsdg_frame_upload(lsdg_ctx* ctx, lsdg_frame* frame, const float* image);
+/* Same for an 8-bit image, the type InputThread hands to SlamSystem::nextImage
+ * (lib/App/InputThread.cpp:58-71). */
+LSDG_API lsdg_status lsdg_frame_upload_u8(lsdg_ctx* ctx, lsdg_frame* frame, const uint8_t* image);
+/* Set level-0 inverse depth and its variance (host arrays, idepth <= 0 = none) and build the
+ * depth pyramid and the tracking reference points (SoA float4 {X, Y, Z, I} + float var). */
+LSDG_API lsdg_status lsdg_frame_set_depth(lsdg_ctx* ctx, lsdg_frame* frame, const float* idepth,
+                                 const float* idepth_var);
+/* Read back one pyramid level as float4 {I, gx, gy, 0} per pixel (4 * w_l * h_l floats). */
+LSDG_API lsdg_status lsdg_frame_get_level(lsdg_ctx* ctx, const lsdg_frame* frame, int level, float* out);
+/* Read back one level of the depth pyramid (Frame::idepth(lvl) / idepthVar(lvl) layout). */
+LSDG_API lsdg_status lsdg_frame_get_depth(lsdg_ctx* ctx, const lsdg_frame* frame, int level, float* idepth,
+                                 float* idepth_var);
+/* Read back the tracking reference points of one level: xyzi = 4 floats per point, var = 1. */
+LSDG_API lsdg_status lsdg_frame_get_points(lsdg_ctx* ctx, const lsdg_frame* frame, int level, float* xyzi,
+                                  float* var, int capacity, int* count);
+
+/* ------------------------------------------------------------------------------------------ */
+/* SE3 direct alignment                                                                        */
+/* ------------------------------------------------------------------------------------------ */
+
+/* calculateWarpUpdate at a fixed pose: one residual pass of `reference`'s level-`level` points
+ * warped into `frame` by ref_to_frame.  out[LSDG_NE_SIZE] =
+ *   [0..20]  upper triangle of sum w J^T J (row-major: 00 01 .. 05 11 .. 55)
+ *   [21..26] sum w J^T r
+ *   [27]     sum of Huber energies
+ *   [28]     points used (warped into the image)
+ *   [29]     inliers, [30] outliers, [31] points that left the image or went behind the camera.
+ * J is d r / d xi for the left increment exp(xi) * ref_to_frame, xi = (v, omega). */
+LSDG_API lsdg_status lsdg_se3_normal_equations(lsdg_ctx* ctx, const lsdg_frame* reference,
+                                      const lsdg_frame* frame, int level,
+                                      const double ref_to_frame[12], double out[LSDG_NE_SIZE]);
+
+/* SE3Tracker::trackFrame: align `frame` to the keyframe `reference` (which carries depth),
+ * coarse to fine, starting from frame_to_ref_init.  Writes the refined frame_to_ref and stats.
+ * Returns LSDG_TRACKING_LOST (pose still written) when the quality tests fail. */
+LSDG_API lsdg_status lsdg_track_se3(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame,
+                           const double frame_to_ref_init[12], double frame_to_ref_out[12],
+                           lsdg_track_stats* stats);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Batched alignment: many independent pairs of mixed size, one persistent launch              */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Create a batch of n pairs; pair i has size widths[i] x heights[i] and intrinsics intr[i]. */
+LSDG_API lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int* heights,
+                              const lsdg_intrinsics* intr, lsdg_batch** out);
+LSDG_API lsdg_status lsdg_batch_destroy(lsdg_ctx* ctx, lsdg_batch* batch);
+/* Host -> device copies (asynchronous on the context stream; the host arrays must stay valid
+ * until the next lsdg_sync / lsdg_batch_read).  Each array holds the pairs' planes back to back
+ * in pair order (pair i: widths[i] * heights[i] floats).  init is 12 doubles per pair. */
+LSDG_API lsdg_status lsdg_batch_load(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
+                            const float* ref_idepth, const float* ref_idepth_var,
+                            const float* new_images, const double* frame_to_ref_init);
+/* Device-only step on the loaded inputs: both pyramids of every pair, the reference points and
+ * the persistent LM tracker over all pairs and levels.  Asynchronous; replayed from a CUDA graph
+ * after the first call. */
+LSDG_API lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* batch);
+/* Device -> host results (synchronises the context stream). */
+LSDG_API lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* batch, double* frame_to_ref_out,
+                            lsdg_track_stats* stats);
+/* load + run + read. */
+LSDG_API lsdg_status lsdg_batch_track_se3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
+                                 const float* ref_idepth, const float* ref_idepth_var,
+                                 const float* new_images, const double* frame_to_ref_init,
+                                 double* frame_to_ref_out, lsdg_track_stats* stats);
+/* Device time of the last run's two phases (pyramids + points; the persistent tracker), read from
+ * CUDA events the captured graph records on the context stream.  Synchronises. */
+LSDG_API lsdg_status lsdg_batch_timing(lsdg_ctx* ctx, lsdg_batch* batch, float* build_ms, float* track_ms);
+/* The launch shape the autotuner picked for this batch (threads per CTA, CTAs per cluster, clusters
+ * in the persistent grid) and the kernel launches one lsdg_batch_run issues. */
+LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* threads, int* cluster, int* clusters,
+                             int* launches_per_run);
+/* Residual passes the last lsdg_batch_run executed, summed over pairs and levels, and the
+ * algorithmic bytes those passes read (points + frame levels + sums). */
+LSDG_API lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* batch, int64_t* passes,
+                            double* pass_bytes, double* unique_bytes);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Autotuner                                                                                   */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Entry `index` of the context's tile-shape cache: workload key, threads per CTA, CTAs per
+ * cluster, clusters resident at once, and the tracker time that won.  LSDG_INVALID_ARG past the
+ * end. */
+LSDG_API lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int key_len, int* threads, int* cluster,
+                           int* max_clusters, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LSDG_H_ */

@@ -1,0 +1,594 @@
+// api.cu -- host side of the C-ABI declared in include/lsdg.h: contexts, frames, batches, the
+// CUDA-graph capture of a batch step and the tile-shape autotuner.  No compute happens here; every
+// result comes from the kernels in frame.cu / track.cu / depth.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lsdg_internal.cuh"
+#include "lsdg_host.h"
+
+using namespace lsdg;
+
+namespace lsdg {
+int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
+int launch_frame_points(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
+void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
+cudaError_t launch_track(const TrackArgs& a, int threads, int cluster, int n_clusters, cudaStream_t s);
+int track_max_clusters(int threads, int cluster);
+cudaError_t track_prepare();
+}  // namespace lsdg
+
+// ============================================================================================
+// Context
+// ============================================================================================
+
+lsdg_status ctx_fail(lsdg_ctx* ctx, lsdg_status st, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->err = buf;
+  }
+  return st;
+}
+
+lsdg_status ctx_cuda(lsdg_ctx* ctx, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return LSDG_OK;
+  return ctx_fail(ctx, e == cudaErrorMemoryAllocation ? LSDG_OUT_OF_MEMORY : LSDG_CUDA_ERROR, "%s: %s (%s)", what,
+                  cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+#define CK(ctx, expr)                                         \
+  do {                                                        \
+    lsdg_status _s = ctx_cuda((ctx), (expr), #expr);          \
+    if (_s != LSDG_OK) return _s;                             \
+  } while (0)
+
+extern "C" {
+
+int32_t lsdg_abi_version(void) { return 1; }
+
+void lsdg_default_params(lsdg_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->levels = 5;
+  const int iters[LSDG_MAX_LEVELS] = {6, 8, 10, 12, 16, 16};
+  for (int i = 0; i < LSDG_MAX_LEVELS; ++i) p->max_iterations[i] = iters[i];
+  p->photometric_variance = 16.0f;
+  p->huber_delta = 2.0f;
+  p->min_z = 0.01f;
+  p->lm_lambda_initial = 0.01f;
+  p->lm_lambda_up = 4.0f;
+  p->lm_lambda_down = 0.5f;
+  p->convergence_eps = 1e-3f;
+  p->step_eps = 1e-6f;
+  p->min_good_ratio = 0.5f;
+  p->min_usage = 0.2f;
+  p->sim3_depth_variance = 1e-4f;
+  p->sim3_depth_weight = 1.0f;
+  p->min_grad = 5.0f;
+  p->min_idepth = 0.05f;
+  p->max_idepth = 2.0f;
+  p->epipolar_var = 0.25f;
+  p->image_var = 4.0f;
+  p->min_grad_along_epl2 = 0.1f;
+  p->max_ssd = 100.0f;
+  p->unique_ratio = 1.2f;
+  p->search_sigmas = 2.0f;
+  p->max_search_len = 120.0f;
+  p->min_search_len = 3.0f;
+  p->fuse_chi2 = 6.25f;
+  p->min_epl_length = 1.0f;
+  p->validity_init = 2;
+  p->validity_max = 20;
+  p->validity_penalty = 2;
+  p->blacklist_limit = 5;
+  p->prediction_var = 1e-4f;
+  p->propagate_max_photo_diff = 30.0f;
+  p->reg_radius = 2;
+  p->reg_chi2 = 4.0f;
+  p->reg_min_support = 2;
+  p->fill_min_support = 8;
+  p->fill_var_factor = 2.0f;
+}
+
+static lsdg_status check_params(lsdg_ctx* ctx, const lsdg_params* p) {
+  if (p->levels < 1 || p->levels > LSDG_MAX_LEVELS) return ctx_fail(ctx, LSDG_INVALID_ARG, "levels must be in 1..%d", LSDG_MAX_LEVELS);
+  for (int i = 0; i < LSDG_MAX_LEVELS; ++i)
+    if (p->max_iterations[i] < 0 || p->max_iterations[i] > 1000) return ctx_fail(ctx, LSDG_INVALID_ARG, "max_iterations out of range");
+  if (!(p->photometric_variance > 0) || !(p->huber_delta > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "variance and huber_delta must be > 0");
+  if (p->reg_radius < 0 || p->reg_radius > 4) return ctx_fail(ctx, LSDG_INVALID_ARG, "reg_radius must be in 0..4");
+  if (!(p->max_search_len > 0) || p->max_search_len > 1024) return ctx_fail(ctx, LSDG_INVALID_ARG, "max_search_len must be in (0, 1024]");
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_create(lsdg_ctx** out, const lsdg_params* params, int device) {
+  if (!out) return LSDG_INVALID_ARG;
+  *out = nullptr;
+  lsdg_ctx* ctx = new (std::nothrow) lsdg_ctx();
+  if (!ctx) return LSDG_OUT_OF_MEMORY;
+  if (params) ctx->params = *params;
+  else lsdg_default_params(&ctx->params);
+  lsdg_status st = check_params(ctx, &ctx->params);
+  if (st != LSDG_OK) { delete ctx; return st; }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev <= device || device < 0) {
+    cudaGetLastError();
+    delete ctx;
+    return LSDG_CUDA_ERROR;
+  }
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return LSDG_CUDA_ERROR;
+  }
+  cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+  int cc_major = 0, cc_minor = 0;
+  cudaDeviceGetAttribute(&cc_major, cudaDevAttrComputeCapabilityMajor, device);
+  cudaDeviceGetAttribute(&cc_minor, cudaDevAttrComputeCapabilityMinor, device);
+  if (cc_major != 10 || cc_minor != 3) {
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return LSDG_NOT_SUPPORTED;  // built for sm_103a only
+  }
+  if (track_prepare() != cudaSuccess) cudaGetLastError();  // clusters then stay <= 8 (the tuner sees 0 for 16)
+  if (cudaMalloc(&ctx->d_small, kSmallBytes) != cudaSuccess || cudaMallocHost(&ctx->h_small, kSmallBytes) != cudaSuccess) {
+    cudaGetLastError();
+    if (ctx->d_small) cudaFree(ctx->d_small);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return LSDG_OUT_OF_MEMORY;
+  }
+  *out = ctx;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_destroy(lsdg_ctx* ctx) {
+  if (!ctx) return LSDG_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->d_small) cudaFree(ctx->d_small);
+  if (ctx->h_small) cudaFreeHost(ctx->h_small);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_set_params(lsdg_ctx* ctx, const lsdg_params* p) {
+  if (!ctx || !p) return LSDG_INVALID_ARG;
+  lsdg_status st = check_params(ctx, p);
+  if (st != LSDG_OK) return st;
+  ctx->params = *p;
+  ctx->params_epoch++;
+  return LSDG_OK;
+}
+
+const char* lsdg_last_error(const lsdg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void* lsdg_stream(lsdg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+int64_t lsdg_launch_count(const lsdg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+lsdg_status lsdg_sync(lsdg_ctx* ctx) {
+  if (!ctx) return LSDG_INVALID_ARG;
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================================
+// Frame sets: device storage for n frames of possibly different sizes
+// ============================================================================================
+
+static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, const int* h,
+                           const lsdg_intrinsics* intr, const bool* depth, int levels) {
+  fs.n = n;
+  fs.levels = levels;
+  fs.w.assign(w, w + n);
+  fs.h.assign(h, h + n);
+  fs.intr.assign(intr, intr + n);
+  fs.depth.assign(depth, depth + n);
+  fs.max_pix = 0;
+  const int mult = 1 << (levels - 1);
+  for (int i = 0; i < n; ++i) {
+    if (w[i] <= 0 || h[i] <= 0 || w[i] % mult || h[i] % mult || (w[i] >> (levels - 1)) < 4 || (h[i] >> (levels - 1)) < 4)
+      return ctx_fail(ctx, LSDG_INVALID_ARG, "frame %d: %dx%d must be positive multiples of %d with >= 4 pixels at the top level", i, w[i], h[i], mult);
+    if (!(intr[i].fx > 0) || !(intr[i].fy > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame %d: focal lengths must be > 0", i);
+    fs.max_pix = std::max(fs.max_pix, (long)w[i] * h[i]);
+  }
+  // sections: level-0 intensity of every frame back to back, then level-0 idepth and variance of
+  // the depth frames back to back (so a batch upload is one copy per kind), then per-frame rest.
+  size_t off = 0;
+  std::vector<size_t> o_plane0(n), o_id0(n), o_var0(n);
+  for (int i = 0; i < n; ++i) { o_plane0[i] = off; off += (size_t)w[i] * h[i] * 4; }
+  off = al256(off);
+  fs.off_id0 = off;
+  for (int i = 0; i < n; ++i) if (depth[i]) { o_id0[i] = off; off += (size_t)w[i] * h[i] * 4; }
+  off = al256(off);
+  fs.off_var0 = off;
+  for (int i = 0; i < n; ++i) if (depth[i]) { o_var0[i] = off; off += (size_t)w[i] * h[i] * 4; }
+  off = al256(off);
+  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], blk[kMaxLevels], cnt; };
+  std::vector<Rest> rest(n);
+  for (int i = 0; i < n; ++i) {
+    Rest& r = rest[i];
+    for (int l = 0; l < levels; ++l) {
+      size_t pix = (size_t)(w[i] >> l) * (h[i] >> l);
+      if (l > 0) { r.plane[l] = off; off = al256(off + pix * 4); }
+      r.pyr[l] = off; off = al256(off + pix * 16);
+      if (depth[i]) {
+        if (l > 0) {
+          r.id[l] = off; off = al256(off + pix * 4);
+          r.var[l] = off; off = al256(off + pix * 4);
+        }
+        r.pxyzi[l] = off; off = al256(off + pix * 16);
+        r.pvar[l] = off; off = al256(off + pix * 4);
+        r.blk[l] = off; off = al256(off + ((pix + kCountBlock - 1) / kCountBlock) * 4);
+      }
+    }
+    r.cnt = off;
+    off = al256(off + kMaxLevels * 4);
+  }
+  fs.arena_bytes = off;
+  CK(ctx, cudaMalloc(&fs.arena, off));
+  CK(ctx, cudaMemsetAsync(fs.arena, 0, off, ctx->stream));
+  char* base = (char*)fs.arena;
+  fs.h_frames.assign(n, FrameDev{});
+  for (int i = 0; i < n; ++i) {
+    FrameDev& F = fs.h_frames[i];
+    const Rest& r = rest[i];
+    F.w = w[i];
+    F.h = h[i];
+    F.has_depth = depth[i] ? 1 : 0;
+    F.levels = levels;
+    double fx = intr[i].fx, fy = intr[i].fy, cx = intr[i].cx, cy = intr[i].cy;
+    for (int l = 0; l < levels; ++l) {
+      F.plane[l] = (float*)(base + (l == 0 ? o_plane0[i] : r.plane[l]));
+      F.pyr[l] = (float4*)(base + r.pyr[l]);
+      if (depth[i]) {
+        F.idepth[l] = (float*)(base + (l == 0 ? o_id0[i] : r.id[l]));
+        F.ivar[l] = (float*)(base + (l == 0 ? o_var0[i] : r.var[l]));
+        F.pxyzi[l] = (float4*)(base + r.pxyzi[l]);
+        F.pvar[l] = (float*)(base + r.pvar[l]);
+        F.blk_count[l] = (int*)(base + r.blk[l]);
+      }
+      F.fx[l] = (float)fx; F.fy[l] = (float)fy; F.cx[l] = (float)cx; F.cy[l] = (float)cy;
+      F.fxi[l] = (float)(1.0 / fx); F.fyi[l] = (float)(1.0 / fy);
+      fx *= 0.5; fy *= 0.5;
+      cx = (cx + 0.5) * 0.5 - 0.5;
+      cy = (cy + 0.5) * 0.5 - 0.5;
+    }
+    F.pcount = (int*)(base + r.cnt);
+  }
+  fs.plane0 = (float*)base;
+  fs.pix_total = 0;
+  fs.pix_depth = 0;
+  for (int i = 0; i < n; ++i) {
+    fs.pix_total += (size_t)w[i] * h[i];
+    if (depth[i]) fs.pix_depth += (size_t)w[i] * h[i];
+  }
+  CK(ctx, cudaMalloc(&fs.d_frames, sizeof(FrameDev) * n));
+  CK(ctx, cudaMemcpyAsync(fs.d_frames, fs.h_frames.data(), sizeof(FrameDev) * n, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+void frameset_free(FrameSet& fs) {
+  if (fs.arena) cudaFree(fs.arena);
+  if (fs.d_frames) cudaFree(fs.d_frames);
+  fs.arena = nullptr;
+  fs.d_frames = nullptr;
+}
+
+// ============================================================================================
+// Tracker launch configuration and autotuner
+// ============================================================================================
+
+TrackArgs make_track_args(const lsdg_params& p) {
+  TrackArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.top_level = p.levels - 1;
+  a.bottom_level = 0;
+  for (int i = 0; i < kMaxLevels; ++i) a.max_iter[i] = p.max_iterations[i];
+  a.photometric_variance = p.photometric_variance;
+  a.huber_delta = p.huber_delta;
+  a.min_z = p.min_z;
+  a.lambda0 = p.lm_lambda_initial;
+  a.lambda_up = p.lm_lambda_up;
+  a.lambda_down = p.lm_lambda_down;
+  a.conv_eps = p.convergence_eps;
+  a.step_eps = p.step_eps;
+  a.min_good_ratio = p.min_good_ratio;
+  a.min_usage = p.min_usage;
+  return a;
+}
+
+// Candidate tile shapes: threads per CTA x CTAs per cluster (the cluster owns one pair).
+static const int kCandThreads[] = {128, 256, 512};
+static const int kCandCluster[] = {2, 4, 8, 16};
+
+lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc) {
+  int n_clusters = std::min(a.n_pairs, std::max(1, tc.max_clusters));
+  CK(ctx, cudaMemsetAsync(a.work_counter, 0, sizeof(int), ctx->stream));
+  CK(ctx, launch_track(a, tc.threads, tc.cluster, n_clusters, ctx->stream));
+  ctx->launches += 1;
+  return LSDG_OK;
+}
+
+// Picks (threads, cluster) for a workload signature by timing every feasible candidate on the
+// caller's own data (two runs each, best kept).  The choice is cached per context.
+lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, TuneChoice* out) {
+  auto it = ctx->tune_cache.find(key);
+  if (it != ctx->tune_cache.end()) {
+    *out = it->second;
+    return LSDG_OK;
+  }
+  cudaEvent_t e0, e1;
+  CK(ctx, cudaEventCreate(&e0));
+  CK(ctx, cudaEventCreate(&e1));
+  TuneChoice best;
+  best.threads = 0;
+  float best_ms = 1e30f;
+  for (int nt : kCandThreads)
+    for (int c : kCandCluster) {
+      int mc = track_max_clusters(nt, c);
+      if (mc <= 0) continue;
+      TuneChoice tc{nt, c, mc};
+      float t_best = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        CK(ctx, cudaEventRecord(e0, ctx->stream));
+        lsdg_status st = run_tracker(ctx, a, tc);
+        if (st != LSDG_OK) return st;
+        CK(ctx, cudaEventRecord(e1, ctx->stream));
+        CK(ctx, cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        t_best = std::min(t_best, ms);
+      }
+      if (t_best < best_ms) {
+        best_ms = t_best;
+        best = tc;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best.threads == 0) return ctx_fail(ctx, LSDG_NOT_SUPPORTED, "no cluster launch shape fits this device");
+  best.tuned_ms = best_ms;
+  ctx->tune_cache[key] = best;
+  *out = best;
+  return LSDG_OK;
+}
+
+extern "C" lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int key_len, int* threads, int* cluster,
+                                      int* max_clusters, float* ms) {
+  if (!ctx) return LSDG_INVALID_ARG;
+  int i = 0;
+  for (auto& kv : ctx->tune_cache) {
+    if (i++ != index) continue;
+    if (key && key_len > 0) {
+      std::strncpy(key, kv.first.c_str(), key_len - 1);
+      key[key_len - 1] = 0;
+    }
+    if (threads) *threads = kv.second.threads;
+    if (cluster) *cluster = kv.second.cluster;
+    if (max_clusters) *max_clusters = kv.second.max_clusters;
+    if (ms) *ms = kv.second.tuned_ms;
+    return LSDG_OK;
+  }
+  return LSDG_INVALID_ARG;
+}
+
+// ============================================================================================
+// Single frames
+// ============================================================================================
+extern "C" {
+
+lsdg_status lsdg_frame_create(lsdg_ctx* ctx, int width, int height, const lsdg_intrinsics* intr, lsdg_frame** out) {
+  if (!ctx || !intr || !out) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  *out = nullptr;
+  CK(ctx, cudaSetDevice(ctx->device));
+  lsdg_frame* f = new (std::nothrow) lsdg_frame();
+  if (!f) return LSDG_OUT_OF_MEMORY;
+  bool depth = true;
+  lsdg_status st = frameset_alloc(ctx, f->fs, 1, &width, &height, intr, &depth, ctx->params.levels);
+  if (st != LSDG_OK) {
+    frameset_free(f->fs);
+    delete f;
+    return st;
+  }
+  f->fs.h_frames[0].has_depth = 0;  // until lsdg_frame_set_depth
+  CK(ctx, cudaMemcpyAsync(f->fs.d_frames, f->fs.h_frames.data(), sizeof(FrameDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = f;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_destroy(lsdg_ctx* ctx, lsdg_frame* f) {
+  if (!ctx || !f) return LSDG_INVALID_ARG;
+  cudaStreamSynchronize(ctx->stream);
+  frameset_free(f->fs);
+  delete f;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_upload(lsdg_ctx* ctx, lsdg_frame* f, const float* image) {
+  if (!ctx || !f || !image) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  const FrameDev& F = f->fs.h_frames[0];
+  CK(ctx, cudaMemcpyAsync(F.plane[0], image, (size_t)F.w * F.h * 4, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->launches += launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, ctx->stream);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  f->has_image = true;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_upload_u8(lsdg_ctx* ctx, lsdg_frame* f, const uint8_t* image) {
+  if (!ctx || !f || !image) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  const FrameDev& F = f->fs.h_frames[0];
+  size_t n = (size_t)F.w * F.h;
+  // stage the bytes in the (not yet built) level-0 gradient plane, which is 16x larger
+  uint8_t* tmp = (uint8_t*)F.pyr[0];
+  CK(ctx, cudaMemcpyAsync(tmp, image, n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_u8_to_plane(tmp, F.plane[0], (int)n, ctx->stream);
+  ctx->launches += 1 + launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, ctx->stream);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  f->has_image = true;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_set_depth(lsdg_ctx* ctx, lsdg_frame* f, const float* idepth, const float* var) {
+  if (!ctx || !f || !idepth || !var) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (!f->has_image) return ctx_fail(ctx, LSDG_INVALID_ARG, "upload the keyframe image before its depth");
+  FrameDev& F = f->fs.h_frames[0];
+  F.has_depth = 1;
+  CK(ctx, cudaMemcpyAsync(f->fs.d_frames, &F, sizeof(FrameDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(F.idepth[0], idepth, (size_t)F.w * F.h * 4, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(F.ivar[0], var, (size_t)F.w * F.h * 4, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->launches += launch_frame_points(f->fs.d_frames, 1, F.levels, f->fs.max_pix, ctx->stream);
+  CK(ctx, cudaGetLastError());
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_get_level(lsdg_ctx* ctx, const lsdg_frame* f, int level, float* out) {
+  if (!ctx || !f || !out) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  const FrameDev& F = f->fs.h_frames[0];
+  if (level < 0 || level >= F.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
+  size_t n = (size_t)(F.w >> level) * (F.h >> level);
+  CK(ctx, cudaMemcpyAsync(out, F.pyr[level], n * 16, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_get_depth(lsdg_ctx* ctx, const lsdg_frame* f, int level, float* idepth, float* var) {
+  if (!ctx || !f) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  const FrameDev& F = f->fs.h_frames[0];
+  if (!F.has_depth) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame has no depth");
+  if (level < 0 || level >= F.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
+  size_t n = (size_t)(F.w >> level) * (F.h >> level);
+  if (idepth) CK(ctx, cudaMemcpyAsync(idepth, F.idepth[level], n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  if (var) CK(ctx, cudaMemcpyAsync(var, F.ivar[level], n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_frame_get_points(lsdg_ctx* ctx, const lsdg_frame* f, int level, float* xyzi, float* var, int capacity,
+                                  int* count) {
+  if (!ctx || !f || !count) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  const FrameDev& F = f->fs.h_frames[0];
+  if (!F.has_depth) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame has no depth");
+  if (level < 0 || level >= F.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
+  int c = 0;
+  CK(ctx, cudaMemcpyAsync(ctx->h_small, F.pcount + level, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  std::memcpy(&c, ctx->h_small, 4);
+  *count = c;
+  if (c > capacity) return ctx_fail(ctx, LSDG_INVALID_ARG, "capacity %d < %d points", capacity, c);
+  if (xyzi && c) CK(ctx, cudaMemcpyAsync(xyzi, F.pxyzi[level], (size_t)c * 16, cudaMemcpyDeviceToHost, ctx->stream));
+  if (var && c) CK(ctx, cudaMemcpyAsync(var, F.pvar[level], (size_t)c * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+}  // extern "C"
+
+// ============================================================================================
+// One-pair tracking and fixed-pose normal equations
+// ============================================================================================
+
+// Small-transfer layout inside ctx->d_small / h_small.
+struct SmallLayout {
+  PairDev pair;
+  int work;
+  int pad;
+  double init[12];
+  double out_pose[12];
+  double out_sums[32];
+  lsdg_track_stats stats;
+};
+static_assert(sizeof(SmallLayout) <= kSmallBytes, "small staging buffer too small");
+
+static lsdg_status track_one(lsdg_ctx* ctx, const lsdg_frame* ref, const lsdg_frame* cur, const double* init,
+                             bool init_is_ref_to_frame, int top, int bottom, bool eval_only, double* pose_out,
+                             lsdg_track_stats* stats, double* sums) {
+  if (!ref->fs.h_frames[0].has_depth) return ctx_fail(ctx, LSDG_INVALID_ARG, "reference frame has no depth");
+  if (!cur->has_image || !ref->has_image) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame image not uploaded");
+  const FrameDev& R = ref->fs.h_frames[0];
+  const FrameDev& Cf = cur->fs.h_frames[0];
+  if (R.w != Cf.w || R.h != Cf.h) return ctx_fail(ctx, LSDG_INVALID_ARG, "reference and frame sizes differ");
+  SmallLayout* hs = (SmallLayout*)ctx->h_small;
+  SmallLayout* ds = (SmallLayout*)ctx->d_small;
+  hs->pair.ref = ref->fs.d_frames;
+  hs->pair.cur = cur->fs.d_frames;
+  std::memcpy(hs->init, init, sizeof(hs->init));
+  CK(ctx, cudaMemcpyAsync(ds, hs, offsetof(SmallLayout, out_pose), cudaMemcpyHostToDevice, ctx->stream));
+  TrackArgs a = make_track_args(ctx->params);
+  a.pairs = &ds->pair;
+  a.order = nullptr;
+  a.n_pairs = 1;
+  a.work_counter = &ds->work;
+  a.init = ds->init;
+  a.init_is_ref_to_frame = init_is_ref_to_frame ? 1 : 0;
+  a.out_pose = ds->out_pose;
+  a.out_stats = &ds->stats;
+  a.out_sums = ds->out_sums;
+  a.top_level = top;
+  a.bottom_level = bottom;
+  if (eval_only)
+    for (int i = 0; i < kMaxLevels; ++i) a.max_iter[i] = 0;
+  char key[64];
+  std::snprintf(key, sizeof(key), "one:%dx%d", R.w, R.h);
+  TuneChoice tc;
+  if (eval_only) {
+    tc = TuneChoice{256, 8, 1};  // a single pass: any shape, deterministic for the parity tests
+  } else {
+    lsdg_status st = autotune(ctx, key, a, &tc);
+    if (st != LSDG_OK) return st;
+  }
+  lsdg_status st = run_tracker(ctx, a, tc);
+  if (st != LSDG_OK) return st;
+  CK(ctx, cudaMemcpyAsync(&hs->out_pose, &ds->out_pose, sizeof(SmallLayout) - offsetof(SmallLayout, out_pose),
+                          cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (pose_out) std::memcpy(pose_out, hs->out_pose, sizeof(hs->out_pose));
+  if (stats) *stats = hs->stats;
+  if (sums) std::memcpy(sums, hs->out_sums, sizeof(hs->out_sums));
+  return (lsdg_status)hs->stats.status;
+}
+
+extern "C" {
+
+lsdg_status lsdg_se3_normal_equations(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame, int level,
+                                      const double ref_to_frame[12], double out[LSDG_NE_SIZE]) {
+  if (!ctx || !reference || !frame || !ref_to_frame || !out) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (level < 0 || level >= ctx->params.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
+  double sums[32];
+  lsdg_status st = track_one(ctx, reference, frame, ref_to_frame, true, level, level, true, nullptr, nullptr, sums);
+  if (st != LSDG_OK && st != LSDG_TRACKING_LOST) return st;
+  std::memcpy(out, sums, sizeof(double) * LSDG_NE_SIZE);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_track_se3(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame,
+                           const double frame_to_ref_init[12], double frame_to_ref_out[12], lsdg_track_stats* stats) {
+  if (!ctx || !reference || !frame || !frame_to_ref_init || !frame_to_ref_out)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  return track_one(ctx, reference, frame, frame_to_ref_init, false, ctx->params.levels - 1, 0, false, frame_to_ref_out,
+                   stats, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,300 @@
+// batch.cu -- batched alignment of many independent frame pairs of mixed size (a11).
+//
+// A batch owns one arena with 2n frames: frames 0..n-1 are the keyframes (with depth), n..2n-1 the
+// frames to track.  The level-0 inputs of all pairs sit back to back per kind, so a batch upload is
+// four host->device copies.  lsdg_batch_run is one CUDA graph: image pyramids of all 2n frames,
+// depth pyramids + point compaction of the keyframes, then ONE persistent cluster launch that runs
+// every pair's full coarse-to-fine LM loop on the device (pairs taken largest first from an atomic
+// queue).  The graph is captured after the autotuner has picked the (threads, cluster) shape for
+// the batch's size mix, and it is recaptured when the parameters change.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "lsdg_host.h"
+
+using namespace lsdg;
+
+namespace lsdg {
+int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
+int launch_frame_points(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
+}  // namespace lsdg
+
+#define CK(ctx, expr)                                         \
+  do {                                                        \
+    lsdg_status _s = ctx_cuda((ctx), (expr), #expr);          \
+    if (_s != LSDG_OK) return _s;                             \
+  } while (0)
+
+struct lsdg_batch {
+  int n = 0;
+  FrameSet fs;
+  PairDev* d_pairs = nullptr;
+  int* d_order = nullptr;
+  double* d_init = nullptr;
+  double* d_out = nullptr;
+  lsdg_track_stats* d_stats = nullptr;
+  int* d_work = nullptr;
+  double* h_out = nullptr;
+  lsdg_track_stats* h_stats = nullptr;
+  int* h_counts = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int graph_epoch = -1;
+  int launches_per_run = 0;
+  TuneChoice tc;
+  std::string key;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // run start, build done, track done
+  bool ran = false;
+};
+
+static void batch_free(lsdg_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  frameset_free(b->fs);
+  if (b->d_pairs) cudaFree(b->d_pairs);
+  if (b->d_order) cudaFree(b->d_order);
+  if (b->d_init) cudaFree(b->d_init);
+  if (b->d_out) cudaFree(b->d_out);
+  if (b->d_stats) cudaFree(b->d_stats);
+  if (b->d_work) cudaFree(b->d_work);
+  if (b->h_out) cudaFreeHost(b->h_out);
+  if (b->h_stats) cudaFreeHost(b->h_stats);
+  if (b->h_counts) cudaFreeHost(b->h_counts);
+  for (auto& e : b->ev)
+    if (e) cudaEventDestroy(e);
+  delete b;
+}
+
+static lsdg_status batch_track_args(lsdg_ctx* ctx, lsdg_batch* b, TrackArgs* a) {
+  *a = make_track_args(ctx->params);
+  a->pairs = b->d_pairs;
+  a->order = b->d_order;
+  a->n_pairs = b->n;
+  a->work_counter = b->d_work;
+  a->init = b->d_init;
+  a->init_is_ref_to_frame = 0;
+  a->out_pose = b->d_out;
+  a->out_stats = b->d_stats;
+  a->out_sums = nullptr;
+  return LSDG_OK;
+}
+
+static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, int* launches) {
+  const int L = ctx->params.levels;
+  int k = launch_frame_pyramid(b->fs.d_frames, 2 * b->n, L, b->fs.max_pix, ctx->stream);
+  k += launch_frame_points(b->fs.d_frames, b->n, L, b->fs.max_pix, ctx->stream);
+  CK(ctx, cudaGetLastError());
+  *launches = k;
+  return LSDG_OK;
+}
+
+extern "C" {
+
+lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
+                              lsdg_batch** out) {
+  if (!ctx || !widths || !heights || !intr || !out || n <= 0) return ctx_fail(ctx, LSDG_INVALID_ARG, "bad batch arguments");
+  *out = nullptr;
+  CK(ctx, cudaSetDevice(ctx->device));
+  lsdg_batch* b = new (std::nothrow) lsdg_batch();
+  if (!b) return LSDG_OUT_OF_MEMORY;
+  b->n = n;
+  std::vector<int> w(2 * n), h(2 * n);
+  std::vector<lsdg_intrinsics> k(2 * n);
+  bool* dep = new bool[2 * n];
+  for (int i = 0; i < n; ++i) {
+    w[i] = w[n + i] = widths[i];
+    h[i] = h[n + i] = heights[i];
+    k[i] = k[n + i] = intr[i];
+    dep[i] = true;
+    dep[n + i] = false;
+  }
+  lsdg_status st = frameset_alloc(ctx, b->fs, 2 * n, w.data(), h.data(), k.data(), dep, ctx->params.levels);
+  delete[] dep;
+  if (st != LSDG_OK) {
+    batch_free(b);
+    return st;
+  }
+  std::vector<PairDev> pairs(n);
+  for (int i = 0; i < n; ++i) pairs[i] = PairDev{b->fs.d_frames + i, b->fs.d_frames + n + i};
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int c) { return (long)widths[a] * heights[a] > (long)widths[c] * heights[c]; });
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(PairDev) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_order, sizeof(int) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_init, sizeof(double) * 12 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_out, sizeof(double) * 12 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_stats, sizeof(lsdg_track_stats) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_work, sizeof(int) * 4);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_out, sizeof(double) * 12 * n);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_stats, sizeof(lsdg_track_stats) * n);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_counts, sizeof(int) * kMaxLevels * n);
+  for (auto& ev : b->ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&ev);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_pairs, pairs.data(), sizeof(PairDev) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    st = ctx_cuda(ctx, e, "batch allocation");
+    batch_free(b);
+    return st;
+  }
+  // autotuner key: the multiset of sizes
+  std::vector<std::pair<int, int>> sz(n);
+  for (int i = 0; i < n; ++i) sz[i] = {widths[i], heights[i]};
+  std::sort(sz.begin(), sz.end());
+  std::string key = "batch:";
+  for (int i = 0; i < n;) {
+    int j = i;
+    while (j < n && sz[j] == sz[i]) ++j;
+    key += std::to_string(j - i) + "x" + std::to_string(sz[i].first) + "x" + std::to_string(sz[i].second) + ";";
+    i = j;
+  }
+  b->key = key;
+  *out = b;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_destroy(lsdg_ctx* ctx, lsdg_batch* b) {
+  if (!ctx || !b) return LSDG_INVALID_ARG;
+  cudaStreamSynchronize(ctx->stream);
+  batch_free(b);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_load(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
+                            const float* ref_var, const float* new_images, const double* init) {
+  if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !init)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  const size_t half = b->fs.pix_depth * 4;  // the keyframes come first, all with depth
+  char* base = (char*)b->fs.arena;
+  CK(ctx, cudaMemcpyAsync(b->fs.plane0, ref_images, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync((char*)b->fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(b->d_init, init, sizeof(double) * 12 * b->n, cudaMemcpyHostToDevice, ctx->stream));
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
+  if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (!b->exec || b->graph_epoch != ctx->params_epoch) {
+    if (b->exec) {
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    // eager build so that the autotuner times the tracker on this batch's real points
+    int k = 0;
+    lsdg_status st = enqueue_build(ctx, b, &k);
+    if (st != LSDG_OK) return st;
+    ctx->launches += k;
+    TrackArgs a;
+    batch_track_args(ctx, b, &a);
+    st = autotune(ctx, b->key, a, &b->tc);
+    if (st != LSDG_OK) return st;
+    // capture: events, build, tracker
+    CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int nl = 0;
+    cudaEventRecord(b->ev[0], ctx->stream);
+    st = enqueue_build(ctx, b, &nl);
+    cudaEventRecord(b->ev[1], ctx->stream);
+    int64_t before = ctx->launches;
+    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc);
+    nl += (int)(ctx->launches - before);
+    ctx->launches = before;
+    cudaEventRecord(b->ev[2], ctx->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (st != LSDG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    CK(ctx, e);
+    e = cudaGraphInstantiate(&b->exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ctx, e);
+    b->launches_per_run = nl;
+    b->graph_epoch = ctx->params_epoch;
+  }
+  CK(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+  ctx->launches += b->launches_per_run;
+  b->ran = true;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* b, double* out, lsdg_track_stats* stats) {
+  if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  CK(ctx, cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * 12 * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (out) std::memcpy(out, b->h_out, sizeof(double) * 12 * b->n);
+  if (stats) std::memcpy(stats, b->h_stats, sizeof(lsdg_track_stats) * b->n);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_track_se3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
+                                 const float* ref_var, const float* new_images, const double* init, double* out,
+                                 lsdg_track_stats* stats) {
+  lsdg_status st = lsdg_batch_load(ctx, b, ref_images, ref_idepth, ref_var, new_images, init);
+  if (st != LSDG_OK) return st;
+  st = lsdg_batch_run(ctx, b);
+  if (st != LSDG_OK) return st;
+  return lsdg_batch_read(ctx, b, out, stats);
+}
+
+// Device time of the last run's two phases (pyramids + points, tracker), from the events the
+// graph records on the context stream.  Synchronises.
+lsdg_status lsdg_batch_timing(lsdg_ctx* ctx, lsdg_batch* b, float* build_ms, float* track_ms) {
+  if (!ctx || !b || !b->ran) return ctx_fail(ctx, LSDG_INVALID_ARG, "no run to time");
+  CK(ctx, cudaEventSynchronize(b->ev[2]));
+  float a = 0, c = 0;
+  CK(ctx, cudaEventElapsedTime(&a, b->ev[0], b->ev[1]));
+  CK(ctx, cudaEventElapsedTime(&c, b->ev[1], b->ev[2]));
+  if (build_ms) *build_ms = a;
+  if (track_ms) *track_ms = c;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* b, int64_t* passes, double* pass_bytes, double* unique_bytes) {
+  if (!ctx || !b || !b->ran) return ctx_fail(ctx, LSDG_INVALID_ARG, "no run to account");
+  const int L = ctx->params.levels;
+  for (int i = 0; i < b->n; ++i)
+    CK(ctx, cudaMemcpyAsync(b->h_counts + kMaxLevels * i, b->fs.h_frames[i].pcount, sizeof(int) * kMaxLevels,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  int64_t np = 0;
+  double pb = 0, ub = 0;
+  for (int i = 0; i < b->n; ++i) {
+    for (int l = 0; l < L; ++l) {
+      const double pts = b->h_counts[kMaxLevels * i + l];
+      const double pix = (double)(b->fs.w[i] >> l) * (b->fs.h[i] >> l);
+      const int ps = b->h_stats[i].passes[l];
+      np += ps;
+      // per pass: points (float4 + float) + the frame level's I, gx, gy + the 27 sums
+      pb += ps * (pts * 20.0 + pix * 12.0 + 27 * 4.0);
+      if (ps > 0) ub += pts * 20.0 + pix * 12.0;
+    }
+  }
+  if (passes) *passes = np;
+  if (pass_bytes) *pass_bytes = pb;
+  if (unique_bytes) *unique_bytes = ub;
+  return LSDG_OK;
+}
+
+// The tile shape the autotuner chose for this batch.
+lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* b, int* threads, int* cluster, int* clusters, int* launches_per_run) {
+  if (!ctx || !b) return LSDG_INVALID_ARG;
+  if (threads) *threads = b->tc.threads;
+  if (cluster) *cluster = b->tc.cluster;
+  if (clusters) *clusters = std::min(b->n, b->tc.max_clusters);
+  if (launches_per_run) *launches_per_run = b->launches_per_run;
+  return LSDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,64 @@
+// lsdg_internal.cuh -- device-side data layout shared by the kernels and the C-ABI host code.
+//
+// HBM layout (one "frame" = one camera image with its pyramid; a keyframe also carries depth):
+//   plane[l]   float  [h_l * w_l]   intensity of level l (level 0 is the upload target)
+//   pyr[l]     float4 [h_l * w_l]   {I, gx, gy, 0}: one 16-byte load gives everything bilinear
+//                                   sampling of intensity and gradient needs at one corner
+//   idepth[l], ivar[l]  float [h_l * w_l]  keyframe depth pyramid (idepth <= 0: none)
+//   pxyzi[l]   float4 [n_l]         tracking reference points, SoA: {X, Y, Z, I_keyframe}
+//   pvar[l]    float  [n_l]         inverse-depth variance of each point
+//   pcount[l]  int                  n_l, written on the device by the compaction
+// All per-pixel planes are row-major and 256-byte aligned.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lsdg.h"
+
+namespace lsdg {
+
+constexpr int kMaxLevels = LSDG_MAX_LEVELS;
+constexpr int kCountBlock = 256;  // pixels per block of the point compaction
+
+struct FrameDev {
+  int w, h;  // level 0
+  int has_depth;
+  int levels;
+  float* plane[kMaxLevels];
+  float4* pyr[kMaxLevels];
+  float* idepth[kMaxLevels];
+  float* ivar[kMaxLevels];
+  float4* pxyzi[kMaxLevels];
+  float* pvar[kMaxLevels];
+  int* pcount;                   // [kMaxLevels]
+  int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per block, then offsets
+  float fx[kMaxLevels], fy[kMaxLevels], cx[kMaxLevels], cy[kMaxLevels];
+  float fxi[kMaxLevels], fyi[kMaxLevels];
+};
+
+struct PairDev {
+  const FrameDev* ref;   // keyframe (carries depth and points)
+  const FrameDev* cur;   // frame being tracked
+};
+
+// Tracker launch arguments (kernel parameter, passed by value).
+struct TrackArgs {
+  const PairDev* pairs;
+  const int* order;          // processing order (largest first); nullptr = identity
+  int n_pairs;
+  int* work_counter;         // zeroed before the launch
+  const double* init;        // 12 per pair: frame_to_ref, or ref_to_frame if init_is_ref_to_frame
+  int init_is_ref_to_frame;
+  double* out_pose;          // 12 per pair: frame_to_ref
+  lsdg_track_stats* out_stats;
+  double* out_sums;          // optional: 32 per pair, the last accepted pass at the bottom level
+  int top_level;             // first (coarsest) level to run
+  int bottom_level;          // last level to run
+  int max_iter[kMaxLevels];
+  float photometric_variance, huber_delta, min_z;
+  double lambda0, lambda_up, lambda_down, conv_eps, step_eps;
+  float min_good_ratio, min_usage;
+};
+
+}  // namespace lsdg

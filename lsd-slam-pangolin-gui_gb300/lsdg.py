@@ -1,0 +1,322 @@
+"""Python view of the C-ABI (include/lsdg.h) through ctypes.
+
+The classes mirror the upstream objects the reference's threads use:
+``Frame`` (Frame: pyramid + optional keyframe depth), ``SE3Tracker.trackFrame``,
+``Batch`` (many trackFrame calls in one persistent launch) and ``DepthMap``
+(updateKeyframe / createKeyFrame / regularize).  Every call goes to liblsdg.so, whose kernels run
+on the GPU; there is no CPU fallback and importing fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+import lsdg_types as T
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblsdg.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "lsdg.h")
+
+_lib = None
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+
+
+class LsdgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{T.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _sig(L, name, restype, argtypes):
+    f = getattr(L, name)
+    f.restype = restype
+    f.argtypes = argtypes
+
+
+def lib():
+    """Load liblsdg.so (built by build_lib.py).  Raises if it is absent: no fallback exists."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"liblsdg.so not built ({LIB_PATH}); run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    st = C.c_int
+    _sig(L, "lsdg_abi_version", C.c_int32, [])
+    _sig(L, "lsdg_default_params", None, [C.POINTER(T.Params)])
+    _sig(L, "lsdg_create", st, [C.POINTER(_vp), C.POINTER(T.Params), C.c_int])
+    _sig(L, "lsdg_destroy", st, [_vp])
+    _sig(L, "lsdg_set_params", st, [_vp, C.POINTER(T.Params)])
+    _sig(L, "lsdg_last_error", C.c_char_p, [_vp])
+    _sig(L, "lsdg_stream", _vp, [_vp])
+    _sig(L, "lsdg_sync", st, [_vp])
+    _sig(L, "lsdg_launch_count", C.c_int64, [_vp])
+    _sig(L, "lsdg_frame_create", st, [_vp, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
+    _sig(L, "lsdg_frame_destroy", st, [_vp, _vp])
+    _sig(L, "lsdg_frame_upload", st, [_vp, _vp, _f32p])
+    _sig(L, "lsdg_frame_upload_u8", st, [_vp, _vp, _u8p])
+    _sig(L, "lsdg_frame_set_depth", st, [_vp, _vp, _f32p, _f32p])
+    _sig(L, "lsdg_frame_get_level", st, [_vp, _vp, C.c_int, _f32p])
+    _sig(L, "lsdg_frame_get_depth", st, [_vp, _vp, C.c_int, _f32p, _f32p])
+    _sig(L, "lsdg_frame_get_points", st, [_vp, _vp, C.c_int, _f32p, _f32p, C.c_int, C.POINTER(C.c_int)])
+    _sig(L, "lsdg_se3_normal_equations", st, [_vp, _vp, _vp, C.c_int, _f64p, _f64p])
+    _sig(L, "lsdg_track_se3", st, [_vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
+    _sig(L, "lsdg_batch_create", st, [_vp, C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
+    _sig(L, "lsdg_batch_destroy", st, [_vp, _vp])
+    _sig(L, "lsdg_batch_load", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p])
+    _sig(L, "lsdg_batch_run", st, [_vp, _vp])
+    _sig(L, "lsdg_batch_read", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
+    _sig(L, "lsdg_batch_track_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
+    _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
+    _sig(L, "lsdg_batch_shape", st, [_vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)])
+    _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
+    _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(C.c_int), C.POINTER(C.c_float)])
+    _lib = L
+    return L
+
+
+def default_params() -> T.Params:
+    p = T.Params()
+    lib().lsdg_default_params(C.byref(p))
+    return p
+
+
+def intrinsics(intr) -> T.Intrinsics:
+    if isinstance(intr, T.Intrinsics):
+        return intr
+    fx, fy, cx, cy = intr.as_tuple() if hasattr(intr, "as_tuple") else intr
+    return T.Intrinsics(fx, fy, cx, cy)
+
+
+def _pose12(p) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(p, np.float64).reshape(-1))
+    assert a.size == 12
+    return a
+
+
+class Context:
+    """One CUDA stream on one device (upstream: one of SlamSystem's threads)."""
+
+    def __init__(self, params: T.Params = None, device: int = 0):
+        self._h = _vp()
+        self.params = (params or default_params()).copy()
+        rc = lib().lsdg_create(C.byref(self._h), C.byref(self.params), device)
+        if rc != T.OK:
+            raise LsdgError(rc, "lsdg_create failed")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, rc: int, allow=(T.OK,)):
+        if rc not in allow:
+            raise LsdgError(rc, (lib().lsdg_last_error(self._h) or b"").decode())
+        return rc
+
+    def set_params(self, p: T.Params):
+        self.check(lib().lsdg_set_params(self._h, C.byref(p)))
+        self.params = p.copy()
+
+    def stream_ptr(self) -> int:
+        return lib().lsdg_stream(self._h) or 0
+
+    def sync(self):
+        self.check(lib().lsdg_sync(self._h))
+
+    def launch_count(self) -> int:
+        return int(lib().lsdg_launch_count(self._h))
+
+    def tune_table(self):
+        out, i = [], 0
+        buf = C.create_string_buffer(256)
+        while True:
+            t, c, m, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+            rc = lib().lsdg_tune_info(self._h, i, buf, 256, C.byref(t), C.byref(c), C.byref(m), C.byref(ms))
+            if rc != T.OK:
+                return out
+            out.append({"key": buf.value.decode(), "threads": t.value, "cluster": c.value, "clusters": m.value, "ms": ms.value})
+            i += 1
+
+    def close(self):
+        if self._h:
+            lib().lsdg_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Frame:
+    """Upstream Frame: intensity + gradient pyramid; a keyframe also carries inverse depth."""
+
+    def __init__(self, ctx: Context, width: int, height: int, intr):
+        self.ctx, self.w, self.h = ctx, width, height
+        self.levels = ctx.params.levels
+        self._h = _vp()
+        self._k = intrinsics(intr)
+        ctx.check(lib().lsdg_frame_create(ctx.handle, width, height, C.byref(self._k), C.byref(self._h)))
+
+    @property
+    def handle(self):
+        return self._h
+
+    def upload(self, image: np.ndarray):
+        if image.dtype == np.uint8:
+            self.ctx.check(lib().lsdg_frame_upload_u8(self.ctx.handle, self._h, np.ascontiguousarray(image)))
+        else:
+            self.ctx.check(lib().lsdg_frame_upload(self.ctx.handle, self._h, np.ascontiguousarray(image, np.float32)))
+        return self
+
+    def set_depth(self, idepth: np.ndarray, idepth_var: np.ndarray):
+        self.ctx.check(lib().lsdg_frame_set_depth(self.ctx.handle, self._h, np.ascontiguousarray(idepth, np.float32),
+                                                  np.ascontiguousarray(idepth_var, np.float32)))
+        return self
+
+    def level(self, l: int) -> np.ndarray:
+        out = np.zeros(((self.h >> l), (self.w >> l), 4), np.float32)
+        self.ctx.check(lib().lsdg_frame_get_level(self.ctx.handle, self._h, l, out.reshape(-1)))
+        return out
+
+    def depth(self, l: int):
+        d = np.zeros(((self.h >> l), (self.w >> l)), np.float32)
+        v = np.zeros_like(d)
+        self.ctx.check(lib().lsdg_frame_get_depth(self.ctx.handle, self._h, l, d.reshape(-1), v.reshape(-1)))
+        return d, v
+
+    def points(self, l: int):
+        cap = (self.w >> l) * (self.h >> l)
+        xyzi = np.zeros(4 * cap, np.float32)
+        var = np.zeros(cap, np.float32)
+        n = C.c_int()
+        self.ctx.check(lib().lsdg_frame_get_points(self.ctx.handle, self._h, l, xyzi, var, cap, C.byref(n)))
+        return xyzi[:4 * n.value].reshape(-1, 4), var[:n.value]
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().lsdg_frame_destroy(self.ctx.handle, self._h)
+        self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def se3_normal_equations(ctx: Context, reference: Frame, frame: Frame, level: int, ref_to_frame) -> np.ndarray:
+    """calculateWarpUpdate at a fixed pose: the LSDG_NE_SIZE record (see include/lsdg.h)."""
+    out = np.zeros(T.NE_SIZE, np.float64)
+    ctx.check(lib().lsdg_se3_normal_equations(ctx.handle, reference.handle, frame.handle, level, _pose12(ref_to_frame), out))
+    return out
+
+
+class SE3Tracker:
+    """Upstream SE3Tracker: trackFrame(reference, frame, frameToReference_initialEstimate)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.last_stats = T.TrackStats()
+
+    def trackFrame(self, reference: Frame, frame: Frame, frame_to_ref_init=None):
+        init = _pose12(np.eye(3, 4) if frame_to_ref_init is None else frame_to_ref_init)
+        out = np.zeros(12, np.float64)
+        st = T.TrackStats()
+        self.ctx.check(lib().lsdg_track_se3(self.ctx.handle, reference.handle, frame.handle, init, out, C.byref(st)),
+                       allow=(T.OK, T.TRACKING_LOST))
+        self.last_stats = st
+        return out.reshape(3, 4), st
+
+
+class Batch:
+    """Many independent trackFrame calls of mixed size in one persistent launch (graph-captured)."""
+
+    def __init__(self, ctx: Context, widths, heights, intrs):
+        self.ctx = ctx
+        self.n = len(widths)
+        self.widths = np.ascontiguousarray(widths, np.int32)
+        self.heights = np.ascontiguousarray(heights, np.int32)
+        self._k = (T.Intrinsics * self.n)(*[intrinsics(k) for k in intrs])
+        self._h = _vp()
+        ctx.check(lib().lsdg_batch_create(ctx.handle, self.n, self.widths, self.heights, self._k, C.byref(self._h)))
+        self.npix = int(np.sum(self.widths.astype(np.int64) * self.heights))
+
+    @staticmethod
+    def _ptr(a: np.ndarray):
+        assert a.flags["C_CONTIGUOUS"] and a.dtype == np.float32
+        return a.ctypes.data
+
+    def load(self, ref_images, ref_idepth, ref_var, new_images, init):
+        """Host arrays (ideally pinned) holding the pairs' planes back to back; init (n,3,4)."""
+        for a in (ref_images, ref_idepth, ref_var, new_images):
+            assert a.size == self.npix, (a.size, self.npix)
+        self._keep = (ref_images, ref_idepth, ref_var, new_images)
+        self.ctx.check(lib().lsdg_batch_load(self.ctx.handle, self._h, self._ptr(ref_images), self._ptr(ref_idepth),
+                                             self._ptr(ref_var), self._ptr(new_images),
+                                             np.ascontiguousarray(init, np.float64).reshape(-1)))
+
+    def run(self):
+        self.ctx.check(lib().lsdg_batch_run(self.ctx.handle, self._h))
+
+    def read(self):
+        out = np.zeros(12 * self.n, np.float64)
+        stats = (T.TrackStats * self.n)()
+        self.ctx.check(lib().lsdg_batch_read(self.ctx.handle, self._h, out, stats))
+        return out.reshape(self.n, 3, 4), stats
+
+    def track(self, ref_images, ref_idepth, ref_var, new_images, init):
+        out = np.zeros(12 * self.n, np.float64)
+        stats = (T.TrackStats * self.n)()
+        self.ctx.check(lib().lsdg_batch_track_se3(self.ctx.handle, self._h, self._ptr(ref_images), self._ptr(ref_idepth),
+                                                  self._ptr(ref_var), self._ptr(new_images),
+                                                  np.ascontiguousarray(init, np.float64).reshape(-1), out, stats))
+        return out.reshape(self.n, 3, 4), stats
+
+    def timing(self):
+        a, b = C.c_float(), C.c_float()
+        self.ctx.check(lib().lsdg_batch_timing(self.ctx.handle, self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def shape(self):
+        t, c, n, k = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self.ctx.check(lib().lsdg_batch_shape(self.ctx.handle, self._h, C.byref(t), C.byref(c), C.byref(n), C.byref(k)))
+        return {"threads": t.value, "cluster": c.value, "clusters": n.value, "launches_per_run": k.value}
+
+    def work(self):
+        p, b, u = C.c_int64(), C.c_double(), C.c_double()
+        self.ctx.check(lib().lsdg_batch_work(self.ctx.handle, self._h, C.byref(p), C.byref(b), C.byref(u)))
+        return p.value, b.value, u.value
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().lsdg_batch_destroy(self.ctx.handle, self._h)
+        self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pack_pairs(pairs):
+    """Concatenate synth.TrackingPair inputs into the back-to-back layout lsdg_batch_load expects."""
+    cat = lambda name: np.ascontiguousarray(np.concatenate([getattr(q, name).ravel() for q in pairs]), np.float32)
+    return cat("ref_image"), cat("ref_idepth"), cat("ref_idepth_var"), cat("new_image")
+
+
+def declared_symbols(header: str = HEADER):
+    """Names of the entry points include/lsdg.h declares."""
+    import re
+    txt = open(header).read()
+    return sorted(set(re.findall(r"^LSDG_API\s+[\w\s\*]+?\b(lsdg_\w+)\s*\(", txt, flags=re.M)))

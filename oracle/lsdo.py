@@ -1,0 +1,155 @@
+"""ctypes wrapper of the CPU ORACLE (oracle/liblsdo.so).  Test infrastructure only: imported by
+tests/, the smoke check and bench.py's cpu_baseline leg, never by the product package."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(os.path.dirname(HERE), "lsd-slam-pangolin-gui_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)
+import lsdg_types as T  # noqa: E402
+
+_lib = None
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        sys.path.insert(0, HERE)
+        import build as _b  # oracle/build.py
+        path = _b.build()
+        L = C.CDLL(path)
+        L.lsdo_default_params.argtypes = [C.POINTER(T.Params)]
+        L.lsdo_pyramid_f.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, _f32p]
+        L.lsdo_pyramid_d.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, _f64p]
+        L.lsdo_keyframe_f.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.c_int,
+                                      _f32p, _f32p, _f32p, _f32p, C.c_int, _i32p]
+        L.lsdo_keyframe_f.restype = C.c_int
+        for nm in ("lsdo_se3_normal_equations_f", "lsdo_se3_normal_equations_d"):
+            f = getattr(L, nm)
+            f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                          C.POINTER(T.Params), C.c_int, _f64p, _f64p]
+            f.restype = C.c_int
+        for nm in ("lsdo_track_se3_f", "lsdo_track_se3_d"):
+            f = getattr(L, nm)
+            f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                          C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), C.c_int]
+            f.restype = C.c_int
+        L.lsdo_track_batch_f.argtypes = [C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), _f32p, _f32p, _f32p,
+                                         _f32p, _f64p, _f64p, C.POINTER(T.TrackStats), C.POINTER(T.Params), C.c_int]
+        L.lsdo_track_batch_f.restype = C.c_int
+        L.lsdo_hardware_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def default_params() -> T.Params:
+    p = T.Params()
+    lib().lsdo_default_params(C.byref(p))
+    return p
+
+
+def _intr(intr) -> T.Intrinsics:
+    if isinstance(intr, T.Intrinsics):
+        return intr
+    fx, fy, cx, cy = intr.as_tuple() if hasattr(intr, "as_tuple") else intr
+    return T.Intrinsics(fx, fy, cx, cy)
+
+
+def level_sizes(w, h, levels):
+    return [(w >> l, h >> l) for l in range(levels)]
+
+
+def pyramid(img: np.ndarray, levels: int = 5, double: bool = False):
+    """List of float4 {I, gx, gy, 0} arrays [h_l, w_l, 4]."""
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape
+    sizes = level_sizes(w, h, levels)
+    n = sum(a * b for a, b in sizes)
+    out = np.zeros(4 * n, np.float64 if double else np.float32)
+    (lib().lsdo_pyramid_d if double else lib().lsdo_pyramid_f)(img, w, h, levels, out)
+    res, off = [], 0
+    for (a, b) in sizes:
+        res.append(out[off:off + 4 * a * b].reshape(b, a, 4))
+        off += 4 * a * b
+    return res
+
+
+def keyframe(img, idepth, var, intr, levels: int = 5):
+    """Depth pyramid and reference points (float oracle).  Returns (depth[l], var[l], xyzi[l], pvar[l])."""
+    img = np.ascontiguousarray(img, np.float32)
+    h, w = img.shape
+    sizes = level_sizes(w, h, levels)
+    n = sum(a * b for a, b in sizes)
+    d = np.zeros(n, np.float32)
+    v = np.zeros(n, np.float32)
+    xyzi = np.zeros(4 * n, np.float32)
+    pv = np.zeros(n, np.float32)
+    counts = np.zeros(levels, np.int32)
+    k = _intr(intr)
+    rc = lib().lsdo_keyframe_f(img, np.ascontiguousarray(idepth, np.float32), np.ascontiguousarray(var, np.float32),
+                               w, h, C.byref(k), levels, d, v, xyzi, pv, n, counts)
+    assert rc == 0
+    D, V, P, PV = [], [], [], []
+    off = 0
+    poff = 0
+    for l, (a, b) in enumerate(sizes):
+        D.append(d[off:off + a * b].reshape(b, a))
+        V.append(v[off:off + a * b].reshape(b, a))
+        off += a * b
+        c = int(counts[l])
+        P.append(xyzi[4 * poff:4 * (poff + c)].reshape(c, 4))
+        PV.append(pv[poff:poff + c])
+        poff += c
+    return D, V, P, PV
+
+
+def se3_normal_equations(pair, ref_to_frame: np.ndarray, level: int, params: T.Params = None, double: bool = False):
+    p = params or default_params()
+    out = np.zeros(T.NE_SIZE, np.float64)
+    f = lib().lsdo_se3_normal_equations_d if double else lib().lsdo_se3_normal_equations_f
+    rc = f(pair.ref_image, pair.ref_idepth, pair.ref_idepth_var, pair.new_image, pair.w, pair.h,
+           C.byref(_intr(pair.intr)), C.byref(p), level, np.ascontiguousarray(ref_to_frame, np.float64).ravel(), out)
+    assert rc == 0
+    return out
+
+
+def track_se3(pair, init: np.ndarray = None, params: T.Params = None, double: bool = False, threads: int = 1):
+    p = params or default_params()
+    init = np.eye(3, 4) if init is None else init
+    out = np.zeros(12, np.float64)
+    st = T.TrackStats()
+    f = lib().lsdo_track_se3_d if double else lib().lsdo_track_se3_f
+    rc = f(pair.ref_image, pair.ref_idepth, pair.ref_idepth_var, pair.new_image, pair.w, pair.h,
+           C.byref(_intr(pair.intr)), C.byref(p), np.ascontiguousarray(init, np.float64).ravel(), out, C.byref(st), threads)
+    return rc, out.reshape(3, 4), st
+
+
+def track_batch(pairs, inits=None, params: T.Params = None, threads: int = None):
+    """CPU baseline of the batched workload (float, pairs spread over threads)."""
+    p = params or default_params()
+    n = len(pairs)
+    threads = threads or hardware_threads()
+    widths = np.array([q.w for q in pairs], np.int32)
+    heights = np.array([q.h for q in pairs], np.int32)
+    intr = (T.Intrinsics * n)(*[_intr(q.intr) for q in pairs])
+    cat = lambda name: np.ascontiguousarray(np.concatenate([getattr(q, name).ravel() for q in pairs]), np.float32)
+    init = np.concatenate([np.eye(3, 4).ravel() for _ in range(n)]) if inits is None else np.ascontiguousarray(inits, np.float64).ravel()
+    out = np.zeros(12 * n, np.float64)
+    stats = (T.TrackStats * n)()
+    lib().lsdo_track_batch_f(n, widths, heights, intr, cat("ref_image"), cat("ref_idepth"), cat("ref_idepth_var"),
+                             cat("new_image"), init, out, stats, C.byref(p), threads)
+    return out.reshape(n, 3, 4), stats
+
+
+def hardware_threads() -> int:
+    return int(lib().lsdo_hardware_threads())
