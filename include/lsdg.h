@@ -81,12 +81,15 @@ typedef struct lsdg_params {
   float photometric_variance; /* sigma_I^2 of a residual (intensity units^2) */
   float huber_delta;          /* Huber threshold on the variance-normalised residual */
   float min_z;                /* warped points with z <= min_z are not used (m) */
+  float border_margin;        /* a point takes part in a level only if its first warp of that level
+                                 lands this many pixels inside the image (px) */
   float lm_lambda_initial;    /* LM damping at the start of each level: A_ii = H_ii (1 + lambda) */
   float lm_lambda_up;         /* lambda *= up after a rejected step */
   float lm_lambda_down;       /* lambda *= down after an accepted step */
-  float convergence_eps;      /* a level ends when an accepted step lowers the mean energy by
-                                 less than this fraction */
-  float step_eps;             /* a level ends when max |delta| falls below this */
+  float step_eps;             /* level l ends when the undamped Gauss-Newton step of the current
+                                 linearisation is below step_eps * 2^l in every twist coordinate */
+  float stall_eps;            /* ... or when a step is rejected while that undamped step is below
+                                 stall_eps * 2^l (the level's noise floor is reached) */
   float min_good_ratio;       /* inliers / used points below which tracking is lost */
   float min_usage;            /* used points / keyframe points below which tracking is lost */
   float sim3_depth_variance;  /* floor of the inverse-depth residual variance (Sim3) */

@@ -67,11 +67,12 @@ void lsdg_default_params(lsdg_params* p) {
   p->photometric_variance = 16.0f;
   p->huber_delta = 2.0f;
   p->min_z = 0.01f;
+  p->border_margin = 2.5f;
   p->lm_lambda_initial = 0.01f;
   p->lm_lambda_up = 4.0f;
   p->lm_lambda_down = 0.5f;
-  p->convergence_eps = 1e-3f;
-  p->step_eps = 1e-6f;
+  p->step_eps = 1e-5f;
+  p->stall_eps = 5e-4f;
   p->min_good_ratio = 0.5f;
   p->min_usage = 0.2f;
   p->sim3_depth_variance = 1e-4f;
@@ -221,7 +222,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
   fs.off_var0 = off;
   for (int i = 0; i < n; ++i) if (depth[i]) { o_var0[i] = off; off += (size_t)w[i] * h[i] * 4; }
   off = al256(off);
-  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], blk[kMaxLevels], cnt; };
+  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], psig[kMaxLevels], blk[kMaxLevels], cnt; };
   std::vector<Rest> rest(n);
   for (int i = 0; i < n; ++i) {
     Rest& r = rest[i];
@@ -236,6 +237,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         }
         r.pxyzi[l] = off; off = al256(off + pix * 16);
         r.pvar[l] = off; off = al256(off + pix * 4);
+        r.psig[l] = off; off = al256(off + pix * 4);
         r.blk[l] = off; off = al256(off + ((pix + kCountBlock - 1) / kCountBlock) * 4);
       }
     }
@@ -263,6 +265,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         F.ivar[l] = (float*)(base + (l == 0 ? o_var0[i] : r.var[l]));
         F.pxyzi[l] = (float4*)(base + r.pxyzi[l]);
         F.pvar[l] = (float*)(base + r.pvar[l]);
+        F.psig[l] = (float*)(base + r.psig[l]);
         F.blk_count[l] = (int*)(base + r.blk[l]);
       }
       F.fx[l] = (float)fx; F.fy[l] = (float)fy; F.cx[l] = (float)cx; F.cy[l] = (float)cy;
@@ -309,8 +312,9 @@ TrackArgs make_track_args(const lsdg_params& p) {
   a.lambda0 = p.lm_lambda_initial;
   a.lambda_up = p.lm_lambda_up;
   a.lambda_down = p.lm_lambda_down;
-  a.conv_eps = p.convergence_eps;
+  a.border_margin = p.border_margin;
   a.step_eps = p.step_eps;
+  a.stall_eps = p.stall_eps;
   a.min_good_ratio = p.min_good_ratio;
   a.min_usage = p.min_usage;
   return a;

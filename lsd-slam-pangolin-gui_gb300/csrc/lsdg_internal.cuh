@@ -7,6 +7,8 @@
 //   idepth[l], ivar[l]  float [h_l * w_l]  keyframe depth pyramid (idepth <= 0: none)
 //   pxyzi[l]   float4 [n_l]         tracking reference points, SoA: {X, Y, Z, I_keyframe}
 //   pvar[l]    float  [n_l]         inverse-depth variance of each point
+//   psig[l]    float  [n_l]         tracker scratch: residual variance of each point, fixed by the
+//                                   first pass of a level (0 = the point sits out the level)
 //   pcount[l]  int                  n_l, written on the device by the compaction
 // All per-pixel planes are row-major and 256-byte aligned.
 #pragma once
@@ -31,6 +33,7 @@ struct FrameDev {
   float* ivar[kMaxLevels];
   float4* pxyzi[kMaxLevels];
   float* pvar[kMaxLevels];
+  float* psig[kMaxLevels];
   int* pcount;                   // [kMaxLevels]
   int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per block, then offsets
   float fx[kMaxLevels], fy[kMaxLevels], cx[kMaxLevels], cy[kMaxLevels];
@@ -56,8 +59,8 @@ struct TrackArgs {
   int top_level;             // first (coarsest) level to run
   int bottom_level;          // last level to run
   int max_iter[kMaxLevels];
-  float photometric_variance, huber_delta, min_z;
-  double lambda0, lambda_up, lambda_down, conv_eps, step_eps;
+  float photometric_variance, huber_delta, min_z, border_margin;
+  double lambda0, lambda_up, lambda_down, step_eps, stall_eps;
   float min_good_ratio, min_usage;
 };
 

@@ -7,10 +7,13 @@
 // GB300 design.  One persistent kernel tracks any number of pairs.  Each pair is owned by one
 // thread-block cluster (C CTAs of NT threads, C up to 16); clusters pull pairs from an atomic work
 // queue (largest first).  A residual pass over a level's points is:
-//   1. every thread walks the SoA points with stride C*NT (coalesced float4 + float loads), warps
-//      the point with the current pose, samples {I, gx, gy} of the new frame bilinearly (four
-//      16-byte float4 gathers, L1/L2 resident), and accumulates the 21 + 6 + 1 Kahan-compensated
-//      float sums of J^T W J, J^T W r and the Huber energy;
+//   1. every thread walks the SoA points with stride C*NT (coalesced float4 loads), warps the point
+//      with the current pose, samples the new frame's intensity with the C1 Catmull-Rom
+//      interpolant and its exact derivative (4x4 taps, L1/L2 resident), and accumulates the
+//      21 + 6 + 1 Kahan-compensated float sums of J^T W J, J^T W r and the Huber energy.  The
+//      first pass of a level fixes each point's residual variance in the psig scratch array (and
+//      leaves out points that do not land border_margin pixels inside the image), so each level
+//      minimises one fixed, continuous energy whose gradient is exactly 2 J^T W r;
 //   2. warp shuffles merge the compensated pairs, then a fixed-order block merge in shared memory;
 //   3. cluster.sync(); rank 0 merges the C block partials through distributed shared memory (fixed
 //      rank order, so the result is deterministic for a given C and NT);
@@ -47,11 +50,27 @@ __device__ __forceinline__ void kmerge(float& s, float& c, float os, float oc) {
   c = (c + oc) - err;
 }
 
+// Catmull-Rom cubic (C1, interpolating): weights of taps -1, 0, 1, 2 at fraction t and their
+// derivatives; at t = 0 the derivative weights are the central difference (-1/2, 0, 1/2, 0).
+__device__ __forceinline__ void catmull_rom(float t, float w[4], float d[4]) {
+  const float t2 = t * t, t3 = t2 * t;
+  w[0] = 0.5f * ((2.f * t2 - t3) - t);
+  w[1] = 0.5f * ((3.f * t3 - 5.f * t2) + 2.f);
+  w[2] = 0.5f * ((4.f * t2 - 3.f * t3) + t);
+  w[3] = 0.5f * (t3 - t2);
+  d[0] = 0.5f * ((4.f * t - 3.f * t2) - 1.f);
+  d[1] = 0.5f * (9.f * t2 - 10.f * t);
+  d[2] = 0.5f * ((8.f * t - 9.f * t2) + 1.f);
+  d[3] = 0.5f * (3.f * t2 - 2.f * t);
+}
+
 struct Ctl {
   float R[9];
   float t[3];
   int pair;  // -1: no more work
   int level;
+  int first;  // first pass of the level: fixes each point's residual variance and participation
+  int pad;
 };
 
 struct CtaPart {
@@ -66,8 +85,8 @@ struct LMState {
   double T[12];     // ref_to_frame, accepted
   double Ttry[12];  // ref_to_frame being evaluated
   double S[32];     // sums of the last accepted pass
-  double E, lambda;
-  int it, phase, level, pair, have_final;
+  double E, lambda, gnmax;
+  int it, phase, level, pair, have_final, fresh;
   lsdg_track_stats st;
 };
 
@@ -185,6 +204,7 @@ __device__ bool start_level(const TrackArgs& a, LMState& lm, Ctl& ctl, int level
       lm.phase = PH_INIT;
       ctl.level = l;
       ctl.pair = lm.pair;
+      ctl.first = 1;
       publish_pose(ctl, lm.T);
       return true;
     }
@@ -251,21 +271,35 @@ __device__ void next_level(const TrackArgs& a, LMState& lm, Ctl& ctl) {
   fetch_pair(a, lm, ctl);
 }
 
+// One LM iteration decision on the current linearisation lm.S (same rules as the CPU oracle):
+// converged when the undamped Gauss-Newton step is below step_eps * 2^level; otherwise solve the
+// damped system and publish the trial pose, unless the level's iteration budget is spent.
 __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl) {
-  while (lm.it < a.max_iter[lm.level]) {
+  const double thr = a.step_eps * (double)(1 << lm.level);
+  for (;;) {
+    if (lm.fresh) {
+      double gn[6];
+      lm.gnmax = 1e300;
+      if (ldlt_solve_d(6, lm.S, lm.S + 21, 0.0, gn)) {
+        double m = 0;
+        for (int i = 0; i < 6; ++i) m = fmax(m, fabs(gn[i]));
+        lm.gnmax = m;
+        if (m < thr) break;
+      }
+      lm.fresh = 0;
+    }
+    if (lm.it >= a.max_iter[lm.level]) break;
+    lm.it++;
     double dx[6];
     if (!ldlt_solve_d(6, lm.S, lm.S + 21, lm.lambda, dx)) {
       lm.lambda *= a.lambda_up;
-      lm.it++;
       continue;
     }
-    double m = 0;
-    for (int i = 0; i < 6; ++i) m = fmax(m, fabs(dx[i]));
-    if (m < a.step_eps) break;
     se3_exp_mul_d(dx, lm.T, lm.Ttry);
     lm.phase = PH_TRY;
     ctl.pair = lm.pair;
     ctl.level = lm.level;
+    ctl.first = 0;
     publish_pose(ctl, lm.Ttry);
     return;
   }
@@ -281,6 +315,7 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
       lm.E = tot[27] / N;
       lm.lambda = a.lambda0;
       lm.it = 0;
+      lm.fresh = 1;
       if (lm.level == a.bottom_level) lm.have_final = 1;
       try_step(a, lm, ctl);
     } else {
@@ -289,20 +324,18 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
     return;
   }
   if (N > 0 && tot[27] / N < lm.E) {
-    const double E2 = tot[27] / N;
-    const double rel = (lm.E - E2) / lm.E;
     for (int i = 0; i < 12; ++i) lm.T[i] = lm.Ttry[i];
     for (int i = 0; i < 32; ++i) lm.S[i] = tot[i];
-    lm.E = E2;
+    lm.E = tot[27] / N;
     lm.lambda *= a.lambda_down;
-    if (rel < a.conv_eps) {
+    lm.fresh = 1;
+  } else {
+    if (lm.gnmax < a.stall_eps * (double)(1 << lm.level)) {  // noise floor of this level
       next_level(a, lm, ctl);
       return;
     }
-  } else {
     lm.lambda *= a.lambda_up;
   }
-  lm.it++;
   try_step(a, lm, ctl);
 }
 
@@ -344,10 +377,14 @@ __global__ void __launch_bounds__(NT) track_se3_kernel(const TrackArgs a) {
     const int n = R->pcount[level];
     const float4* __restrict__ pts = R->pxyzi[level];
     const float* __restrict__ pvar = R->pvar[level];
-    const float4* __restrict__ img = Fc->pyr[level];
+    float* __restrict__ psig = R->psig[level];
+    const float* __restrict__ img = Fc->plane[level];
     const int w = Fc->w >> level, h = Fc->h >> level;
     const float fx = Fc->fx[level], fy = Fc->fy[level], cx = Fc->cx[level], cy = Fc->cy[level];
     const float umax = (float)(w - 2), vmax = (float)(h - 2);
+    const float margin = a.border_margin;
+    const float ulo = margin, vlo = margin, uhi = (float)(w - 1) - margin, vhi = (float)(h - 1) - margin;
+    const bool first = ctl.first != 0;
     const float R00 = ctl.R[0], R01 = ctl.R[1], R02 = ctl.R[2];
     const float R10 = ctl.R[3], R11 = ctl.R[4], R12 = ctl.R[5];
     const float R20 = ctl.R[6], R21 = ctl.R[7], R22 = ctl.R[8];
@@ -362,27 +399,52 @@ __global__ void __launch_bounds__(NT) track_se3_kernel(const TrackArgs a) {
     int good = 0, bad = 0, oob = 0;
 
     for (int k = (int)rank * NT + tid; k < n; k += (int)C * NT) {
+      float s2 = 0.f;
+      if (!first) {
+        s2 = psig[k];
+        if (!(s2 > 0.f)) continue;  // sits out this level
+      }
       const float4 p = __ldg(&pts[k]);
-      const float var = __ldg(&pvar[k]);
       const float X = p.x, Y = p.y, Z = p.z, Ik = p.w;
       const float Rpx = (R00 * X + R01 * Y) + R02 * Z;
       const float Rpy = (R10 * X + R11 * Y) + R12 * Z;
       const float Rpz = (R20 * X + R21 * Y) + R22 * Z;
       const float Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
-      if (!(Zp > minz)) { ++oob; continue; }
+      if (!(Zp > minz)) {
+        if (first) psig[k] = 0.f;
+        ++oob;
+        continue;
+      }
       const float iz = 1.0f / Zp;
       const float u = fx * (Xp * iz) + cx;
       const float v = fy * (Yp * iz) + cy;
-      if (!(u >= 1.f && v >= 1.f && u < umax && v < vmax)) { ++oob; continue; }
+      if (first) {
+        if (!(u >= ulo && v >= vlo && u < uhi && v < vhi)) {
+          psig[k] = 0.f;
+          ++oob;
+          continue;
+        }
+      } else if (!(u >= 1.f && v >= 1.f && u < umax && v < vmax)) {
+        ++oob;
+        continue;
+      }
       const int ix = (int)u, iy = (int)v;
       const float ax = u - (float)ix, ay = v - (float)iy;
-      const float bx = 1.f - ax, by = 1.f - ay;
-      const float w00 = bx * by, w10 = ax * by, w01 = bx * ay, w11 = ax * ay;
-      const float4* q = img + (size_t)iy * w + ix;
-      const float4 c00 = __ldg(q), c10 = __ldg(q + 1), c01 = __ldg(q + w), c11 = __ldg(q + w + 1);
-      const float In = ((w00 * c00.x + w10 * c10.x) + w01 * c01.x) + w11 * c11.x;
-      const float Gx = ((w00 * c00.y + w10 * c10.y) + w01 * c01.y) + w11 * c11.y;
-      const float Gy = ((w00 * c00.z + w10 * c10.z) + w01 * c01.z) + w11 * c11.z;
+      float wx[4], dxw[4], wy[4], dyw[4];
+      catmull_rom(ax, wx, dxw);
+      catmull_rom(ay, wy, dyw);
+      float rI[4], rD[4];
+      const float* q = img + (size_t)(iy - 1) * w + (ix - 1);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float i0 = __ldg(q), i1 = __ldg(q + 1), i2 = __ldg(q + 2), i3 = __ldg(q + 3);
+        rI[j] = ((wx[0] * i0 + wx[1] * i1) + wx[2] * i2) + wx[3] * i3;
+        rD[j] = ((dxw[0] * i0 + dxw[1] * i1) + dxw[2] * i2) + dxw[3] * i3;
+        q += w;
+      }
+      const float In = ((wy[0] * rI[0] + wy[1] * rI[1]) + wy[2] * rI[2]) + wy[3] * rI[3];
+      const float Gx = ((wy[0] * rD[0] + wy[1] * rD[1]) + wy[2] * rD[2]) + wy[3] * rD[3];
+      const float Gy = ((dyw[0] * rI[0] + dyw[1] * rI[1]) + dyw[2] * rI[2]) + dyw[3] * rI[3];
       const float r = In - Ik;
       const float gxs = Gx * fx, gys = Gy * fy;
       const float a0 = gxs * iz, a1 = gys * iz;
@@ -394,8 +456,11 @@ __global__ void __launch_bounds__(NT) track_se3_kernel(const TrackArgs a) {
       J[3] = Yp * a2 - Zp * a1;
       J[4] = Zp * a0 - Xp * a2;
       J[5] = Xp * a1 - Yp * a0;
-      const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
-      const float s2 = pvr + (drd * drd) * var;
+      if (first) {
+        const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
+        s2 = pvr + (drd * drd) * __ldg(&pvar[k]);
+        psig[k] = s2;
+      }
       const float e2 = (r * r) / s2;
       const float ae = sqrtf(e2);
       float wh, rho;

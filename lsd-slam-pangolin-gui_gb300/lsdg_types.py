@@ -31,11 +31,12 @@ class Params(C.Structure):
         ("photometric_variance", C.c_float),
         ("huber_delta", C.c_float),
         ("min_z", C.c_float),
+        ("border_margin", C.c_float),
         ("lm_lambda_initial", C.c_float),
         ("lm_lambda_up", C.c_float),
         ("lm_lambda_down", C.c_float),
-        ("convergence_eps", C.c_float),
         ("step_eps", C.c_float),
+        ("stall_eps", C.c_float),
         ("min_good_ratio", C.c_float),
         ("min_usage", C.c_float),
         ("sim3_depth_variance", C.c_float),

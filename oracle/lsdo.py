@@ -44,6 +44,13 @@ def lib():
             f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
                           C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), C.c_int]
             f.restype = C.c_int
+        L.lsdo_se3_fixed_energy_d.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                              C.POINTER(T.Params), C.c_int, _f64p, _f64p, _f64p]
+        L.lsdo_se3_fixed_energy_d.restype = C.c_int
+        L.lsdo_track_trace.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                       C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), _f64p, C.c_int,
+                                       C.POINTER(C.c_int)]
+        L.lsdo_track_trace.restype = C.c_int
         L.lsdo_track_batch_f.argtypes = [C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), _f32p, _f32p, _f32p,
                                          _f32p, _f64p, _f64p, C.POINTER(T.TrackStats), C.POINTER(T.Params), C.c_int]
         L.lsdo_track_batch_f.restype = C.c_int
@@ -123,6 +130,18 @@ def se3_normal_equations(pair, ref_to_frame: np.ndarray, level: int, params: T.P
     return out
 
 
+def se3_fixed_energy(pair, T_fix, T_eval, level, params=None):
+    """FP64 sums at T_eval with variances and participating points fixed by a first pass at T_fix."""
+    p = params or default_params()
+    out = np.zeros(T.NE_SIZE, np.float64)
+    rc = lib().lsdo_se3_fixed_energy_d(pair.ref_image, pair.ref_idepth, pair.ref_idepth_var, pair.new_image, pair.w,
+                                       pair.h, C.byref(_intr(pair.intr)), C.byref(p), level,
+                                       np.ascontiguousarray(T_fix, np.float64).ravel(),
+                                       np.ascontiguousarray(T_eval, np.float64).ravel(), out)
+    assert rc == 0
+    return out
+
+
 def track_se3(pair, init: np.ndarray = None, params: T.Params = None, double: bool = False, threads: int = 1):
     p = params or default_params()
     init = np.eye(3, 4) if init is None else init
@@ -132,6 +151,21 @@ def track_se3(pair, init: np.ndarray = None, params: T.Params = None, double: bo
     rc = f(pair.ref_image, pair.ref_idepth, pair.ref_idepth_var, pair.new_image, pair.w, pair.h,
            C.byref(_intr(pair.intr)), C.byref(p), np.ascontiguousarray(init, np.float64).ravel(), out, C.byref(st), threads)
     return rc, out.reshape(3, 4), st
+
+
+def track_trace(pair, init=None, params=None, double=False):
+    """trackFrame with a per-pass trace: rows {level, iteration, lambda, accepted (2 = convergence
+    test), mean energy, points, max |undamped step|, 0}."""
+    p = params or default_params()
+    init = np.eye(3, 4) if init is None else init
+    out = np.zeros(12, np.float64)
+    st = T.TrackStats()
+    buf = np.zeros(8 * 4096, np.float64)
+    n = C.c_int()
+    rc = lib().lsdo_track_trace(int(double), pair.ref_image, pair.ref_idepth, pair.ref_idepth_var, pair.new_image,
+                                pair.w, pair.h, C.byref(_intr(pair.intr)), C.byref(p),
+                                np.ascontiguousarray(init, np.float64).ravel(), out, C.byref(st), buf, buf.size, C.byref(n))
+    return rc, out.reshape(3, 4), st, buf[:8 * n.value].reshape(-1, 8)
 
 
 def track_batch(pairs, inits=None, params: T.Params = None, threads: int = None):

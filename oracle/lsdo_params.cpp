@@ -16,11 +16,12 @@ void default_params(lsdg_params* p) {
   p->photometric_variance = 16.0f;
   p->huber_delta = 2.0f;
   p->min_z = 0.01f;
+  p->border_margin = 2.5f;
   p->lm_lambda_initial = 0.01f;
   p->lm_lambda_up = 4.0f;
   p->lm_lambda_down = 0.5f;
-  p->convergence_eps = 1e-3f;
-  p->step_eps = 1e-6f;
+  p->step_eps = 1e-5f;
+  p->stall_eps = 5e-4f;
   p->min_good_ratio = 0.5f;
   p->min_usage = 0.2f;
   p->sim3_depth_variance = 1e-4f;

@@ -187,6 +187,24 @@ struct KSum {
 };
 
 // ------------------------------------------------------------------------------------------
+// Catmull-Rom cubic (C1, interpolating): weights of taps -1, 0, 1, 2 at fraction t and their
+// derivatives.  At t = 0 the derivative weights are (-1/2, 0, 1/2, 0): the central difference.
+// ------------------------------------------------------------------------------------------
+template <class T>
+static inline void catmull_rom(T t, T w[4], T d[4]) {
+  const T t2 = t * t, t3 = t2 * t;
+  const T h = (T)0.5;
+  w[0] = h * (((T)2 * t2 - t3) - t);
+  w[1] = h * (((T)3 * t3 - (T)5 * t2) + (T)2);
+  w[2] = h * (((T)4 * t2 - (T)3 * t3) + t);
+  w[3] = h * (t3 - t2);
+  d[0] = h * (((T)4 * t - (T)3 * t2) - (T)1);
+  d[1] = h * ((T)9 * t2 - (T)10 * t);
+  d[2] = h * (((T)8 * t - (T)9 * t2) + (T)1);
+  d[3] = h * ((T)3 * t2 - (T)2 * t);
+}
+
+// ------------------------------------------------------------------------------------------
 // a3 + a4: one residual pass (calculateWarpUpdate) over [begin, end) of a level's points
 // ------------------------------------------------------------------------------------------
 template <class T>
@@ -201,37 +219,70 @@ struct PassSums {
   }
 };
 
+// Residual model (own restatement of ECCV 2014 sec. 3.2):
+//   r = I_new(pi(R p + t)) - I_key(p), I_new sampled with the C1 Catmull-Rom interpolant,
+//   J = dr/dxi with the exact derivative of that interpolant (so that 2 J^T W r is the gradient
+//       of the energy the LM step is accepted on, and J is continuous in the pose -- at pixel
+//       centres it equals the central-difference gradient),
+//   sigma^2 = sigma_I^2 + (dr/dd)^2 V(p), d = inverse depth, Huber weight on r / sigma,
+//   energy = sum of Huber(r / sigma) (rho = e^2 inside delta, delta (2|e| - delta) outside).
+// The first pass of a level ("first") fixes, per point, sigma^2 and whether the point takes part
+// in the level (its warp must land border_margin pixels inside the image); sig2[k] stores sigma^2,
+// or 0 for a point left out.  The later passes of the level reuse them, so every level minimises
+// one fixed, continuous energy.
 template <class T>
 static void se3_pass_range(const Points<T>& P, size_t begin, size_t end, const FrameLevel<T>& F,
                            const LevelCam& cam, const double Tp[12], const lsdg_params& prm,
-                           PassSums<T>& S) {
+                           bool first, T* sig2, PassSums<T>& S) {
   const T R00 = (T)Tp[0], R01 = (T)Tp[1], R02 = (T)Tp[2], t0 = (T)Tp[3];
   const T R10 = (T)Tp[4], R11 = (T)Tp[5], R12 = (T)Tp[6], t1 = (T)Tp[7];
   const T R20 = (T)Tp[8], R21 = (T)Tp[9], R22 = (T)Tp[10], t2 = (T)Tp[11];
   const T fx = (T)cam.fx, fy = (T)cam.fy, cx = (T)cam.cx, cy = (T)cam.cy;
+  // the 4x4 Catmull-Rom footprint of u needs columns floor(u)-1 .. floor(u)+2
   const T umax = (T)(cam.w - 2), vmax = (T)(cam.h - 2);
+  const T margin = (T)prm.border_margin;
+  const T ulo = margin, vlo = margin, uhi = (T)(cam.w - 1) - margin, vhi = (T)(cam.h - 1) - margin;
   const T pvar = (T)prm.photometric_variance, delta = (T)prm.huber_delta, minz = (T)prm.min_z;
   const int w = cam.w;
   for (size_t k = begin; k < end; ++k) {
+    if (!first && !(sig2[k] > (T)0)) continue;
     const T X = P.xyzi[4 * k + 0], Y = P.xyzi[4 * k + 1], Z = P.xyzi[4 * k + 2], Ik = P.xyzi[4 * k + 3];
-    const T var = P.var[k];
     const T Rpx = (R00 * X + R01 * Y) + R02 * Z;
     const T Rpy = (R10 * X + R11 * Y) + R12 * Z;
     const T Rpz = (R20 * X + R21 * Y) + R22 * Z;
     const T Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
-    if (!(Zp > minz)) { ++S.oob; continue; }
+    if (!(Zp > minz)) {
+      if (first) sig2[k] = (T)0;
+      ++S.oob;
+      continue;
+    }
     const T iz = (T)1 / Zp;
     const T u = fx * (Xp * iz) + cx;
     const T v = fy * (Yp * iz) + cy;
-    if (!(u >= (T)1 && v >= (T)1 && u < umax && v < vmax)) { ++S.oob; continue; }
+    if (first) {
+      if (!(u >= ulo && v >= vlo && u < uhi && v < vhi)) {
+        sig2[k] = (T)0;
+        ++S.oob;
+        continue;
+      }
+    } else if (!(u >= (T)1 && v >= (T)1 && u < umax && v < vmax)) {
+      ++S.oob;
+      continue;
+    }
     const int ix = (int)u, iy = (int)v;
     const T ax = u - (T)ix, ay = v - (T)iy;
-    const T bx = (T)1 - ax, by = (T)1 - ay;
-    const T w00 = bx * by, w10 = ax * by, w01 = bx * ay, w11 = ax * ay;
-    const size_t i00 = (size_t)iy * w + ix;
-    const T In = ((w00 * F.I[i00] + w10 * F.I[i00 + 1]) + w01 * F.I[i00 + w]) + w11 * F.I[i00 + w + 1];
-    const T Gx = ((w00 * F.gx[i00] + w10 * F.gx[i00 + 1]) + w01 * F.gx[i00 + w]) + w11 * F.gx[i00 + w + 1];
-    const T Gy = ((w00 * F.gy[i00] + w10 * F.gy[i00 + 1]) + w01 * F.gy[i00 + w]) + w11 * F.gy[i00 + w + 1];
+    T wx[4], dx[4], wy[4], dy[4];
+    catmull_rom(ax, wx, dx);
+    catmull_rom(ay, wy, dy);
+    T rI[4], rD[4];
+    for (int j = 0; j < 4; ++j) {
+      const T* row = &F.I[(size_t)(iy - 1 + j) * w + (ix - 1)];
+      rI[j] = ((wx[0] * row[0] + wx[1] * row[1]) + wx[2] * row[2]) + wx[3] * row[3];
+      rD[j] = ((dx[0] * row[0] + dx[1] * row[1]) + dx[2] * row[2]) + dx[3] * row[3];
+    }
+    const T In = ((wy[0] * rI[0] + wy[1] * rI[1]) + wy[2] * rI[2]) + wy[3] * rI[3];
+    const T Gx = ((wy[0] * rD[0] + wy[1] * rD[1]) + wy[2] * rD[2]) + wy[3] * rD[3];
+    const T Gy = ((dy[0] * rI[0] + dy[1] * rI[1]) + dy[2] * rI[2]) + dy[3] * rI[3];
     const T r = In - Ik;
     const T gxs = Gx * fx, gys = Gy * fy;
     const T a0 = gxs * iz, a1 = gys * iz;
@@ -241,8 +292,14 @@ static void se3_pass_range(const Points<T>& P, size_t begin, size_t end, const F
     J[3] = Yp * a2 - Zp * a1;
     J[4] = Zp * a0 - Xp * a2;
     J[5] = Xp * a1 - Yp * a0;
-    const T drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
-    const T s2 = pvar + (drd * drd) * var;
+    T s2;
+    if (first) {
+      const T drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
+      s2 = pvar + (drd * drd) * P.var[k];
+      sig2[k] = s2;
+    } else {
+      s2 = sig2[k];
+    }
     const T e2 = (r * r) / s2;
     const T ae = std::sqrt(e2);
     T wh, rho;
@@ -262,17 +319,19 @@ static void se3_pass_range(const Points<T>& P, size_t begin, size_t end, const F
 
 template <class T>
 static void se3_pass(const Points<T>& P, const FrameLevel<T>& F, const LevelCam& cam,
-                     const double Tp[12], const lsdg_params& prm, int threads, double out[32]) {
+                     const double Tp[12], const lsdg_params& prm, int threads, bool first,
+                     std::vector<T>& sig2, double out[32]) {
   size_t n = P.var.size();
+  if (sig2.size() != n) sig2.assign(n, (T)0);
   PassSums<T> total;
   if (threads <= 1 || n < 4096) {
-    se3_pass_range(P, 0, n, F, cam, Tp, prm, total);
+    se3_pass_range(P, 0, n, F, cam, Tp, prm, first, sig2.data(), total);
   } else {
     std::vector<PassSums<T>> part(threads);
     std::vector<std::thread> th;
     for (int k = 0; k < threads; ++k) {
       size_t b = n * k / threads, e = n * (k + 1) / threads;
-      th.emplace_back([&, k, b, e] { se3_pass_range(P, b, e, F, cam, Tp, prm, part[k]); });
+      th.emplace_back([&, k, b, e] { se3_pass_range(P, b, e, F, cam, Tp, prm, first, sig2.data(), part[k]); });
     }
     for (auto& t : th) t.join();
     for (int k = 0; k < threads; ++k) total.merge(part[k]);
@@ -384,6 +443,15 @@ bool ldlt_solve(int n, const double* hu, const double* g, double lambda, double*
   return true;
 }
 
+// Optional per-pass trace for debugging and tests: 8 doubles per pass
+// {level, iteration, lambda, accepted, mean energy, points, max|undamped step|, 0}.
+thread_local std::vector<double>* g_trace = nullptr;
+static inline void trace(int lvl, int it, double lambda, int acc, double E, double N, double gn) {
+  if (!g_trace) return;
+  const double rec[8] = {(double)lvl, (double)it, lambda, (double)acc, E, N, gn, 0.0};
+  g_trace->insert(g_trace->end(), rec, rec + 8);
+}
+
 // ------------------------------------------------------------------------------------------
 // a5: SE3Tracker::trackFrame -- LM over the pyramid, coarse to fine
 // ------------------------------------------------------------------------------------------
@@ -401,35 +469,51 @@ int track_se3(const KeyframeData<T>& kf, const FrameData<T>& fr, const lsdg_para
     const Points<T>& P = kf.pts[lvl];
     if (P.var.empty()) continue;
     const LevelCam& cam = fr.cam[lvl];  // projection into the tracked frame
-    se3_pass(P, fr.lv[lvl], cam, Tc, prm, threads, S);
+    std::vector<T> sig2;
+    se3_pass(P, fr.lv[lvl], cam, Tc, prm, threads, true, sig2, S);
     st->passes[lvl]++;
     if (!(S[28] > 0)) continue;
     double E = S[27] / S[28];
     double lambda = prm.lm_lambda_initial;
-    for (int it = 0; it < prm.max_iterations[lvl]; ++it) {
+    const double thr = (double)prm.step_eps * (double)(1 << lvl);
+    const double stall = (double)prm.stall_eps * (double)(1 << lvl);
+    bool fresh = true;  // S is the linearisation at Tc (first pass or an accepted step)
+    double gnmax = 1e300;  // max |undamped Gauss-Newton step| of the current linearisation
+    for (int it = 0;;) {
+      if (fresh) {
+        // converged when the undamped Gauss-Newton step of this linearisation is negligible
+        double gn[6];
+        gnmax = 1e300;
+        if (ldlt_solve(6, S, S + 21, 0.0, gn)) {
+          gnmax = 0;
+          for (int i = 0; i < 6; ++i) gnmax = std::max(gnmax, std::fabs(gn[i]));
+          trace(lvl, it, lambda, 2, E, S[28], gnmax);
+          if (gnmax < thr) break;
+        }
+        fresh = false;
+      }
+      if (it >= prm.max_iterations[lvl]) break;
       double dx[6];
+      ++it;
       if (!ldlt_solve(6, S, S + 21, lambda, dx)) {
         lambda *= prm.lm_lambda_up;
         continue;
       }
-      double m = 0;
-      for (int i = 0; i < 6; ++i) m = std::max(m, std::fabs(dx[i]));
-      if (m < prm.step_eps) break;
       double Ex[12], Tt[12];
       se3_exp(dx, Ex);
       se3_mul(Ex, Tc, Tt);
       double S2[32];
-      se3_pass(P, fr.lv[lvl], cam, Tt, prm, threads, S2);
+      se3_pass(P, fr.lv[lvl], cam, Tt, prm, threads, false, sig2, S2);
       st->passes[lvl]++;
+      trace(lvl, it, lambda, S2[28] > 0 && S2[27] / S2[28] < E, S2[28] > 0 ? S2[27] / S2[28] : 0.0, S2[28], 0.0);
       if (S2[28] > 0 && S2[27] / S2[28] < E) {
-        const double E2 = S2[27] / S2[28];
-        const double rel = (E - E2) / E;
         std::memcpy(Tc, Tt, sizeof(Tc));
         std::memcpy(S, S2, sizeof(S));
-        E = E2;
+        E = S2[27] / S2[28];
         lambda *= prm.lm_lambda_down;
-        if (rel < prm.convergence_eps) break;
+        fresh = true;
       } else {
+        if (gnmax < stall) break;  // a step this small cannot lower the energy: noise floor
         lambda *= prm.lm_lambda_up;
       }
     }
@@ -563,11 +647,37 @@ static int ne_impl(const float* kimg, const float* idepth, const float* var, con
   KeyframeData<T> K;
   make_keyframe<T>(KF, idepth, var, K);
   if (level < 0 || level >= p->levels) return -1;
-  se3_pass(K.pts[level], F.lv[level], F.cam[level], ref_to_frame, *p, 1, out);
+  std::vector<T> sig2;
+  se3_pass(K.pts[level], F.lv[level], F.cam[level], ref_to_frame, *p, 1, true, sig2, out);
+  return 0;
+}
+
+// Energy and normal equations at T_eval with the residual variances and the participating points
+// fixed by a first pass at T_fix (the quantity one LM level minimises).
+template <class T>
+static int fixed_impl(const float* kimg, const float* idepth, const float* var, const float* fimg, int w, int h,
+                      const lsdg_intrinsics* k, const lsdg_params* p, int level, const double T_fix[12],
+                      const double T_eval[12], double out[32]) {
+  FrameData<T> KF, F;
+  make_frame<T>(kimg, w, h, *k, p->levels, KF);
+  make_frame<T>(fimg, w, h, *k, p->levels, F);
+  KeyframeData<T> K;
+  make_keyframe<T>(KF, idepth, var, K);
+  if (level < 0 || level >= p->levels) return -1;
+  std::vector<T> sig2;
+  double tmp[32];
+  se3_pass(K.pts[level], F.lv[level], F.cam[level], T_fix, *p, 1, true, sig2, tmp);
+  se3_pass(K.pts[level], F.lv[level], F.cam[level], T_eval, *p, 1, false, sig2, out);
   return 0;
 }
 
 extern "C" {
+
+int lsdo_se3_fixed_energy_d(const float* kimg, const float* idepth, const float* var, const float* fimg, int w,
+                            int h, const lsdg_intrinsics* k, const lsdg_params* p, int level, const double T_fix[12],
+                            const double T_eval[12], double out[32]) {
+  return fixed_impl<double>(kimg, idepth, var, fimg, w, h, k, p, level, T_fix, T_eval, out);
+}
 
 int lsdo_se3_normal_equations_f(const float* kimg, const float* idepth, const float* var,
                                 const float* fimg, int w, int h, const lsdg_intrinsics* k,
@@ -603,6 +713,20 @@ int lsdo_track_se3_f(const float* kimg, const float* idepth, const float* var, c
                      const double init[12], double out[12], lsdg_track_stats* st, int threads) {
   return track_impl<float>(kimg, idepth, var, fimg, w, h, k, p, init, out, st, threads);
 }
+int lsdo_track_trace(int use_double, const float* kimg, const float* idepth, const float* var, const float* fimg,
+                     int w, int h, const lsdg_intrinsics* k, const lsdg_params* p, const double init[12],
+                     double out[12], lsdg_track_stats* st, double* trace_out, int trace_cap, int* trace_len) {
+  std::vector<double> tr;
+  g_trace = &tr;
+  int rc = use_double ? track_impl<double>(kimg, idepth, var, fimg, w, h, k, p, init, out, st, 1)
+                      : track_impl<float>(kimg, idepth, var, fimg, w, h, k, p, init, out, st, 1);
+  g_trace = nullptr;
+  int n = (int)std::min<size_t>(tr.size(), (size_t)trace_cap);
+  std::memcpy(trace_out, tr.data(), n * sizeof(double));
+  *trace_len = n / 8;
+  return rc;
+}
+
 int lsdo_track_se3_d(const float* kimg, const float* idepth, const float* var, const float* fimg,
                      int w, int h, const lsdg_intrinsics* k, const lsdg_params* p,
                      const double init[12], double out[12], lsdg_track_stats* st, int threads) {

@@ -69,6 +69,26 @@ def test_normal_equations_descent_direction(pair0):
     assert ne1[27] / ne1[28] < ne[27] / ne[28]
 
 
+@pytest.mark.parametrize("level", [0, 2, 4])
+def test_gradient_is_exact_derivative_of_level_energy(pair0, level):
+    """2 J^T W r equals the central finite difference of the energy one LM level minimises (variances
+    and participating points fixed by the level's first pass).  This consistency is what lets the
+    float oracle, the FP64 oracle and the GPU take the same accept/reject decisions."""
+    rng = np.random.default_rng(level)
+    T0 = synth.pose_mul(synth.random_motion(rng, (0.1, 0.3), (0.002, 0.005)), synth.pose_inv(pair0.frame_to_ref))
+    S = lsdo.se3_fixed_energy(pair0, T0, T0, level)
+    h = 1e-6
+    fd = np.zeros(6)
+    for k in range(6):
+        e = np.zeros(6)
+        e[k] = h
+        Ep = lsdo.se3_fixed_energy(pair0, T0, synth.pose_mul(_se3_exp(e), T0), level)
+        Em = lsdo.se3_fixed_energy(pair0, T0, synth.pose_mul(_se3_exp(-e), T0), level)
+        assert Ep[28] == Em[28] == S[28]
+        fd[k] = (Ep[27] - Em[27]) / (2 * h)
+    np.testing.assert_allclose(2 * S[21:27], fd, rtol=0, atol=2e-3 * np.abs(fd).max())
+
+
 def _se3_exp(xi):
     v, w = xi[:3], xi[3:]
     R = synth.rodrigues(w)
@@ -88,7 +108,7 @@ def test_track_converges_to_ground_truth(pairs4, seed):
     assert rc == 0, st.as_dict()
     ang, dist = synth.pose_error(T, p.frame_to_ref)
     # limited by the 5 % inverse-depth noise and sigma=2 image noise of the synthetic keyframe
-    assert ang < 5e-3 and dist < 1.5e-2, (ang, dist)
+    assert ang < 3e-3 and dist < 1.5e-2, (ang, dist)
     assert st.good_ratio > 0.8 and st.usage > 0.8
     rcd, Td, std = lsdo.track_se3(p, double=True)
     a2, d2 = synth.pose_error(T, Td)
