@@ -200,14 +200,15 @@ lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
     // capture: events, build, tracker
     CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int nl = 0;
-    cudaEventRecord(b->ev[0], ctx->stream);
+    // external records become event-record nodes of the graph (timed on every replay)
+    cudaEventRecordWithFlags(b->ev[0], ctx->stream, cudaEventRecordExternal);
     st = enqueue_build(ctx, b, &nl);
-    cudaEventRecord(b->ev[1], ctx->stream);
+    cudaEventRecordWithFlags(b->ev[1], ctx->stream, cudaEventRecordExternal);
     int64_t before = ctx->launches;
     if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc);
     nl += (int)(ctx->launches - before);
     ctx->launches = before;
-    cudaEventRecord(b->ev[2], ctx->stream);
+    cudaEventRecordWithFlags(b->ev[2], ctx->stream, cudaEventRecordExternal);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (st != LSDG_OK) {
