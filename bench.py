@@ -338,9 +338,9 @@ def cpu_baseline(pairs, args, min_seconds=10.0):
     dt = time.time() - t0
     # FP64 restatement on a sample, for the accuracy report
     errs = []
-    for p in pairs[:4]:
-        _, Td, _ = lsdo.track_se3(p, double=True)
-        errs.append(synth.pose_error(out[pairs.index(p)], Td))
+    for i in range(4):
+        _, Td, _ = lsdo.track_se3(pairs[i], double=True)
+        errs.append(synth.pose_error(out[i], Td))
     return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{reps} x the {len(pairs)}-pair 640x480 batch (float CPU restatement, pairs over {cores} threads)",
             "float_vs_fp64_max_rot_err_rad": max(e[0] for e in errs)}
