@@ -132,6 +132,26 @@ def profiled_traffic(workload_key: str):
 # ----------------------------------------------------------------------------------------------
 # our arm
 # ----------------------------------------------------------------------------------------------
+def run_profile(args):
+    """Lean driver for ncu: one batch of --pairs 640x480 pairs, W + K graph replays, no soak, no
+    side measurements.  Prints one line."""
+    import lsdg
+
+    pairs = gen_pairs([(i, W, H) for i in range(args.pairs)], os.cpu_count() or 8)
+    ctx = lsdg.Context()
+    batch = lsdg.Batch(ctx, [p.w for p in pairs], [p.h for p in pairs], [p.intr for p in pairs])
+    batch.load(*[np.ascontiguousarray(x) for x in lsdg.pack_pairs(pairs)], np.stack([np.eye(3, 4)] * len(pairs)))
+    batch.run()
+    for _ in range(args.warmup + args.steps):
+        batch.run()
+    out, stats = batch.read()
+    b_ms, t_ms = batch.timing()
+    print(json.dumps({"profile_pairs": len(pairs), "shape": batch.shape(), "passes": batch.work()[0],
+                      "build_ms": b_ms, "track_ms": t_ms, "tune": ctx.tune_table()}))
+    batch.close()
+    ctx.close()
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -393,12 +413,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--quick", action="store_true", help="skip the mixed batch; one CPU-baseline pass")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="lean run for ncu captures")
+    ap.add_argument("--pairs", type=int, default=16, help="pairs in the --profile batch")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         run_ours(args, rank, world, local_rank)

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <new>
@@ -334,11 +335,25 @@ lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc)
 
 // Picks (threads, cluster) for a workload signature by timing every feasible candidate on the
 // caller's own data (two runs each, best kept).  The choice is cached per context.
+// The environment variable LSDG_TRACK_SHAPE="threads,cluster" pins the shape instead (used to
+// profile one known configuration); it is ignored when that shape does not fit the device.
 lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, TuneChoice* out) {
   auto it = ctx->tune_cache.find(key);
   if (it != ctx->tune_cache.end()) {
     *out = it->second;
     return LSDG_OK;
+  }
+  if (const char* env = std::getenv("LSDG_TRACK_SHAPE")) {
+    int nt = 0, c = 0;
+    if (std::sscanf(env, "%d,%d", &nt, &c) == 2) {
+      int mc = track_max_clusters(nt, c);
+      if (mc > 0) {
+        TuneChoice tc{nt, c, mc, 0.f};
+        ctx->tune_cache[key] = tc;
+        *out = tc;
+        return LSDG_OK;
+      }
+    }
   }
   cudaEvent_t e0, e1;
   CK(ctx, cudaEventCreate(&e0));
