@@ -246,8 +246,8 @@ LSDG_API lsdg_status lsdg_batch_track_se3(lsdg_ctx* ctx, lsdg_batch* batch, cons
 LSDG_API lsdg_status lsdg_batch_timing(lsdg_ctx* ctx, lsdg_batch* batch, float* build_ms, float* track_ms);
 /* The launch shape the autotuner picked for this batch (threads per CTA, CTAs per cluster, clusters
  * in the persistent grid) and the kernel launches one lsdg_batch_run issues. */
-LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* threads, int* cluster, int* clusters,
-                             int* launches_per_run);
+LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* threads, int* minblocks, int* cluster,
+                                      int* clusters, int* launches_per_run);
 /* Residual passes the last lsdg_batch_run executed, summed over pairs and levels, and the
  * algorithmic bytes those passes read (points + frame levels + sums). */
 LSDG_API lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* batch, int64_t* passes,
@@ -257,11 +257,12 @@ LSDG_API lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* batch, int64_t* 
 /* Autotuner                                                                                   */
 /* ------------------------------------------------------------------------------------------ */
 
-/* Entry `index` of the context's tile-shape cache: workload key, threads per CTA, CTAs per
- * cluster, clusters resident at once, and the tracker time that won.  LSDG_INVALID_ARG past the
- * end. */
-LSDG_API lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int key_len, int* threads, int* cluster,
-                           int* max_clusters, float* ms);
+/* Entry `index` of the context's tile-shape cache: workload key, threads per CTA, CTAs per SM the
+ * register budget allows for, CTAs per cluster, clusters resident at once, and the tracker time
+ * that won.  LSDG_INVALID_ARG past the end.  The environment variable
+ * LSDG_TRACK_SHAPE="threads,cluster[,minblocks]" pins the shape instead of timing candidates. */
+LSDG_API lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int key_len, int* threads, int* minblocks,
+                                    int* cluster, int* max_clusters, float* ms);
 
 #ifdef __cplusplus
 }

@@ -1,9 +1,11 @@
 """Build recipe of the product library liblsdg.so (CUDA sm_103a + C-ABI), in-tree.
 
 Each csrc/*.cu is compiled by nvcc in parallel (one -gencode, compute_103a -> sm_103a) and linked
-into lsd-slam-pangolin-gui_gb300/liblsdg.so.  Kernels are built with -fmad=false: every float
+into lsd-slam-pangolin-gui_gb300/liblsdg.so.  Kernels are built with -fmad=false (every float
 operation rounds on its own, exactly like the CPU oracle built with -ffp-contract=off, which is what
-makes pyramids, points and depth-filter decisions bit-identical to it.  No cmake.
+makes pyramids, points and depth-filter decisions bit-identical to it), except the tracker, which
+is built with FMA contraction (see FMAD).  The rebuild is triggered by source or header changes and
+by a change of this file.  No cmake.
 """
 from __future__ import annotations
 
@@ -20,8 +22,11 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-I", INCLUDE]
+# Translation units whose float results must be bit-identical to the CPU oracle are built without
+# FMA contraction; the tracker (parity by tolerance, throughput-critical) is built with it.
+FMAD = {"track.cu": "-fmad=true"}
 
 
 def sources():
@@ -35,10 +40,11 @@ def headers():
 
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    deps = [src] + headers()
+    deps = [src] + headers() + [os.path.abspath(__file__)]
     if os.path.exists(obj) and all(os.path.getmtime(d) <= os.path.getmtime(obj) for d in deps):
         return obj
-    cmd = [NVCC] + GENCODE + FLAGS + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj + ".tmp"]
+    fmad = FMAD.get(os.path.basename(src), "-fmad=false")
+    cmd = [NVCC] + GENCODE + FLAGS + [fmad] + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj + ".tmp"]
     subprocess.check_call(cmd)
     os.replace(obj + ".tmp", obj)
     return obj

@@ -22,9 +22,11 @@ namespace lsdg {
 int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
 int launch_frame_points(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
 void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
-cudaError_t launch_track(const TrackArgs& a, int threads, int cluster, int n_clusters, cudaStream_t s);
-int track_max_clusters(int threads, int cluster);
+cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s);
+int track_max_clusters(int threads, int minblocks, int cluster);
 cudaError_t track_prepare();
+int track_shape_count();
+void track_shape(int i, int* threads, int* minblocks);
 }  // namespace lsdg
 
 // ============================================================================================
@@ -321,14 +323,14 @@ TrackArgs make_track_args(const lsdg_params& p) {
   return a;
 }
 
-// Candidate tile shapes: threads per CTA x CTAs per cluster (the cluster owns one pair).
-static const int kCandThreads[] = {128, 256, 512};
+// Candidate tile shapes: (threads per CTA, register budget for that many CTAs per SM) x CTAs per
+// cluster (the cluster owns one pair).
 static const int kCandCluster[] = {2, 4, 8, 16};
 
 lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc) {
   int n_clusters = std::min(a.n_pairs, std::max(1, tc.max_clusters));
   CK(ctx, cudaMemsetAsync(a.work_counter, 0, sizeof(int), ctx->stream));
-  CK(ctx, launch_track(a, tc.threads, tc.cluster, n_clusters, ctx->stream));
+  CK(ctx, launch_track(a, tc.threads, tc.minblocks, tc.cluster, n_clusters, ctx->stream));
   ctx->launches += 1;
   return LSDG_OK;
 }
@@ -344,11 +346,11 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
     return LSDG_OK;
   }
   if (const char* env = std::getenv("LSDG_TRACK_SHAPE")) {
-    int nt = 0, c = 0;
-    if (std::sscanf(env, "%d,%d", &nt, &c) == 2) {
-      int mc = track_max_clusters(nt, c);
+    int nt = 0, c = 0, mb = 1;
+    if (std::sscanf(env, "%d,%d,%d", &nt, &c, &mb) >= 2) {
+      int mc = track_max_clusters(nt, mb, c);
       if (mc > 0) {
-        TuneChoice tc{nt, c, mc, 0.f};
+        TuneChoice tc{nt, mb, c, mc, 0.f};
         ctx->tune_cache[key] = tc;
         *out = tc;
         return LSDG_OK;
@@ -361,11 +363,13 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
   TuneChoice best;
   best.threads = 0;
   float best_ms = 1e30f;
-  for (int nt : kCandThreads)
+  for (int si = 0; si < track_shape_count(); ++si)
     for (int c : kCandCluster) {
-      int mc = track_max_clusters(nt, c);
+      int nt = 0, mb = 0;
+      track_shape(si, &nt, &mb);
+      int mc = track_max_clusters(nt, mb, c);
       if (mc <= 0) continue;
-      TuneChoice tc{nt, c, mc};
+      TuneChoice tc{nt, mb, c, mc, 0.f};
       float t_best = 1e30f;
       for (int rep = 0; rep < 2; ++rep) {
         CK(ctx, cudaEventRecord(e0, ctx->stream));
@@ -391,8 +395,8 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
   return LSDG_OK;
 }
 
-extern "C" lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int key_len, int* threads, int* cluster,
-                                      int* max_clusters, float* ms) {
+extern "C" lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int key_len, int* threads, int* minblocks,
+                                      int* cluster, int* max_clusters, float* ms) {
   if (!ctx) return LSDG_INVALID_ARG;
   int i = 0;
   for (auto& kv : ctx->tune_cache) {
@@ -402,6 +406,7 @@ extern "C" lsdg_status lsdg_tune_info(lsdg_ctx* ctx, int index, char* key, int k
       key[key_len - 1] = 0;
     }
     if (threads) *threads = kv.second.threads;
+    if (minblocks) *minblocks = kv.second.minblocks;
     if (cluster) *cluster = kv.second.cluster;
     if (max_clusters) *max_clusters = kv.second.max_clusters;
     if (ms) *ms = kv.second.tuned_ms;
@@ -573,7 +578,7 @@ static lsdg_status track_one(lsdg_ctx* ctx, const lsdg_frame* ref, const lsdg_fr
   std::snprintf(key, sizeof(key), "one:%dx%d", R.w, R.h);
   TuneChoice tc;
   if (eval_only) {
-    tc = TuneChoice{256, 8, 1};  // a single pass: any shape, deterministic for the parity tests
+    tc = TuneChoice{256, 2, 8, 1, 0.f};  // a single pass: any shape, deterministic for the parity tests
   } else {
     lsdg_status st = autotune(ctx, key, a, &tc);
     if (st != LSDG_OK) return st;

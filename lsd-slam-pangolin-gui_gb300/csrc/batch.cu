@@ -289,9 +289,11 @@ lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* b, int64_t* passes, doubl
 }
 
 // The tile shape the autotuner chose for this batch.
-lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* b, int* threads, int* cluster, int* clusters, int* launches_per_run) {
+lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* b, int* threads, int* minblocks, int* cluster, int* clusters,
+                             int* launches_per_run) {
   if (!ctx || !b) return LSDG_INVALID_ARG;
   if (threads) *threads = b->tc.threads;
+  if (minblocks) *minblocks = b->tc.minblocks;
   if (cluster) *cluster = b->tc.cluster;
   if (clusters) *clusters = std::min(b->n, b->tc.max_clusters);
   if (launches_per_run) *launches_per_run = b->launches_per_run;

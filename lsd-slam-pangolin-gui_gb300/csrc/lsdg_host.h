@@ -13,6 +13,7 @@ constexpr size_t kSmallBytes = 4096;
 
 struct TuneChoice {
   int threads = 256;
+  int minblocks = 2;
   int cluster = 8;
   int max_clusters = 1;
   float tuned_ms = 0.f;

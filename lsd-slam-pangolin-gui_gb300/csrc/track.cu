@@ -24,8 +24,9 @@
 // without global-memory scratch for the reduction.  The one-pair form (lsdg_track_se3) is the same
 // kernel with a single cluster.
 //
-// Arithmetic: FP32 residuals/weights/Jacobians (built with -fmad=false so that each operation
-// rounds exactly as in the CPU oracle), Kahan-compensated sums, FP64 only in the LM step.
+// Arithmetic: FP32 residuals/weights/Jacobians (this translation unit is built with FMA contraction,
+// so per-point values differ from the CPU oracle in the last bits; parity is by tolerance),
+// Kahan-compensated sums, FP64 only in the LM step.
 #include <cooperative_groups.h>
 
 #include "lsdg_internal.cuh"
@@ -342,8 +343,8 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
 // ------------------------------------------------------------------------------------------
 // The persistent cluster kernel
 // ------------------------------------------------------------------------------------------
-template <int NT>
-__global__ void __launch_bounds__(NT) track_se3_kernel(const TrackArgs a) {
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) {
   constexpr int NW = NT / 32;
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
@@ -541,9 +542,10 @@ __global__ void __launch_bounds__(NT) track_se3_kernel(const TrackArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Host side: launch with a cluster shape
+// Host side: launch with a cluster shape.  Shapes are (threads per CTA, CTAs the register budget
+// must leave room for on one SM); the autotuner picks one together with the cluster size.
 // ------------------------------------------------------------------------------------------
-template <int NT>
+template <int NT, int MINB>
 static cudaError_t launch_nt(const TrackArgs& a, int cluster, int n_clusters, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster * n_clusters);
@@ -557,10 +559,10 @@ static cudaError_t launch_nt(const TrackArgs& a, int cluster, int n_clusters, cu
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, track_se3_kernel<NT>, a);
+  return cudaLaunchKernelEx(&cfg, track_se3_kernel<NT, MINB>, a);
 }
 
-template <int NT>
+template <int NT, int MINB>
 static int max_clusters_nt(int cluster) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster);
@@ -573,38 +575,59 @@ static int max_clusters_nt(int cluster) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, track_se3_kernel<NT>, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, track_se3_kernel<NT, MINB>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return n;
 }
 
+#define LSDG_TRACK_SHAPES(X) X(128, 4) X(128, 8) X(256, 2) X(256, 4) X(512, 1) X(512, 2)
+
 // Allows clusters of up to 16 CTAs (non-portable size) for every instantiation.  Called once
 // per context, outside any stream capture.
 cudaError_t track_prepare() {
-  cudaError_t e = cudaFuncSetAttribute(track_se3_kernel<128>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(track_se3_kernel<256>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(track_se3_kernel<512>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaError_t e = cudaSuccess;
+#define X(nt, mb) \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(track_se3_kernel<nt, mb>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  LSDG_TRACK_SHAPES(X)
+#undef X
   return e;
 }
 
-cudaError_t launch_track(const TrackArgs& a, int threads, int cluster, int n_clusters, cudaStream_t s) {
-  switch (threads) {
-    case 128: return launch_nt<128>(a, cluster, n_clusters, s);
-    case 256: return launch_nt<256>(a, cluster, n_clusters, s);
-    case 512: return launch_nt<512>(a, cluster, n_clusters, s);
-    default: return cudaErrorInvalidValue;
-  }
+int track_shape_count() {
+  int n = 0;
+#define X(nt, mb) ++n;
+  LSDG_TRACK_SHAPES(X)
+#undef X
+  return n;
 }
 
-int track_max_clusters(int threads, int cluster) {
-  switch (threads) {
-    case 128: return max_clusters_nt<128>(cluster);
-    case 256: return max_clusters_nt<256>(cluster);
-    case 512: return max_clusters_nt<512>(cluster);
-    default: return 0;
+void track_shape(int i, int* threads, int* minblocks) {
+  int k = 0;
+#define X(nt, mb)       \
+  if (k++ == i) {       \
+    *threads = nt;      \
+    *minblocks = mb;    \
   }
+  LSDG_TRACK_SHAPES(X)
+#undef X
+}
+
+cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s) {
+#define X(nt, mb) \
+  if (threads == nt && minblocks == mb) return launch_nt<nt, mb>(a, cluster, n_clusters, s);
+  LSDG_TRACK_SHAPES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+int track_max_clusters(int threads, int minblocks, int cluster) {
+#define X(nt, mb) \
+  if (threads == nt && minblocks == mb) return max_clusters_nt<nt, mb>(cluster);
+  LSDG_TRACK_SHAPES(X)
+#undef X
+  return 0;
 }
 
 }  // namespace lsdg

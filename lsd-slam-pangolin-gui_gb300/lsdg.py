@@ -75,10 +75,9 @@ def lib():
     _sig(L, "lsdg_batch_read", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_track_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
-    _sig(L, "lsdg_batch_shape", st, [_vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)])
+    _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
-    _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                   C.POINTER(C.c_int), C.POINTER(C.c_float)])
+    _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
     _lib = L
     return L
 
@@ -138,11 +137,12 @@ class Context:
         out, i = [], 0
         buf = C.create_string_buffer(256)
         while True:
-            t, c, m, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
-            rc = lib().lsdg_tune_info(self._h, i, buf, 256, C.byref(t), C.byref(c), C.byref(m), C.byref(ms))
+            t, mb, c, m, ms = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_float()
+            rc = lib().lsdg_tune_info(self._h, i, buf, 256, C.byref(t), C.byref(mb), C.byref(c), C.byref(m), C.byref(ms))
             if rc != T.OK:
                 return out
-            out.append({"key": buf.value.decode(), "threads": t.value, "cluster": c.value, "clusters": m.value, "ms": ms.value})
+            out.append({"key": buf.value.decode(), "threads": t.value, "minblocks": mb.value, "cluster": c.value,
+                        "clusters": m.value, "ms": ms.value})
             i += 1
 
     def close(self):
@@ -288,9 +288,11 @@ class Batch:
         return a.value, b.value
 
     def shape(self):
-        t, c, n, k = C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        self.ctx.check(lib().lsdg_batch_shape(self.ctx.handle, self._h, C.byref(t), C.byref(c), C.byref(n), C.byref(k)))
-        return {"threads": t.value, "cluster": c.value, "clusters": n.value, "launches_per_run": k.value}
+        t, mb, c, n, k = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self.ctx.check(lib().lsdg_batch_shape(self.ctx.handle, self._h, C.byref(t), C.byref(mb), C.byref(c), C.byref(n),
+                                              C.byref(k)))
+        return {"threads": t.value, "minblocks": mb.value, "cluster": c.value, "clusters": n.value,
+                "launches_per_run": k.value}
 
     def work(self):
         p, b, u = C.c_int64(), C.c_double(), C.c_double()
