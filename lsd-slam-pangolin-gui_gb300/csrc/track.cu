@@ -14,12 +14,15 @@
 //      first pass of a level fixes each point's residual variance in the psig scratch array (and
 //      leaves out points that do not land border_margin pixels inside the image), so each level
 //      minimises one fixed, continuous energy whose gradient is exactly 2 J^T W r;
-//   2. warp shuffles merge the compensated pairs, then a fixed-order block merge in shared memory;
-//   3. cluster.sync(); rank 0 merges the C block partials through distributed shared memory (fixed
-//      rank order, so the result is deterministic for a given C and NT);
-//   4. thread 0 of rank 0 runs the LM step in FP64 (6x6 LDLT, se(3) exp, composition, accept /
-//      reject, convergence and level changes) and publishes the next pose in its shared memory;
-//   5. cluster.sync(); every CTA reads the pose through DSMEM and starts the next pass.
+//   2. warp shuffles merge the compensated pairs (reduce-scatter), then a fixed-order block merge;
+//   2'. every CTA stores its partial straight into rank 0's shared memory (distributed shared
+//      memory stores, no global-memory scratch); cluster.sync(); rank 0 merges the C partials in
+//      fixed rank order, so the result is deterministic for a given C and NT;
+//   4. warp 0 of rank 0 runs the LM step in FP64: three lanes solve the 6x6 systems the decision
+//      may need (undamped; damped if accepted; damped if rejected) in parallel with register-
+//      resident LDL^T, then lane 0 decides (accept / reject, convergence, level changes), applies
+//      the se(3) exp and composition, and writes the next pose into every rank's shared memory;
+//   5. cluster.sync(); every CTA reads the pose from its own shared memory and starts the next pass.
 // The whole LM loop over all levels therefore runs on the device without a host round trip and
 // without global-memory scratch for the reduction.  The one-pair form (lsdg_track_se3) is the same
 // kernel with a single cluster.
@@ -88,6 +91,7 @@ struct LMState {
   double S[32];     // sums of the last accepted pass
   double E, lambda, gnmax;
   int it, phase, level, pair, have_final, fresh;
+  int s_src;  // 0: lm.S holds the sums of the pass just merged, 1: of an earlier pass
   lsdg_track_stats st;
 };
 
@@ -147,42 +151,67 @@ __device__ __noinline__ void se3_exp_mul_d(const double* xi, const double* Tin, 
   for (int i = 0; i < 12; ++i) Tout[i] = o[i];
 }
 
-// (H + lambda diag H) x = -g, H given as its upper triangle.  False if a pivot is not positive.
-__device__ __noinline__ bool ldlt_solve_d(int n, const double* hu, const double* g, double lambda, double* x) {
-  double A[7][7], L[7][7], d[7], y[7];
-  int q = 0;
-  for (int i = 0; i < n; ++i)
-    for (int j = i; j < n; ++j) {
-      A[i][j] = hu[q];
-      A[j][i] = hu[q];
-      ++q;
+// (H + lambda diag H) x = -g for N x N symmetric H given as its upper triangle (row-major), by an
+// LDL^T factorisation held entirely in registers (every loop has compile-time bounds).  Returns
+// false when a pivot is not positive.
+template <int N>
+__device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, const double* __restrict__ g,
+                                               double lambda, double* x) {
+  double L[N * (N + 1) / 2];
+  double d[N], id[N], y[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) L[i * (i + 1) / 2 + j] = hu[j * N - (j * (j - 1)) / 2 + (i - j)];
+#pragma unroll
+  for (int i = 0; i < N; ++i) L[i * (i + 1) / 2 + i] *= (1.0 + lambda);
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    double sj = L[j * (j + 1) / 2 + j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) sj -= (L[j * (j + 1) / 2 + k] * L[j * (j + 1) / 2 + k]) * d[k];
+    ok = ok && (sj > 1e-30);
+    d[j] = sj;
+    id[j] = 1.0 / sj;
+#pragma unroll
+    for (int i = j + 1; i < N; ++i) {
+      double t = L[i * (i + 1) / 2 + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) t -= (L[i * (i + 1) / 2 + k] * L[j * (j + 1) / 2 + k]) * d[k];
+      L[i * (i + 1) / 2 + j] = t * id[j];
     }
-  for (int i = 0; i < n; ++i) A[i][i] = A[i][i] * (1.0 + lambda);
-  for (int j = 0; j < n; ++j) {
-    double s = A[j][j];
-    for (int k = 0; k < j; ++k) s = s - (L[j][k] * L[j][k]) * d[k];
-    if (!(s > 1e-30)) return false;
-    d[j] = s;
-    L[j][j] = 1.0;
-    for (int i = j + 1; i < n; ++i) {
-      double t = A[i][j];
-      for (int k = 0; k < j; ++k) t = t - (L[i][k] * L[j][k]) * d[k];
-      L[i][j] = t / s;
-    }
   }
-  for (int i = 0; i < n; ++i) {
-    double s = -g[i];
-    for (int k = 0; k < i; ++k) s = s - L[i][k] * y[k];
-    y[i] = s;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    double si = -g[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) si -= L[i * (i + 1) / 2 + k] * y[k];
+    y[i] = si;
   }
-  for (int i = 0; i < n; ++i) y[i] = y[i] / d[i];
-  for (int i = n - 1; i >= 0; --i) {
-    double s = y[i];
-    for (int k = i + 1; k < n; ++k) s = s - L[k][i] * x[k];
-    x[i] = s;
+#pragma unroll
+  for (int i = 0; i < N; ++i) y[i] *= id[i];
+#pragma unroll
+  for (int i = N - 1; i >= 0; --i) {
+    double si = y[i];
+#pragma unroll
+    for (int k = i + 1; k < N; ++k) si -= L[k * (k + 1) / 2 + i] * x[k];
+    x[i] = si;
   }
-  return true;
+  return ok;
 }
+
+// Solves computed ahead of the LM decision by three lanes of warp 0 at once (same instruction
+// stream, different data): [0] undamped step of the new pass, [1] damped step if the new pass is
+// accepted (or is a level's first pass), [2] damped step on the old linearisation if it is
+// rejected.  The decision logic takes an entry only when its source and lambda match exactly.
+struct SolveCache {
+  double x[3][6];
+  double lambda[3];
+  int src[3];  // 0: the sums of the pass just merged, 1: the sums kept from an earlier pass
+  int ok[3];
+  int valid[3];
+};
 
 // ------------------------------------------------------------------------------------------
 // LM control (thread 0 of cluster rank 0)
@@ -272,16 +301,28 @@ __device__ void next_level(const TrackArgs& a, LMState& lm, Ctl& ctl) {
   fetch_pair(a, lm, ctl);
 }
 
+__device__ __forceinline__ bool cached_solve(LMState& lm, SolveCache& sc, double lambda, double* x) {
+#pragma unroll 1
+  for (int k = 0; k < 3; ++k) {
+    if (sc.valid[k] && sc.src[k] == lm.s_src && sc.lambda[k] == lambda) {
+      for (int i = 0; i < 6; ++i) x[i] = sc.x[k][i];
+      sc.valid[k] = 0;
+      return sc.ok[k] != 0;
+    }
+  }
+  return ldlt_solve_reg<6>(lm.S, lm.S + 21, lambda, x);
+}
+
 // One LM iteration decision on the current linearisation lm.S (same rules as the CPU oracle):
 // converged when the undamped Gauss-Newton step is below step_eps * 2^level; otherwise solve the
 // damped system and publish the trial pose, unless the level's iteration budget is spent.
-__device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl) {
+__device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& sc) {
   const double thr = a.step_eps * (double)(1 << lm.level);
   for (;;) {
     if (lm.fresh) {
       double gn[6];
       lm.gnmax = 1e300;
-      if (ldlt_solve_d(6, lm.S, lm.S + 21, 0.0, gn)) {
+      if (cached_solve(lm, sc, 0.0, gn)) {
         double m = 0;
         for (int i = 0; i < 6; ++i) m = fmax(m, fabs(gn[i]));
         lm.gnmax = m;
@@ -292,7 +333,7 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl) {
     if (lm.it >= a.max_iter[lm.level]) break;
     lm.it++;
     double dx[6];
-    if (!ldlt_solve_d(6, lm.S, lm.S + 21, lm.lambda, dx)) {
+    if (!cached_solve(lm, sc, lm.lambda, dx)) {
       lm.lambda *= a.lambda_up;
       continue;
     }
@@ -307,18 +348,19 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl) {
   next_level(a, lm, ctl);
 }
 
-__device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ctl, const double* tot) {
+__device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ctl, const double* tot, SolveCache& sc) {
   lm.st.passes[lm.level]++;
   const double N = tot[28];
   if (lm.phase == PH_INIT) {
     if (N > 0) {
       for (int i = 0; i < 32; ++i) lm.S[i] = tot[i];
+      lm.s_src = 0;
       lm.E = tot[27] / N;
       lm.lambda = a.lambda0;
       lm.it = 0;
       lm.fresh = 1;
       if (lm.level == a.bottom_level) lm.have_final = 1;
-      try_step(a, lm, ctl);
+      try_step(a, lm, ctl, sc);
     } else {
       next_level(a, lm, ctl);
     }
@@ -327,22 +369,64 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
   if (N > 0 && tot[27] / N < lm.E) {
     for (int i = 0; i < 12; ++i) lm.T[i] = lm.Ttry[i];
     for (int i = 0; i < 32; ++i) lm.S[i] = tot[i];
+    lm.s_src = 0;
     lm.E = tot[27] / N;
     lm.lambda *= a.lambda_down;
     lm.fresh = 1;
   } else {
+    lm.s_src = 1;
     if (lm.gnmax < a.stall_eps * (double)(1 << lm.level)) {  // noise floor of this level
       next_level(a, lm, ctl);
       return;
     }
     lm.lambda *= a.lambda_up;
   }
-  try_step(a, lm, ctl);
+  try_step(a, lm, ctl, sc);
+}
+
+// Lanes 0..2 of warp 0 (cluster rank 0) solve the three systems the decision may need, in parallel.
+__device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm, const double* tot, SolveCache& sc,
+                                          int lane) {
+  if (lane < 3) {
+    const bool init = lm.phase == PH_INIT;
+    const double* S = lane == 2 ? lm.S : tot;
+    const double lam = lane == 0 ? 0.0 : lane == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down) : lm.lambda * a.lambda_up;
+    double x[6];
+    const bool ok = ldlt_solve_reg<6>(S, S + 21, lam, x);
+    const bool useful = tot[28] > 0 && (lane < 2 || !init);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) sc.x[lane][i] = x[i];
+    sc.lambda[lane] = lam;
+    sc.src[lane] = lane == 2 ? 1 : 0;
+    sc.ok[lane] = ok ? 1 : 0;
+    sc.valid[lane] = useful ? 1 : 0;
+  }
 }
 
 // ------------------------------------------------------------------------------------------
 // The persistent cluster kernel
 // ------------------------------------------------------------------------------------------
+constexpr int kMaxCluster = 16;
+
+// Merge of the 28 compensated sums of a warp by reduce-scatter: after five halving rounds (31
+// shuffle pairs instead of the 140 of a butterfly) lane l holds the warp total of sum l.
+__device__ __forceinline__ void warp_reduce_scatter(float (&s)[32], float (&c)[32], int lane) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < o; ++i) {
+      const float ks = up ? s[i + o] : s[i], kc = up ? c[i + o] : c[i];
+      const float ss = up ? s[i] : s[i + o], sc = up ? c[i] : c[i + o];
+      const float rs = __shfl_xor_sync(0xffffffffu, ss, o), rc = __shfl_xor_sync(0xffffffffu, sc, o);
+      float ns = ks, nc = kc;
+      kmerge(ns, nc, rs, rc);
+      s[i] = ns;
+      c[i] = nc;
+    }
+  }
+}
+
 template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) {
   constexpr int NW = NT / 32;
@@ -354,20 +438,30 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
   __shared__ float ws[NW][kSums];
   __shared__ float wc[NW][kSums];
   __shared__ int wn[NW][3];
-  __shared__ CtaPart part;
-  __shared__ Ctl ctl;
+  __shared__ CtaPart allpart[kMaxCluster];  // rank 0's copy receives every rank's partial
+  __shared__ Ctl ctl;                       // every rank's copy is written by rank 0
   __shared__ double tot[32];
   __shared__ LMState lm;
+  __shared__ SolveCache sc;
 
-  if (rank == 0 && tid == 0) fetch_pair(a, lm, ctl);
+  // rank 0 publishes the control word to the other ranks' shared memory
+  auto push_ctl = [&]() {
+    if (lane >= 1 && lane < (int)C) {
+      int* dst = reinterpret_cast<int*>(cluster.map_shared_rank(&ctl, (unsigned)lane));
+      const int* src = reinterpret_cast<const int*>(&ctl);
+#pragma unroll
+      for (int i = 0; i < (int)(sizeof(Ctl) / 4); ++i) dst[i] = src[i];
+    }
+  };
+
+  if (rank == 0 && wid == 0) {
+    if (lane == 0) fetch_pair(a, lm, ctl);
+    __syncwarp();
+    push_ctl();
+  }
   cluster.sync();
 
   for (;;) {
-    if (rank != 0 && tid < (int)(sizeof(Ctl) / 4)) {
-      const int* src = reinterpret_cast<const int*>(cluster.map_shared_rank(&ctl, 0));
-      reinterpret_cast<int*>(&ctl)[tid] = src[tid];
-    }
-    __syncthreads();
     const int pair = ctl.pair;
     if (pair < 0) break;
     const int level = ctl.level;
@@ -481,59 +575,64 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
       kadd(es, ec, rho);
     }
 
-    // warp merge
+    // warp merge (reduce-scatter: lane l ends with sum l), then a fixed-order merge over warps
+    {
+      float S[32], Cc[32];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+      for (int i = 0; i < 21; ++i) { S[i] = hs[i]; Cc[i] = hc[i]; }
 #pragma unroll
-      for (int i = 0; i < 21; ++i) kmerge(hs[i], hc[i], __shfl_xor_sync(0xffffffffu, hs[i], o), __shfl_xor_sync(0xffffffffu, hc[i], o));
+      for (int i = 0; i < 6; ++i) { S[21 + i] = gs[i]; Cc[21 + i] = gc[i]; }
+      S[27] = es;
+      Cc[27] = ec;
 #pragma unroll
-      for (int i = 0; i < 6; ++i) kmerge(gs[i], gc[i], __shfl_xor_sync(0xffffffffu, gs[i], o), __shfl_xor_sync(0xffffffffu, gc[i], o));
-      kmerge(es, ec, __shfl_xor_sync(0xffffffffu, es, o), __shfl_xor_sync(0xffffffffu, ec, o));
-    }
-    good = __reduce_add_sync(0xffffffffu, good);
-    bad = __reduce_add_sync(0xffffffffu, bad);
-    oob = __reduce_add_sync(0xffffffffu, oob);
-    if (lane == 0) {
-#pragma unroll
-      for (int i = 0; i < 21; ++i) { ws[wid][i] = hs[i]; wc[wid][i] = hc[i]; }
-#pragma unroll
-      for (int i = 0; i < 6; ++i) { ws[wid][21 + i] = gs[i]; wc[wid][21 + i] = gc[i]; }
-      ws[wid][27] = es;
-      wc[wid][27] = ec;
-      wn[wid][0] = good;
-      wn[wid][1] = bad;
-      wn[wid][2] = oob;
+      for (int i = 28; i < 32; ++i) { S[i] = 0.f; Cc[i] = 0.f; }
+      warp_reduce_scatter(S, Cc, lane);
+      good = __reduce_add_sync(0xffffffffu, good);
+      bad = __reduce_add_sync(0xffffffffu, bad);
+      oob = __reduce_add_sync(0xffffffffu, oob);
+      if (lane < kSums) {
+        ws[wid][lane] = S[0];
+        wc[wid][lane] = Cc[0];
+      } else if (lane == kSums) {
+        wn[wid][0] = good;
+        wn[wid][1] = bad;
+        wn[wid][2] = oob;
+      }
     }
     __syncthreads();
+    // this CTA's partial goes straight into rank 0's shared memory
     if (tid < kSums) {
       float s = 0.f, c = 0.f;
       for (int k = 0; k < NW; ++k) kmerge(s, c, ws[k][tid], wc[k][tid]);
-      part.s[tid] = s;
-      part.c[tid] = c;
+      CtaPart* dst = cluster.map_shared_rank(&allpart[rank], 0u);
+      dst->s[tid] = s;
+      dst->c[tid] = c;
     } else if (tid < kSums + 3) {
       int v = 0;
       for (int k = 0; k < NW; ++k) v += wn[k][tid - kSums];
-      part.cnt[tid - kSums] = v;
+      cluster.map_shared_rank(&allpart[rank], 0u)->cnt[tid - kSums] = v;
     }
     cluster.sync();
 
     if (rank == 0) {
       if (tid < kSums) {
         float s = 0.f, c = 0.f;
-        for (unsigned r = 0; r < C; ++r) {
-          const CtaPart* pr = cluster.map_shared_rank(&part, r);
-          kmerge(s, c, pr->s[tid], pr->c[tid]);
-        }
+        for (unsigned r = 0; r < C; ++r) kmerge(s, c, allpart[r].s[tid], allpart[r].c[tid]);
         tot[tid] = (double)s - (double)c;
       } else if (tid < kSums + 3) {
         int v = 0;
-        for (unsigned r = 0; r < C; ++r) v += cluster.map_shared_rank(&part, r)->cnt[tid - kSums];
+        for (unsigned r = 0; r < C; ++r) v += allpart[r].cnt[tid - kSums];
         tot[tid + 1] = (double)v;  // 29 good, 30 bad, 31 out of image
       }
       __syncthreads();
-      if (tid == 0) {
-        tot[28] = tot[29] + tot[30];
-        lm_advance(a, lm, ctl, tot);
+      if (wid == 0) {
+        if (lane == 0) tot[28] = tot[29] + tot[30];
+        __syncwarp();
+        speculate(a, lm, tot, sc, lane);
+        __syncwarp();
+        if (lane == 0) lm_advance(a, lm, ctl, tot, sc);
+        __syncwarp();
+        push_ctl();
       }
     }
     cluster.sync();
