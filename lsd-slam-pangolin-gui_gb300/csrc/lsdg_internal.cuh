@@ -16,7 +16,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/lsdg.h"
+#include "lsdg.h"  // include/ is on the include path (build_lib.py)
 
 namespace lsdg {
 
