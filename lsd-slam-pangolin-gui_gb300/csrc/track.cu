@@ -92,6 +92,8 @@ struct LMState {
   double E, lambda, gnmax;
   int it, phase, level, pair, have_final, fresh;
   int s_src;  // 0: lm.S holds the sums of the pass just merged, 1: of an earlier pass
+  int need_exp;  // try_step chose dx: the warp applies exp(dx) * T and publishes the trial pose
+  double dx[6];
   lsdg_track_stats st;
 };
 
@@ -106,49 +108,62 @@ __device__ __noinline__ void se3_inv_d(const double* A, double* B) {
   for (int i = 0; i < 12; ++i) B[i] = o[i];
 }
 
-__device__ __noinline__ void se3_exp_mul_d(const double* xi, const double* Tin, double* Tout) {
-  const double v0 = xi[0], v1 = xi[1], v2 = xi[2], w0 = xi[3], w1 = xi[4], w2 = xi[5];
-  const double th2 = w0 * w0 + w1 * w1 + w2 * w2;
-  const double th = sqrt(th2);
-  double A, B, Cc;
-  if (th < 1e-4) {
-    A = 1.0 - th2 / 6.0;
-    B = 0.5 - th2 / 24.0;
-    Cc = 1.0 / 6.0 - th2 / 120.0;
+// On GB300 one FP64 warp instruction holds a sub-partition's FP64 pipe for ~64 cycles however few
+// lanes are active, so the FP64 parts below are written lane-parallel: each lane owns one matrix
+// element or row, and the instruction count on the critical path is what is minimised.
+
+// Coefficients of the se(3) exp (A = sin t / t, B = (1 - cos t) / t^2, C = (t - sin t) / t^3 with
+// t^2 = th2): Taylor series in t^2 through t^10 for t < 0.05 (no sqrt, sincos or division),
+// closed form otherwise.  Same rule as the CPU oracle.
+__device__ __forceinline__ void se3_coeffs(double th2, double& A, double& B, double& C) {
+  if (th2 < 0.0025) {
+    A = 1.0 + th2 * (-1.0 / 6.0 + th2 * (1.0 / 120.0 + th2 * (-1.0 / 5040.0 + th2 * (1.0 / 362880.0 + th2 * (-1.0 / 39916800.0)))));
+    B = 0.5 + th2 * (-1.0 / 24.0 + th2 * (1.0 / 720.0 + th2 * (-1.0 / 40320.0 + th2 * (1.0 / 3628800.0 + th2 * (-1.0 / 479001600.0)))));
+    C = 1.0 / 6.0 + th2 * (-1.0 / 120.0 + th2 * (1.0 / 5040.0 + th2 * (-1.0 / 362880.0 + th2 * (1.0 / 39916800.0 + th2 * (-1.0 / 6227020800.0)))));
   } else {
-    double s, c;
-    sincos(th, &s, &c);
-    A = s / th;
-    B = (1.0 - c) / th2;
-    Cc = (th - s) / (th2 * th);
+    const double th = sqrt(th2);
+    double sn, cs;
+    sincos(th, &sn, &cs);
+    A = sn / th;
+    B = (1.0 - cs) / th2;
+    C = (th - sn) / (th2 * th);
   }
-  const double K[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
-  double K2[9], E[12];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double s = 0;
-      for (int k = 0; k < 3; ++k) s = s + K[3 * i + k] * K[3 * k + j];
-      K2[3 * i + j] = s;
-    }
-  double R[9], V[9];
-  for (int i = 0; i < 9; ++i) {
-    const double I = (i % 4 == 0) ? 1.0 : 0.0;
-    R[i] = (I + A * K[i]) + B * K2[i];
-    V[i] = (I + B * K[i]) + Cc * K2[i];
-  }
-  for (int i = 0; i < 3; ++i) {
-    E[4 * i + 0] = R[3 * i + 0];
-    E[4 * i + 1] = R[3 * i + 1];
-    E[4 * i + 2] = R[3 * i + 2];
-    E[4 * i + 3] = (V[3 * i + 0] * v0 + V[3 * i + 1] * v1) + V[3 * i + 2] * v2;
-  }
-  double o[12];
-  for (int i = 0; i < 3; ++i) {
-    for (int j = 0; j < 3; ++j)
-      o[4 * i + j] = (E[4 * i + 0] * Tin[j] + E[4 * i + 1] * Tin[4 + j]) + E[4 * i + 2] * Tin[8 + j];
-    o[4 * i + 3] = ((E[4 * i + 0] * Tin[3] + E[4 * i + 1] * Tin[7]) + E[4 * i + 2] * Tin[11]) + E[4 * i + 3];
-  }
-  for (int i = 0; i < 12; ++i) Tout[i] = o[i];
+}
+
+// Tout = exp(xi) * Tin (3x4 row-major), computed by a whole warp: lane e < 9 builds element e of
+// R and V, lanes 0..2 the translation, lane o < 12 one element of the product.  xi, Tin, Tout are
+// in shared memory; every lane must call.
+__device__ __forceinline__ void warp_exp_mul(const double* xi, const double* Tin, double* Tout, int lane) {
+  const double v0 = xi[0], v1 = xi[1], v2 = xi[2], w0 = xi[3], w1 = xi[4], w2 = xi[5];
+  const double th2 = (w0 * w0 + w1 * w1) + w2 * w2;
+  double A, B, Cc;
+  se3_coeffs(th2, A, B, Cc);
+  const int e = lane < 9 ? lane : 0;
+  const int i = e / 3, j = e % 3;
+  const double wi = i == 0 ? w0 : i == 1 ? w1 : w2;
+  const double wj = j == 0 ? w0 : j == 1 ? w1 : w2;
+  // K = [w]x: K01 = -w2, K02 = w1, K10 = w2, K12 = -w0, K20 = -w1, K21 = w0
+  const double K = e == 1 ? -w2 : e == 2 ? w1 : e == 3 ? w2 : e == 5 ? -w0 : e == 6 ? -w1 : e == 7 ? w0 : 0.0;
+  const double I = (i == j) ? 1.0 : 0.0;
+  const double K2 = wi * wj - ((i == j) ? th2 : 0.0);
+  const double R = (I + A * K) + B * K2;
+  const double V = (I + B * K) + Cc * K2;
+  // translation t_i = V_i0 v0 + V_i1 v1 + V_i2 v2 (lanes 0..2 gather their row of V)
+  const int tr = lane < 3 ? lane : 0;
+  const double V0 = __shfl_sync(0xffffffffu, V, 3 * tr + 0);
+  const double V1 = __shfl_sync(0xffffffffu, V, 3 * tr + 1);
+  const double V2 = __shfl_sync(0xffffffffu, V, 3 * tr + 2);
+  const double t = (V0 * v0 + V1 * v1) + V2 * v2;
+  // product: out[r][c] = sum_k E[r][k] Tin[k][c] (+ E[r][3] for c == 3)
+  const int o = lane < 12 ? lane : 0;
+  const int r = o / 4, c = o % 4;
+  const double E0 = __shfl_sync(0xffffffffu, R, 3 * r + 0);
+  const double E1 = __shfl_sync(0xffffffffu, R, 3 * r + 1);
+  const double E2 = __shfl_sync(0xffffffffu, R, 3 * r + 2);
+  const double Et = __shfl_sync(0xffffffffu, t, r);
+  double out = (E0 * Tin[c] + E1 * Tin[4 + c]) + E2 * Tin[8 + c];
+  if (c == 3) out = out + Et;
+  if (lane < 12) Tout[o] = out;
 }
 
 // (H + lambda diag H) x = -g for N x N symmetric H given as its upper triangle (row-major), by an
@@ -201,17 +216,79 @@ __device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, co
   return ok;
 }
 
-// Solves computed ahead of the LM decision by three lanes of warp 0 at once (same instruction
-// stream, different data): [0] undamped step of the new pass, [1] damped step if the new pass is
-// accepted (or is a level's first pass), [2] damped step on the old linearisation if it is
-// rejected.  The decision logic takes an entry only when its source and lambda match exactly.
+// Solves computed ahead of the LM decision by warp 0, four systems at once (lanes 8g .. 8g+5 own
+// the rows of system g): [0] undamped step of the pass just merged, [1] damped step if that pass is
+// accepted (or is a level's first pass), [2] and [3] damped steps on the kept linearisation after
+// one or two rejections.  The decision logic takes an entry only when source and lambda match.
 struct SolveCache {
-  double x[3][6];
-  double lambda[3];
-  int src[3];  // 0: the sums of the pass just merged, 1: the sums kept from an earlier pass
-  int ok[3];
-  int valid[3];
+  double x[4][6];
+  double lambda[4];
+  int src[4];  // 0: the sums of the pass just merged, 1: the sums kept from an earlier pass
+  int ok[4];
+  int valid[4];
+  double Ls[4][6][6];  // per-group L of the factorisation (row-major), for the back substitution
 };
+
+// Row-per-lane LDL^T solve of (H + lambda diag H) x = -g for the group of 8 lanes starting at
+// `base` (rows 0..5; lanes 6, 7 mirror row 5 and their results are dropped).  hu: upper triangle of
+// H (row-major), g: right-hand side, both in shared memory.  About 25 FP64 warp instructions plus
+// six reciprocals, whatever the group count.
+__device__ __forceinline__ void warp_solve6(const double* __restrict__ hu, const double* __restrict__ g, double lambda,
+                                            int lane, double (*Ls)[6], double* xout, int* okout) {
+  const int base = lane & ~7;
+  const int r = (lane & 7) < 6 ? (lane & 7) : 5;
+  double a[6], l[6], wv[6], inv[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    const int lo = r < j ? r : j, hi = r < j ? j : r;
+    a[j] = hu[lo * 6 - (lo * (lo - 1)) / 2 + (hi - lo)];
+    l[j] = 0.0;
+    wv[j] = 0.0;
+  }
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+    if (j == r) a[j] = a[j] * (1.0 + lambda);
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    double t = a[j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) t = t - l[k] * __shfl_sync(0xffffffffu, wv[k], base + j);  // L_rk * (L_jk d_k)
+    const double dj = __shfl_sync(0xffffffffu, t, base + j);
+    ok = ok && (dj > 1e-30);
+    inv[j] = 1.0 / dj;
+    if (r > j) {
+      l[j] = t * inv[j];
+      wv[j] = t;
+    }
+  }
+  // forward: y_r = -g_r - sum_{k<r} L_rk y_k, column by column
+  double y = -g[r];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    const double yk = __shfl_sync(0xffffffffu, y, base + k);
+    if (r > k) y = y - l[k] * yk;
+  }
+  double ir = inv[0];
+#pragma unroll
+  for (int j = 1; j < 6; ++j)
+    if (j == r) ir = inv[j];
+  y = y * ir;
+  // backward: x_r = y_r - sum_{k>r} L_kr x_k (L rows exchanged through shared memory)
+  if ((lane & 7) < 6) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) Ls[r][k] = l[k];
+  }
+  __syncwarp();
+  double x = y;
+#pragma unroll
+  for (int k = 5; k >= 0; --k) {
+    const double xk = __shfl_sync(0xffffffffu, x, base + k);
+    if (r < k) x = x - Ls[k][r] * xk;
+  }
+  if ((lane & 7) < 6) xout[r] = x;
+  if ((lane & 7) == 0) *okout = ok ? 1 : 0;
+}
 
 // ------------------------------------------------------------------------------------------
 // LM control (thread 0 of cluster rank 0)
@@ -279,6 +356,8 @@ __device__ __noinline__ void fetch_pair(const TrackArgs& a, LMState& lm, Ctl& ct
     const int p = a.order ? a.order[k] : k;
     lm.pair = p;
     lm.have_final = 0;
+    lm.need_exp = 0;
+    lm.s_src = 1;
     lm.it = 0;
     lm.E = 0;
     lm.lambda = a.lambda0;
@@ -303,7 +382,7 @@ __device__ void next_level(const TrackArgs& a, LMState& lm, Ctl& ctl) {
 
 __device__ __forceinline__ bool cached_solve(LMState& lm, SolveCache& sc, double lambda, double* x) {
 #pragma unroll 1
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < 4; ++k) {
     if (sc.valid[k] && sc.src[k] == lm.s_src && sc.lambda[k] == lambda) {
       for (int i = 0; i < 6; ++i) x[i] = sc.x[k][i];
       sc.valid[k] = 0;
@@ -337,12 +416,12 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& 
       lm.lambda *= a.lambda_up;
       continue;
     }
-    se3_exp_mul_d(dx, lm.T, lm.Ttry);
+    for (int i = 0; i < 6; ++i) lm.dx[i] = dx[i];
+    lm.need_exp = 1;  // the warp computes lm.Ttry = exp(dx) * lm.T and publishes it
     lm.phase = PH_TRY;
     ctl.pair = lm.pair;
     ctl.level = lm.level;
     ctl.first = 0;
-    publish_pose(ctl, lm.Ttry);
     return;
   }
   next_level(a, lm, ctl);
@@ -384,22 +463,21 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
   try_step(a, lm, ctl, sc);
 }
 
-// Lanes 0..2 of warp 0 (cluster rank 0) solve the three systems the decision may need, in parallel.
+// Warp 0 of cluster rank 0 solves the four systems the decision may need (see SolveCache).
 __device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm, const double* tot, SolveCache& sc,
                                           int lane) {
-  if (lane < 3) {
-    const bool init = lm.phase == PH_INIT;
-    const double* S = lane == 2 ? lm.S : tot;
-    const double lam = lane == 0 ? 0.0 : lane == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down) : lm.lambda * a.lambda_up;
-    double x[6];
-    const bool ok = ldlt_solve_reg<6>(S, S + 21, lam, x);
-    const bool useful = tot[28] > 0 && (lane < 2 || !init);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) sc.x[lane][i] = x[i];
-    sc.lambda[lane] = lam;
-    sc.src[lane] = lane == 2 ? 1 : 0;
-    sc.ok[lane] = ok ? 1 : 0;
-    sc.valid[lane] = useful ? 1 : 0;
+  const int grp = lane >> 3;
+  const bool init = lm.phase == PH_INIT;
+  const double* S = grp >= 2 ? lm.S : tot;
+  const double lam = grp == 0 ? 0.0
+                   : grp == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down)
+                   : grp == 2 ? lm.lambda * a.lambda_up
+                              : (lm.lambda * a.lambda_up) * a.lambda_up;
+  warp_solve6(S, S + 21, lam, lane, sc.Ls[grp], sc.x[grp], &sc.ok[grp]);
+  if ((lane & 7) == 0) {
+    sc.lambda[grp] = lam;
+    sc.src[grp] = grp >= 2 ? 1 : 0;
+    sc.valid[grp] = (tot[28] > 0 && (grp < 2 || !init)) ? 1 : 0;
   }
 }
 
@@ -632,6 +710,18 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
         __syncwarp();
         if (lane == 0) lm_advance(a, lm, ctl, tot, sc);
         __syncwarp();
+        if (lm.need_exp) {
+          warp_exp_mul(lm.dx, lm.T, lm.Ttry, lane);
+          __syncwarp();
+          if (lane < 12) {  // publish the trial pose as float, one element per lane
+            const float f = (float)lm.Ttry[lane];
+            if ((lane & 3) == 3) ctl.t[lane >> 2] = f;
+            else ctl.R[3 * (lane >> 2) + (lane & 3)] = f;
+          }
+          __syncwarp();
+          if (lane == 0) lm.need_exp = 0;
+          __syncwarp();
+        }
         push_ctl();
       }
     }

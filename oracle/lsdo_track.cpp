@@ -348,41 +348,42 @@ static void se3_pass(const Points<T>& P, const FrameLevel<T>& F, const LevelCam&
 // ------------------------------------------------------------------------------------------
 // SE3 in double: exp map, composition, inverse; 6x6 LDLT
 // ------------------------------------------------------------------------------------------
-void se3_exp(const double xi[6], double T[12]) {
-  const double v0 = xi[0], v1 = xi[1], v2 = xi[2], w0 = xi[3], w1 = xi[4], w2 = xi[5];
-  const double th2 = w0 * w0 + w1 * w1 + w2 * w2;
-  const double th = std::sqrt(th2);
-  double A, B, C;
-  if (th < 1e-4) {
-    A = 1.0 - th2 / 6.0;
-    B = 0.5 - th2 / 24.0;
-    C = 1.0 / 6.0 - th2 / 120.0;
+// exp of a twist xi = (v, w): R = I + A K + B K^2, t = (I + B K + C K^2) v with K = [w]x,
+// K^2 = w w^T - |w|^2 I, A = sin(t)/t, B = (1 - cos t)/t^2, C = (t - sin t)/t^3 (t = |w|).  For
+// t < 0.05 the coefficients are their Taylor series in t^2 through t^10 (truncation < 1e-25).
+void se3_coeffs(double th2, double* A, double* B, double* C) {
+  if (th2 < 0.0025) {
+    *A = 1.0 + th2 * (-1.0 / 6.0 + th2 * (1.0 / 120.0 + th2 * (-1.0 / 5040.0 + th2 * (1.0 / 362880.0 + th2 * (-1.0 / 39916800.0)))));
+    *B = 0.5 + th2 * (-1.0 / 24.0 + th2 * (1.0 / 720.0 + th2 * (-1.0 / 40320.0 + th2 * (1.0 / 3628800.0 + th2 * (-1.0 / 479001600.0)))));
+    *C = 1.0 / 6.0 + th2 * (-1.0 / 120.0 + th2 * (1.0 / 5040.0 + th2 * (-1.0 / 362880.0 + th2 * (1.0 / 39916800.0 + th2 * (-1.0 / 6227020800.0)))));
   } else {
-    const double s = std::sin(th), c = std::cos(th);
-    A = s / th;
-    B = (1.0 - c) / th2;
-    C = (th - s) / (th2 * th);
+    const double th = std::sqrt(th2), sn = std::sin(th), cs = std::cos(th);
+    *A = sn / th;
+    *B = (1.0 - cs) / th2;
+    *C = (th - sn) / (th2 * th);
   }
-  // K = [w]x, K2 = K*K
-  const double K[9] = {0, -w2, w1, w2, 0, -w0, -w1, w0, 0};
-  double K2[9];
+}
+
+void se3_exp(const double xi[6], double T[12]) {
+  const double v[3] = {xi[0], xi[1], xi[2]}, w[3] = {xi[3], xi[4], xi[5]};
+  const double th2 = (w[0] * w[0] + w[1] * w[1]) + w[2] * w[2];
+  double A, B, C;
+  se3_coeffs(th2, &A, &B, &C);
+  const double K[9] = {0, -w[2], w[1], w[2], 0, -w[0], -w[1], w[0], 0};
+  double R[9], V[9];
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) {
-      double s = 0;
-      for (int k = 0; k < 3; ++k) s = s + K[3 * i + k] * K[3 * k + j];
-      K2[3 * i + j] = s;
+      const int e = 3 * i + j;
+      const double I = (i == j) ? 1.0 : 0.0;
+      const double K2 = w[i] * w[j] - ((i == j) ? th2 : 0.0);
+      R[e] = (I + A * K[e]) + B * K2;
+      V[e] = (I + B * K[e]) + C * K2;
     }
-  double R[9], Vm[9];
-  for (int i = 0; i < 9; ++i) {
-    const double I = (i % 4 == 0) ? 1.0 : 0.0;
-    R[i] = (I + A * K[i]) + B * K2[i];
-    Vm[i] = (I + B * K[i]) + C * K2[i];
-  }
   for (int i = 0; i < 3; ++i) {
     T[4 * i + 0] = R[3 * i + 0];
     T[4 * i + 1] = R[3 * i + 1];
     T[4 * i + 2] = R[3 * i + 2];
-    T[4 * i + 3] = (Vm[3 * i + 0] * v0 + Vm[3 * i + 1] * v1) + Vm[3 * i + 2] * v2;
+    T[4 * i + 3] = (V[3 * i + 0] * v[0] + V[3 * i + 1] * v[1]) + V[3 * i + 2] * v[2];
   }
 }
 
