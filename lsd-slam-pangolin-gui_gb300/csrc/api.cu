@@ -198,7 +198,7 @@ lsdg_status lsdg_sync(lsdg_ctx* ctx) {
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, const int* h,
-                           const lsdg_intrinsics* intr, const bool* depth, int levels) {
+                           const lsdg_intrinsics* intr, const bool* depth, int levels, bool grads) {
   fs.n = n;
   fs.levels = levels;
   fs.w.assign(w, w + n);
@@ -232,7 +232,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
     for (int l = 0; l < levels; ++l) {
       size_t pix = (size_t)(w[i] >> l) * (h[i] >> l);
       if (l > 0) { r.plane[l] = off; off = al256(off + pix * 4); }
-      r.pyr[l] = off; off = al256(off + pix * 16);
+      if (grads) { r.pyr[l] = off; off = al256(off + pix * 16); }
       if (depth[i]) {
         if (l > 0) {
           r.id[l] = off; off = al256(off + pix * 4);
@@ -262,7 +262,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
     double fx = intr[i].fx, fy = intr[i].fy, cx = intr[i].cx, cy = intr[i].cy;
     for (int l = 0; l < levels; ++l) {
       F.plane[l] = (float*)(base + (l == 0 ? o_plane0[i] : r.plane[l]));
-      F.pyr[l] = (float4*)(base + r.pyr[l]);
+      F.pyr[l] = grads ? (float4*)(base + r.pyr[l]) : nullptr;
       if (depth[i]) {
         F.idepth[l] = (float*)(base + (l == 0 ? o_id0[i] : r.id[l]));
         F.ivar[l] = (float*)(base + (l == 0 ? o_var0[i] : r.var[l]));
@@ -427,7 +427,7 @@ lsdg_status lsdg_frame_create(lsdg_ctx* ctx, int width, int height, const lsdg_i
   lsdg_frame* f = new (std::nothrow) lsdg_frame();
   if (!f) return LSDG_OUT_OF_MEMORY;
   bool depth = true;
-  lsdg_status st = frameset_alloc(ctx, f->fs, 1, &width, &height, intr, &depth, ctx->params.levels);
+  lsdg_status st = frameset_alloc(ctx, f->fs, 1, &width, &height, intr, &depth, ctx->params.levels, true);
   if (st != LSDG_OK) {
     frameset_free(f->fs);
     delete f;

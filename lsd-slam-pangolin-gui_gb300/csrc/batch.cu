@@ -112,7 +112,8 @@ lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int
     dep[i] = true;
     dep[n + i] = false;
   }
-  lsdg_status st = frameset_alloc(ctx, b->fs, 2 * n, w.data(), h.data(), k.data(), dep, ctx->params.levels);
+  // the tracker samples intensity planes only: no gradient pyramid for batch frames
+  lsdg_status st = frameset_alloc(ctx, b->fs, 2 * n, w.data(), h.data(), k.data(), dep, ctx->params.levels, false);
   delete[] dep;
   if (st != LSDG_OK) {
     batch_free(b);

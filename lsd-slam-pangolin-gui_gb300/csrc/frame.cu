@@ -25,8 +25,9 @@ __global__ void u8_to_plane_kernel(const uint8_t* __restrict__ src, float* __res
   if (i < n) dst[i] = (float)src[i];
 }
 
-// Level `level` of every frame: intensity (2x2 mean of level-1, or the input at level 0) and
-// central-difference gradients (zero on the one-pixel border).
+// Level `level` of every frame: intensity (2x2 mean of level-1, or the input at level 0) and, for
+// frames that keep a gradient pyramid, the float4 {I, gx, gy, 0} with central-difference gradients
+// (zero on the one-pixel border).  The tracker samples the intensity planes only.
 __global__ void __launch_bounds__(256) pyramid_level_kernel(const FrameDev* __restrict__ frames, int level) {
   const FrameDev& F = frames[blockIdx.y];
   if (level >= F.levels) return;
@@ -35,8 +36,10 @@ __global__ void __launch_bounds__(256) pyramid_level_kernel(const FrameDev* __re
   if (idx >= w * h) return;
   const int x = idx % w, y = idx / w;
   const bool ix = (x >= 1 && x <= w - 2), iy = (y >= 1 && y <= h - 2);
+  float4* __restrict__ out = F.pyr[level];  // null for frames that only need intensity
   float I, Il = 0.f, Ir = 0.f, Iu = 0.f, Id = 0.f;
   if (level == 0) {
+    if (!out) return;
     const float* P = F.plane[0];
     I = P[idx];
     if (ix) { Il = P[idx - 1]; Ir = P[idx + 1]; }
@@ -45,13 +48,14 @@ __global__ void __launch_bounds__(256) pyramid_level_kernel(const FrameDev* __re
     const float* P = F.plane[level - 1];
     const int pw = 2 * w;
     I = mean4(P, pw, x, y);
+    F.plane[level][idx] = I;
+    if (!out) return;
     if (ix) { Il = mean4(P, pw, x - 1, y); Ir = mean4(P, pw, x + 1, y); }
     if (iy) { Iu = mean4(P, pw, x, y - 1); Id = mean4(P, pw, x, y + 1); }
-    F.plane[level][idx] = I;
   }
   const float gx = ix ? (Ir - Il) * 0.5f : 0.f;
   const float gy = iy ? (Id - Iu) * 0.5f : 0.f;
-  F.pyr[level][idx] = make_float4(I, gx, gy, 0.f);
+  out[idx] = make_float4(I, gx, gy, 0.f);
 }
 
 // Depth pyramid level `level` (level 0: sanitise the upload in place; level l: inverse-variance

@@ -55,7 +55,7 @@ struct lsdg_frame {
 lsdg_status ctx_fail(lsdg_ctx* ctx, lsdg_status st, const char* fmt, ...);
 lsdg_status ctx_cuda(lsdg_ctx* ctx, cudaError_t e, const char* what);
 lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, const int* h, const lsdg_intrinsics* intr,
-                           const bool* depth, int levels);
+                           const bool* depth, int levels, bool grads);
 void frameset_free(FrameSet& fs);
 lsdg::TrackArgs make_track_args(const lsdg_params& p);
 lsdg_status run_tracker(lsdg_ctx* ctx, const lsdg::TrackArgs& a, const TuneChoice& tc);

@@ -2,8 +2,8 @@
 //
 // HBM layout (one "frame" = one camera image with its pyramid; a keyframe also carries depth):
 //   plane[l]   float  [h_l * w_l]   intensity of level l (level 0 is the upload target)
-//   pyr[l]     float4 [h_l * w_l]   {I, gx, gy, 0}: one 16-byte load gives everything bilinear
-//                                   sampling of intensity and gradient needs at one corner
+//   pyr[l]     float4 [h_l * w_l]   {I, gx, gy, 0} (frames that keep gradients: single frames and
+//                                   depth-filter keyframes; batch frames only keep the planes)
 //   idepth[l], ivar[l]  float [h_l * w_l]  keyframe depth pyramid (idepth <= 0: none)
 //   pxyzi[l]   float4 [n_l]         tracking reference points, SoA: {X, Y, Z, I_keyframe}
 //   pvar[l]    float  [n_l]         inverse-depth variance of each point
