@@ -19,8 +19,9 @@
 using namespace lsdg;
 
 namespace lsdg {
-int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
-int launch_frame_points(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
+int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, int max_h, bool with_grads,
+                         cudaStream_t s);
+int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cudaStream_t s);
 void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
 cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s);
 int track_max_clusters(int threads, int minblocks, int cluster);
@@ -206,12 +207,14 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
   fs.intr.assign(intr, intr + n);
   fs.depth.assign(depth, depth + n);
   fs.max_pix = 0;
+  fs.max_h = 0;
   const int mult = 1 << (levels - 1);
   for (int i = 0; i < n; ++i) {
     if (w[i] <= 0 || h[i] <= 0 || w[i] % mult || h[i] % mult || (w[i] >> (levels - 1)) < 4 || (h[i] >> (levels - 1)) < 4)
       return ctx_fail(ctx, LSDG_INVALID_ARG, "frame %d: %dx%d must be positive multiples of %d with >= 4 pixels at the top level", i, w[i], h[i], mult);
     if (!(intr[i].fx > 0) || !(intr[i].fy > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame %d: focal lengths must be > 0", i);
     fs.max_pix = std::max(fs.max_pix, (long)w[i] * h[i]);
+    fs.max_h = std::max(fs.max_h, h[i]);
   }
   // sections: level-0 intensity of every frame back to back, then level-0 idepth and variance of
   // the depth frames back to back (so a batch upload is one copy per kind), then per-frame rest.
@@ -241,7 +244,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         r.pxyzi[l] = off; off = al256(off + pix * 16);
         r.pvar[l] = off; off = al256(off + pix * 4);
         r.psig[l] = off; off = al256(off + pix * 4);
-        r.blk[l] = off; off = al256(off + ((pix + kCountBlock - 1) / kCountBlock) * 4);
+        r.blk[l] = off; off = al256(off + (size_t)(h[i] >> (levels - 1)) * 4);  // one count per band
       }
     }
     r.cnt = off;
@@ -452,7 +455,7 @@ lsdg_status lsdg_frame_upload(lsdg_ctx* ctx, lsdg_frame* f, const float* image) 
   if (!ctx || !f || !image) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   const FrameDev& F = f->fs.h_frames[0];
   CK(ctx, cudaMemcpyAsync(F.plane[0], image, (size_t)F.w * F.h * 4, cudaMemcpyHostToDevice, ctx->stream));
-  ctx->launches += launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, ctx->stream);
+  ctx->launches += launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, f->fs.max_h, true, ctx->stream);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   f->has_image = true;
@@ -467,7 +470,7 @@ lsdg_status lsdg_frame_upload_u8(lsdg_ctx* ctx, lsdg_frame* f, const uint8_t* im
   uint8_t* tmp = (uint8_t*)F.pyr[0];
   CK(ctx, cudaMemcpyAsync(tmp, image, n, cudaMemcpyHostToDevice, ctx->stream));
   launch_u8_to_plane(tmp, F.plane[0], (int)n, ctx->stream);
-  ctx->launches += 1 + launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, ctx->stream);
+  ctx->launches += 1 + launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, f->fs.max_h, true, ctx->stream);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   f->has_image = true;
@@ -482,7 +485,9 @@ lsdg_status lsdg_frame_set_depth(lsdg_ctx* ctx, lsdg_frame* f, const float* idep
   CK(ctx, cudaMemcpyAsync(f->fs.d_frames, &F, sizeof(FrameDev), cudaMemcpyHostToDevice, ctx->stream));
   CK(ctx, cudaMemcpyAsync(F.idepth[0], idepth, (size_t)F.w * F.h * 4, cudaMemcpyHostToDevice, ctx->stream));
   CK(ctx, cudaMemcpyAsync(F.ivar[0], var, (size_t)F.w * F.h * 4, cudaMemcpyHostToDevice, ctx->stream));
-  ctx->launches += launch_frame_points(f->fs.d_frames, 1, F.levels, f->fs.max_pix, ctx->stream);
+  // band pass again (intensity levels are rebuilt identically) for the depth pyramid and counts
+  ctx->launches += launch_frame_pyramid(f->fs.d_frames, 1, F.levels, f->fs.max_pix, f->fs.max_h, false, ctx->stream);
+  ctx->launches += launch_frame_points(f->fs.d_frames, 1, F.levels, f->fs.max_h, ctx->stream);
   CK(ctx, cudaGetLastError());
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   return LSDG_OK;

@@ -21,8 +21,9 @@
 using namespace lsdg;
 
 namespace lsdg {
-int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
-int launch_frame_points(const FrameDev* frames, int n, int levels, long max_pix, cudaStream_t s);
+int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, int max_h, bool with_grads,
+                         cudaStream_t s);
+int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cudaStream_t s);
 }  // namespace lsdg
 
 #define CK(ctx, expr)                                         \
@@ -85,8 +86,8 @@ static lsdg_status batch_track_args(lsdg_ctx* ctx, lsdg_batch* b, TrackArgs* a) 
 
 static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, int* launches) {
   const int L = ctx->params.levels;
-  int k = launch_frame_pyramid(b->fs.d_frames, 2 * b->n, L, b->fs.max_pix, ctx->stream);
-  k += launch_frame_points(b->fs.d_frames, b->n, L, b->fs.max_pix, ctx->stream);
+  int k = launch_frame_pyramid(b->fs.d_frames, 2 * b->n, L, b->fs.max_pix, b->fs.max_h, false, ctx->stream);
+  k += launch_frame_points(b->fs.d_frames, b->n, L, b->fs.max_h, ctx->stream);
   CK(ctx, cudaGetLastError());
   *launches = k;
   return LSDG_OK;

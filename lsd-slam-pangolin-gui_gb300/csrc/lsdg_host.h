@@ -38,6 +38,7 @@ struct FrameSet {
   std::vector<lsdg_intrinsics> intr;
   std::vector<bool> depth;
   long max_pix = 0;
+  int max_h = 0;
   size_t pix_total = 0, pix_depth = 0;
   void* arena = nullptr;
   size_t arena_bytes = 0;

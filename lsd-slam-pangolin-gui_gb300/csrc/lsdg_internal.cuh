@@ -21,7 +21,6 @@
 namespace lsdg {
 
 constexpr int kMaxLevels = LSDG_MAX_LEVELS;
-constexpr int kCountBlock = 256;  // pixels per block of the point compaction
 
 struct FrameDev {
   int w, h;  // level 0
@@ -35,7 +34,7 @@ struct FrameDev {
   float* pvar[kMaxLevels];
   float* psig[kMaxLevels];
   int* pcount;                   // [kMaxLevels]
-  int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per block, then offsets
+  int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per band, then offsets
   float fx[kMaxLevels], fy[kMaxLevels], cx[kMaxLevels], cy[kMaxLevels];
   float fxi[kMaxLevels], fyi[kMaxLevels];
 };

@@ -142,4 +142,5 @@ def test_batch_with_lost_pair(ctx):
 def test_launch_counter_counts_kernels(ctx, small_pair):
     n0 = ctx.launch_count()
     kf, fr = _frames(ctx, small_pair)
-    assert ctx.launch_count() - n0 == 5 + 5 + 11  # two pyramids + depth/points
+    # per image: band pyramid + gradients; depth: band pass + scan + scatter
+    assert ctx.launch_count() - n0 == 2 + 2 + 3
