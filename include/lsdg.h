@@ -108,7 +108,8 @@ typedef struct lsdg_params {
   float max_search_len;    /* longest epipolar segment searched (px) */
   float min_search_len;    /* shortest epipolar segment searched (px) */
   float fuse_chi2;         /* (d_obs - d)^2 / (var + var_obs) above this: inconsistent */
-  float min_epl_length;    /* full-range epipolar segment shorter than this (px): no baseline, skip */
+  float min_epl_length;    /* epipolar disparity below this many pixels per unit of inverse depth
+                              (1/m) means no usable baseline: the observation is skipped */
   int32_t validity_init;   /* validity of a new hypothesis */
   int32_t validity_max;
   int32_t validity_penalty; /* subtracted on an inconsistent observation */
@@ -252,6 +253,44 @@ LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* thr
  * algorithmic bytes those passes read (points + frame levels + sums). */
 LSDG_API lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* batch, int64_t* passes,
                             double* pass_bytes, double* unique_bytes);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Semi-dense inverse-depth filter (upstream DepthMap)                                         */
+/* ------------------------------------------------------------------------------------------ */
+
+#define LSDG_MAX_REFS 16
+
+/* A keyframe depth map: the keyframe image (level 0 with gradients) and the per-pixel state
+ * {idepth, var, idepth_smoothed, var_smoothed, validity, blacklist} in HBM. */
+LSDG_API lsdg_status lsdg_depth_create(lsdg_ctx* ctx, int width, int height, const lsdg_intrinsics* intr,
+                                       lsdg_depthmap** out);
+LSDG_API lsdg_status lsdg_depth_destroy(lsdg_ctx* ctx, lsdg_depthmap* dm);
+/* Keyframe image and initial hypotheses (idepth <= 0 or var <= 0: none; others start with
+ * validity = params.validity_init). */
+LSDG_API lsdg_status lsdg_depth_set_keyframe(lsdg_ctx* ctx, lsdg_depthmap* dm, const float* image,
+                                             const float* idepth, const float* idepth_var);
+/* Upload n_refs (<= LSDG_MAX_REFS) reference images, back to back (asynchronous). */
+LSDG_API lsdg_status lsdg_depth_load_refs(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs, const float* ref_images);
+/* DepthMap::updateKeyframe on the loaded references: observeDepth of every pixel against
+ * references 0..n_refs-1 in order (epipolar search + fusion), then, if regularize != 0,
+ * regularizeDepthMap.  key_to_ref: 12 doubles per reference.  Asynchronous. */
+LSDG_API lsdg_status lsdg_depth_update_loaded(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs,
+                                              const double* key_to_ref, int regularize);
+/* load_refs + update_loaded, synchronous. */
+LSDG_API lsdg_status lsdg_depth_update(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs, const float* ref_images,
+                                       const double* key_to_ref, int regularize);
+/* regularizeDepthMap (+ hole filling and removal of unsupported hypotheses), synchronous. */
+LSDG_API lsdg_status lsdg_depth_regularize(lsdg_ctx* ctx, lsdg_depthmap* dm);
+/* DepthMap::createKeyFrame: propagateDepth of every hypothesis into the new keyframe (nearest
+ * hypothesis wins a pixel), which then becomes this depth map's keyframe; regularize != 0 runs
+ * regularizeDepthMap on it.  Synchronous. */
+LSDG_API lsdg_status lsdg_depth_create_keyframe(lsdg_ctx* ctx, lsdg_depthmap* dm, const float* new_image,
+                                                const double key_to_new[12], int regularize);
+/* Read the state (any pointer may be NULL).  idepth / idepth_smoothed <= 0 means no depth
+ * (the layout Frame::idepth(0) / idepthVar(0) hands to the viewer). */
+LSDG_API lsdg_status lsdg_depth_get(lsdg_ctx* ctx, lsdg_depthmap* dm, float* idepth, float* idepth_var,
+                                    float* idepth_smoothed, float* var_smoothed, int32_t* validity,
+                                    int32_t* blacklist);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                   */

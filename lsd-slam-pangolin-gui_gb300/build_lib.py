@@ -23,7 +23,9 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 NVCC = os.environ.get("NVCC", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-         "--expt-relaxed-constexpr", "-I", INCLUDE]
+         "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr", "-I", INCLUDE]
+# (host code too is built without FMA contraction: the per-reference geometry the depth filter
+# derives from a pose in double must round to the same floats as the CPU oracle's on any host)
 # Translation units whose float results must be bit-identical to the CPU oracle are built without
 # FMA contraction; the tracker (parity by tolerance, throughput-critical) is built with it.
 FMAD = {"track.cu": "-fmad=true"}

@@ -77,6 +77,15 @@ def lib():
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
+    _sig(L, "lsdg_depth_create", st, [_vp, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
+    _sig(L, "lsdg_depth_destroy", st, [_vp, _vp])
+    _sig(L, "lsdg_depth_set_keyframe", st, [_vp, _vp, _f32p, _f32p, _f32p])
+    _sig(L, "lsdg_depth_load_refs", st, [_vp, _vp, C.c_int, _f32p])
+    _sig(L, "lsdg_depth_update_loaded", st, [_vp, _vp, C.c_int, _f64p, C.c_int])
+    _sig(L, "lsdg_depth_update", st, [_vp, _vp, C.c_int, _f32p, _f64p, C.c_int])
+    _sig(L, "lsdg_depth_regularize", st, [_vp, _vp])
+    _sig(L, "lsdg_depth_create_keyframe", st, [_vp, _vp, _f32p, _f64p, C.c_int])
+    _sig(L, "lsdg_depth_get", st, [_vp, _vp] + [C.c_void_p] * 6)
     _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
     _lib = L
     return L
@@ -302,6 +311,69 @@ class Batch:
     def close(self):
         if self._h and self.ctx.handle:
             lib().lsdg_batch_destroy(self.ctx.handle, self._h)
+        self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class DepthMap:
+    """Upstream DepthMap: semi-dense inverse-depth hypotheses of one keyframe on the GPU."""
+
+    PLANES = ("idepth", "var", "idepth_smoothed", "var_smoothed", "validity", "blacklist")
+
+    def __init__(self, ctx: Context, width: int, height: int, intr):
+        self.ctx, self.w, self.h = ctx, width, height
+        self._k = intrinsics(intr)
+        self._h = _vp()
+        ctx.check(lib().lsdg_depth_create(ctx.handle, width, height, C.byref(self._k), C.byref(self._h)))
+
+    def set_keyframe(self, image, idepth, idepth_var):
+        self.ctx.check(lib().lsdg_depth_set_keyframe(self.ctx.handle, self._h, np.ascontiguousarray(image, np.float32),
+                                                     np.ascontiguousarray(idepth, np.float32),
+                                                     np.ascontiguousarray(idepth_var, np.float32)))
+        return self
+
+    @staticmethod
+    def _refs(ref_images, key_to_ref):
+        imgs = np.ascontiguousarray(np.concatenate([np.asarray(r, np.float32).ravel() for r in ref_images]), np.float32)
+        poses = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1) for p in key_to_ref]))
+        return imgs, poses
+
+    def updateKeyframe(self, ref_images, key_to_ref, regularize=True):
+        imgs, poses = self._refs(ref_images, key_to_ref)
+        self.ctx.check(lib().lsdg_depth_update(self.ctx.handle, self._h, len(ref_images), imgs, poses, int(regularize)))
+
+    def load_refs(self, ref_images):
+        imgs = np.ascontiguousarray(np.concatenate([np.asarray(r, np.float32).ravel() for r in ref_images]), np.float32)
+        self._keep = imgs
+        self.ctx.check(lib().lsdg_depth_load_refs(self.ctx.handle, self._h, len(ref_images), imgs))
+
+    def update_loaded(self, key_to_ref, regularize=True):
+        poses = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1) for p in key_to_ref]))
+        self.ctx.check(lib().lsdg_depth_update_loaded(self.ctx.handle, self._h, len(key_to_ref), poses, int(regularize)))
+
+    def regularize(self):
+        self.ctx.check(lib().lsdg_depth_regularize(self.ctx.handle, self._h))
+
+    def createKeyFrame(self, new_image, key_to_new, regularize=True):
+        self.ctx.check(lib().lsdg_depth_create_keyframe(self.ctx.handle, self._h, np.ascontiguousarray(new_image, np.float32),
+                                                        _pose12(key_to_new), int(regularize)))
+
+    def get(self):
+        out = {}
+        for name in self.PLANES:
+            dt = np.int32 if name in ("validity", "blacklist") else np.float32
+            out[name] = np.zeros((self.h, self.w), dt)
+        self.ctx.check(lib().lsdg_depth_get(self.ctx.handle, self._h, *[out[n].ctypes.data for n in self.PLANES]))
+        return out
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().lsdg_depth_destroy(self.ctx.handle, self._h)
         self._h = _vp()
 
     def __del__(self):

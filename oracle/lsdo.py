@@ -54,6 +54,11 @@ def lib():
         L.lsdo_track_batch_f.argtypes = [C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), _f32p, _f32p, _f32p,
                                          _f32p, _f64p, _f64p, C.POINTER(T.TrackStats), C.POINTER(T.Params), C.c_int]
         L.lsdo_track_batch_f.restype = C.c_int
+        for nm in ("lsdo_depth_pipeline_f", "lsdo_depth_pipeline_d"):
+            f = getattr(L, nm)
+            f.argtypes = [C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(T.Params), _f32p, _f32p, _f32p, C.c_int,
+                          _f32p, _f64p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+            f.restype = C.c_int
         L.lsdo_hardware_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -187,3 +192,48 @@ def track_batch(pairs, inits=None, params: T.Params = None, threads: int = None)
 
 def hardware_threads() -> int:
     return int(lib().lsdo_hardware_threads())
+
+
+DEPTH_PLANES = ("idepth", "var", "idepth_smoothed", "var_smoothed", "validity", "blacklist")
+
+
+def _planes(buf, h, w):
+    n = h * w
+    out = {}
+    for k, name in enumerate(DEPTH_PLANES):
+        a = buf[k * n:(k + 1) * n].reshape(h, w)
+        out[name] = a.astype(np.int32) if name in ("validity", "blacklist") else a
+    return out
+
+
+def depth_pipeline(seq, params=None, double=False, regularize=True, propagate=True, n_refs=None, threads=1,
+                   init_idepth=None, init_var=None):
+    """DepthMap::updateKeyframe over the sequence's references (+ regularize), then createKeyFrame
+    (propagate + regularize) into the next frame.  Returns (after_update, after_propagate) dicts."""
+    p = params or default_params()
+    h, w = seq.h, seq.w
+    n = len(seq.ref_images) if n_refs is None else n_refs
+    refs = np.ascontiguousarray(np.concatenate([r.ravel() for r in seq.ref_images[:n]]), np.float32)
+    poses = np.concatenate([np.ascontiguousarray(_inv(T_), np.float64).ravel() for T_ in seq.ref_frame_to_key[:n]])
+    upd = np.zeros(6 * h * w, np.float32)
+    prop = np.zeros(6 * h * w, np.float32) if propagate else None
+    nimg = np.ascontiguousarray(seq.next_image, np.float32) if propagate else None
+    knew = np.ascontiguousarray(_inv(seq.next_to_key), np.float64).ravel() if propagate else None
+    flags = (1 if regularize else 0) | (2 if regularize else 0)
+    f = lib().lsdo_depth_pipeline_d if double else lib().lsdo_depth_pipeline_f
+    d0 = seq.init_idepth if init_idepth is None else init_idepth
+    v0 = seq.init_var if init_var is None else init_var
+    f(w, h, C.byref(_intr(seq.intr)), C.byref(p), np.ascontiguousarray(seq.key_image, np.float32),
+      np.ascontiguousarray(d0, np.float32), np.ascontiguousarray(v0, np.float32), n, refs, poses,
+      nimg.ctypes.data if propagate else None, knew.ctypes.data if propagate else None, flags,
+      upd.ctypes.data, prop.ctypes.data if propagate else None, threads)
+    return _planes(upd, h, w), (_planes(prop, h, w) if propagate else None)
+
+
+def _inv(T_):
+    R = T_[:, :3]
+    t = T_[:, 3]
+    out = np.zeros((3, 4))
+    out[:, :3] = R.T
+    out[:, 3] = -R.T @ t
+    return out
