@@ -45,6 +45,11 @@ def _gen(seed, w, h):
     return synth.tracking_pair(seed, w, h)
 
 
+def _gen_depth(seed, w, h):
+    import synth
+    return synth.depth_sequence(seed, w, h)
+
+
 def gen_pairs(specs, workers):
     ctx = mp.get_context("spawn")  # never fork a process that may touch CUDA
     with ctx.Pool(max(1, min(workers, len(specs)))) as pool:
@@ -162,6 +167,8 @@ def run_ours(args, rank, world, local_rank):
     # all host-side generation happens before the first CUDA call
     pairs = gen_pairs([(1000 * rank + i, W, H) for i in range(N_PAIRS)], workers)
     mixed = gen_pairs([(5000 + 1000 * rank + i, w, h) for i, (w, h) in enumerate(MIXED)], workers) if not args.quick else []
+    with mp.get_context("spawn").Pool(1) as pool:
+        dseq = pool.apply(_gen_depth, (7 + rank, W, H))
 
     torch.cuda.set_device(local_rank)
     dist = None
@@ -301,6 +308,8 @@ def run_ours(args, rank, world, local_rank):
                      "lost": sum(1 for s in ms_ if s.status != 0)}
         mb.close()
 
+    depth_res = bench_depth(ctx, stream, dseq, args)
+
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -326,17 +335,81 @@ def run_ours(args, rank, world, local_rank):
         "plain": {"pairs_per_s": plain_value, "pairs_per_s_device": plain_dev, "api": "lsdg_track_se3, one pair per call",
                   "batched_over_plain": value / plain_value},
         "mixed_batch": mixed_res,
+        "keyframe_update": depth_res,
         "accuracy": {"max_gt_rot_err_rad": max(e[0] for e in errs), "max_gt_trans_err_m": max(e[1] for e in errs),
                      "lost": lost},
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(pairs, args)
+        depth_res["cpu_ms"], depth_res["cpu_cores"] = cpu_depth_baseline(dseq)
     if rank == 0:
         print(json.dumps(result), flush=True)
     batch.close()
     ctx.close()
     if dist:
         dist.destroy_process_group()
+
+
+def bench_depth(ctx, stream, seq, args):
+    """DepthMap::updateKeyframe of one 640x480 keyframe against 8 references (observe + regularize):
+    device time with the references resident, and end to end through lsdg_depth_update (reference
+    upload, update, state read-back).  Each timed update starts from the same initial hypotheses."""
+    import torch
+
+    import lsdg
+    import synth
+
+    inv = lambda T_: synth.pose_inv(T_)
+    poses = [inv(T_) for T_ in seq.ref_frame_to_key]
+    dm = lsdg.DepthMap(ctx, seq.w, seq.h, seq.intr)
+    dm.load_refs(seq.ref_images)
+    dev = []
+    for it in range(max(3, args.warmup) + max(10, args.steps)):
+        dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dm.update_loaded(poses, regularize=True)
+        e1.record(stream)
+        e1.synchronize()
+        if it >= max(3, args.warmup):
+            dev.append(e0.elapsed_time(e1))
+    e2e = []
+    for it in range(max(3, args.warmup) + max(10, args.steps)):
+        dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+        t0 = time.perf_counter()
+        dm.updateKeyframe(seq.ref_images, poses, regularize=True)
+        st = dm.get()
+        if it >= max(3, args.warmup):
+            e2e.append((time.perf_counter() - t0) * 1e3)
+    prop = []
+    for it in range(6):
+        dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+        dm.updateKeyframe(seq.ref_images, poses, regularize=True)
+        t0 = time.perf_counter()
+        dm.createKeyFrame(seq.next_image, inv(seq.next_to_key), regularize=True)
+        if it >= 2:
+            prop.append((time.perf_counter() - t0) * 1e3)
+    good = (st["validity"] > 0) & (st["var"] < 0.01)
+    rel = np.abs(st["idepth"][good] - seq.key_true_idepth[good]) / seq.key_true_idepth[good]
+    dm.close()
+    return {"workload": "updateKeyframe: 1 keyframe 640x480, 8 references on a 10 cm arc, observe + regularize",
+            "ms_device": statistics.median(dev), "ms_e2e": statistics.median(e2e),
+            "e2e_api": "lsdg_depth_update + lsdg_depth_get (reference upload, update, state read-back)",
+            "create_keyframe_ms_e2e": statistics.median(prop),
+            "well_observed_pixels": int(good.sum()), "median_rel_idepth_err_vs_truth": float(np.median(rel))}
+
+
+def cpu_depth_baseline(seq):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lsdo
+
+    cores = os.cpu_count() or 1
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        lsdo.depth_pipeline(seq, propagate=False, threads=cores)
+        ts.append((time.perf_counter() - t0) * 1e3)
+    return statistics.median(ts), cores
 
 
 def cpu_baseline(pairs, args, min_seconds=10.0):
