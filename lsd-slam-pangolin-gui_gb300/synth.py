@@ -84,10 +84,12 @@ def pose_mul(A: np.ndarray, B: np.ndarray) -> np.ndarray:
 
 
 def pose_error(A: np.ndarray, B: np.ndarray):
-    """(rotation angle [rad], translation distance [m]) between two 3x4 poses."""
+    """(rotation angle [rad], translation distance [m]) between two 3x4 poses.  The angle is
+    atan2(|vee(dR - dR^T)| / 2, (tr dR - 1) / 2), accurate for small angles too."""
     dR = A[:, :3].T @ B[:, :3]
     c = (np.trace(dR) - 1.0) * 0.5
-    ang = math.acos(max(-1.0, min(1.0, c)))
+    v = np.array([dR[2, 1] - dR[1, 2], dR[0, 2] - dR[2, 0], dR[1, 0] - dR[0, 1]]) * 0.5
+    ang = math.atan2(float(np.linalg.norm(v)), float(c))
     return ang, float(np.linalg.norm(A[:, 3] - B[:, 3]))
 
 

@@ -36,7 +36,7 @@ int main(int argc, char** argv) {
     lsdg::SE3Tracker tracker(ctx);
     const lsdg::Pose T = tracker.trackFrame(kf, fr, lsdg::identity());
     std::printf("pose");
-    for (double v : T) std::printf(" %.9g", v);
+    for (double v : T) std::printf(" %.17g", v);
     std::printf(" good %d passes %d\n", tracker.trackingWasGood() ? 1 : 0, tracker.lastStats.total_passes);
     lsdg::DepthMap dm(ctx, w, h, K);
     dm.initializeKeyframe(key.data(), idepth.data(), var.data());

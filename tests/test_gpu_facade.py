@@ -15,7 +15,10 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_cpp_facade_tracks_and_maps():
+def test_cpp_facade_tracks_and_maps(monkeypatch):
+    # both sides use the same launch shape (the autotuner could otherwise pick different ones per
+    # context, which changes the reduction order and the last bits of the pose)
+    monkeypatch.setenv("LSDG_TRACK_SHAPE", "256,8,2")
     p = synth.tracking_pair(21, 320, 240)
     with tempfile.TemporaryDirectory() as d:
         for name, arr in (("key", p.ref_image), ("idepth", p.ref_idepth), ("var", p.ref_idepth_var), ("cur", p.new_image)):
@@ -37,5 +40,5 @@ def test_cpp_facade_tracks_and_maps():
     fr = lsdg.Frame(ctx, p.w, p.h, p.intr).upload(p.new_image)
     T_py, st = lsdg.SE3Tracker(ctx).trackFrame(kf, fr)
     a, t = synth.pose_error(T_cpp, T_py)
-    assert a < 1e-6 and t < 1e-6
+    assert a < 1e-7 and t < 1e-7, (a, t)
     assert int(lines[1].split()[1]) > 1000  # depth_valid
