@@ -286,6 +286,34 @@ LSDG_API lsdg_status lsdg_depth_regularize(lsdg_ctx* ctx, lsdg_depthmap* dm);
  * regularizeDepthMap on it.  Synchronous. */
 LSDG_API lsdg_status lsdg_depth_create_keyframe(lsdg_ctx* ctx, lsdg_depthmap* dm, const float* new_image,
                                                 const double key_to_new[12], int regularize);
+/* propagateDepth for callers that cannot allocate device memory when a keyframe changes: an
+ * application that reserves all GPU memory at start-up and forbids allocation in its real-time
+ * mapping thread, one that records the mapping step inside its own stream capture (allocation
+ * cannot be captured), or one that cannot accept the device-wide synchronisation an allocation may
+ * imply.  No counterpart in the reference: upstream DepthMap allocates its own buffers.
+ *
+ * Same computation as lsdg_depth_create_keyframe's propagation (without regularisation), but no
+ * context and no allocation: inputs and outputs are the caller's device buffers (width * height
+ * elements each, row-major), the work is enqueued on the caller's `stream` (cudaStream_t; NULL = the
+ * legacy default stream) and the call returns without synchronising.  old_* is the old keyframe's raw
+ * state (idepth, var, validity), new_* receive the new keyframe's state.  The current device of the
+ * calling thread must own `stream` and the buffers.
+ *
+ * The only scratch, a 64-bit z-buffer of one entry per pixel, is a device array inside the library
+ * that every GPU which loads the library holds until the process exits: at most 1280 x 960 =
+ * 1,228,800 pixels (9.8 MB); larger sizes return LSDG_INVALID_ARG.  The first call on a device looks
+ * up that array's device address (cudaGetSymbolAddress), so make the first call on each device before
+ * any stream capture.  All calls share the array: calls that overlap on the GPU (different streams,
+ * or different host threads, on one device) race on it -- serialise them.  Errors are reported by the
+ * return value only (there is no context for lsdg_last_error). */
+LSDG_API lsdg_status lsdg_depth_propagate_noalloc(void* stream, int width, int height, const lsdg_intrinsics* intr,
+                                                  const lsdg_params* params, const double old_to_new[12],
+                                                  const float* old_image, const float* new_image,
+                                                  const float* old_idepth, const float* old_var,
+                                                  const int32_t* old_validity, float* new_idepth, float* new_var,
+                                                  float* new_idepth_smoothed, float* new_var_smoothed,
+                                                  int32_t* new_validity, int32_t* new_blacklist);
+
 /* Read the state (any pointer may be NULL).  idepth / idepth_smoothed <= 0 means no depth
  * (the layout Frame::idepth(0) / idepthVar(0) hands to the viewer). */
 LSDG_API lsdg_status lsdg_depth_get(lsdg_ctx* ctx, lsdg_depthmap* dm, float* idepth, float* idepth_var,

@@ -23,6 +23,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "lsdg_host.h"
@@ -691,3 +692,96 @@ lsdg_status lsdg_depth_get(lsdg_ctx* ctx, lsdg_depthmap* dm, float* idepth, floa
 }
 
 }  // extern "C"
+
+// ============================================================================================
+// propagateDepth without allocation (lsdg_depth_propagate_noalloc)
+// ============================================================================================
+// Some callers cannot call cudaMalloc at the moment they need a keyframe change: an application
+// that reserves all device memory up front and forbids allocation in its real-time mapping thread,
+// one that runs the mapping step inside its own stream capture (allocation is not capturable), or
+// one that cannot afford the device-wide synchronisation cudaMalloc may imply.  For them the z-buffer
+// of the propagation -- its only scratch -- lives in this file-scope device array instead of a
+// context.  Every GPU that loads the library holds it until the process exits.
+
+constexpr long kNoAllocMaxPixels = 1280L * 960L;  // largest keyframe: 1,228,800 pixels (9.8 MB of keys)
+
+static __device__ __align__(256) unsigned long long g_noalloc_zbuffer[kNoAllocMaxPixels];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the z-buffer on the current device, looked up once per device (the name is a
+// host-side stand-in, not a device address).
+lsdg_status noalloc_zbuffer(unsigned long long** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return LSDG_CUDA_ERROR;
+  }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return LSDG_NOT_SUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_zbuffer);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return LSDG_CUDA_ERROR;
+    }
+    g_noalloc_ptr[dev] = static_cast<unsigned long long*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return LSDG_OK;
+}
+}  // namespace
+
+extern "C" lsdg_status lsdg_depth_propagate_noalloc(void* stream, int width, int height, const lsdg_intrinsics* intr,
+                                                   const lsdg_params* params, const double old_to_new[12],
+                                                   const float* old_image, const float* new_image,
+                                                   const float* old_idepth, const float* old_var,
+                                                   const int32_t* old_validity, float* new_idepth, float* new_var,
+                                                   float* new_idepth_smoothed, float* new_var_smoothed,
+                                                   int32_t* new_validity, int32_t* new_blacklist) {
+  if (!intr || !params || !old_to_new || !old_image || !new_image || !old_idepth || !old_var || !old_validity ||
+      !new_idepth || !new_var || !new_idepth_smoothed || !new_var_smoothed || !new_validity || !new_blacklist)
+    return LSDG_INVALID_ARG;
+  if (width < 1 || height < 1 || (long)width * height > kNoAllocMaxPixels) return LSDG_INVALID_ARG;
+  if (!(intr->fx > 0) || !(intr->fy > 0)) return LSDG_INVALID_ARG;
+  unsigned long long* keys = nullptr;
+  const lsdg_status st = noalloc_zbuffer(&keys);
+  if (st != LSDG_OK) return st;
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  PropArgs A;
+  A.w = width;
+  A.h = height;
+  A.fx = intr->fx;
+  A.fy = intr->fy;
+  A.cx = intr->cx;
+  A.cy = intr->cy;
+  A.fxi = (float)(1.0 / intr->fx);
+  A.fyi = (float)(1.0 / intr->fy);
+  A.min_z = params->min_z;
+  A.max_photo_diff = params->propagate_max_photo_diff;
+  A.prediction_var = params->prediction_var;
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) A.R[3 * i + j] = (float)old_to_new[4 * i + j];
+    A.t[i] = (float)old_to_new[4 * i + 3];
+  }
+  A.Iold = old_image;
+  A.Inew = new_image;
+  A.src = DepthPlanes{const_cast<float*>(old_idepth), const_cast<float*>(old_var), nullptr, nullptr,
+                      const_cast<int*>(old_validity), nullptr};  // propagation reads idepth, var, validity
+  A.dst = DepthPlanes{new_idepth, new_var, new_idepth_smoothed, new_var_smoothed, new_validity, new_blacklist};
+  A.key = keys;
+  const size_t n = (size_t)width * height;
+  // the array keeps the previous call's keys: every call starts from an empty z-buffer
+  if (cudaMemsetAsync(keys, 0xff, n * sizeof(unsigned long long), s) != cudaSuccess) {
+    cudaGetLastError();
+    return LSDG_CUDA_ERROR;
+  }
+  const int blocks = (int)((n + 255) / 256);
+  depth_prop_key_kernel<<<blocks, 256, 0, s>>>(A);
+  depth_prop_write_kernel<<<blocks, 256, 0, s>>>(A);
+  return cudaGetLastError() == cudaSuccess ? LSDG_OK : LSDG_CUDA_ERROR;
+}
