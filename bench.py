@@ -157,6 +157,26 @@ def run_profile(args):
     ctx.close()
 
 
+def run_profile_depth(args):
+    """Lean driver for ncu: one 640x480 keyframe, W + K depth updates (8 references)."""
+    import lsdg
+    import synth
+
+    with mp.get_context("spawn").Pool(1) as pool:
+        seq = pool.apply(_gen_depth, (7, W, H))
+    ctx = lsdg.Context()
+    dm = lsdg.DepthMap(ctx, seq.w, seq.h, seq.intr)
+    dm.load_refs(seq.ref_images)
+    poses = [synth.pose_inv(T_) for T_ in seq.ref_frame_to_key]
+    for _ in range(args.warmup + args.steps):
+        dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+        dm.update_loaded(poses, regularize=True)
+    st = dm.get()
+    print(json.dumps({"profile_depth": True, "valid": int((st["validity"] > 0).sum())}))
+    dm.close()
+    ctx.close()
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -488,12 +508,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", action="store_true", help="lean run for ncu captures")
     ap.add_argument("--pairs", type=int, default=16, help="pairs in the --profile batch")
+    ap.add_argument("--profile-depth", action="store_true", help="lean depth-update run for ncu captures")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.profile:
+    if args.profile_depth:
+        run_profile_depth(args)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args, rank, world)
