@@ -346,9 +346,10 @@ def run_ours(args, rank, world, local_rank):
                 "api": "lsdg_batch_track_se3 (pinned host buffers)"},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "kernel": "track_se3_kernel",
-                     "note": "achieved = algorithmic bytes of all LM residual passes (points 20 B + frame level "
-                             "12 B/px + sums, per pass) / tracker kernel time; re-reads across passes are L2 "
+                     "traffic": traffic, "kernel": "track_kernel",
+                     "note": "achieved = algorithmic bytes of all LM residual passes (point float4 + frozen "
+                             "variance 20 B, intensity plane 4 B/px, sums; per pass) / tracker kernel time; "
+                             "re-reads across passes are L2 "
                              "hits, so this is an L2-side figure against the HBM peak (%s)" % peak_kind,
                      "first_touch_GBps": unique_bytes / (track_ms / 1e3) / 1e9,
                      "tracker_ms": track_ms, "build_ms": build_ms, "passes_per_step": passes},

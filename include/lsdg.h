@@ -217,6 +217,28 @@ LSDG_API lsdg_status lsdg_track_se3(lsdg_ctx* ctx, const lsdg_frame* reference, 
                            lsdg_track_stats* stats);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Sim3 direct alignment of two keyframes (constraint search)                                   */
+/* ------------------------------------------------------------------------------------------ */
+
+/* A Sim3 pose is 13 doubles {R (9, row-major), t (3), s}: x_b = s R x_a + t. */
+
+/* One Sim3 residual pass at a fixed pose (both frames need depth).  out[LSDG_NE_SIZE_SIM3] =
+ *   [0..27] upper triangle of sum w J^T J (7x7), [28..34] sum w J^T r, [35] energy, [36] points
+ *   used, [37] inliers, [38] outliers, [39] points that left the image.  J is d r / d xi for the
+ *   left increment exp(xi) * ref_to_frame, xi = (v, omega, log-scale); each point contributes its
+ *   photometric residual and, where frame's depth map has the four bilinear corners, the
+ *   inverse-depth residual 1/z' - D_frame(u'). */
+LSDG_API lsdg_status lsdg_sim3_normal_equations(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame,
+                                                int level, const double ref_to_frame[13],
+                                                double out[LSDG_NE_SIZE_SIM3]);
+
+/* Sim3Tracker::trackFrameSim3: align keyframe `frame` (with depth) to keyframe `reference`,
+ * 7 parameters, the same LM rules as lsdg_track_se3 with a 7x7 FP64 solve. */
+LSDG_API lsdg_status lsdg_track_sim3(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame,
+                                     const double frame_to_ref_init[13], double frame_to_ref_out[13],
+                                     lsdg_track_stats* stats);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Batched alignment: many independent pairs of mixed size, one persistent launch              */
 /* ------------------------------------------------------------------------------------------ */
 
@@ -237,6 +259,20 @@ LSDG_API lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* batch);
 /* Device -> host results (synchronises the context stream). */
 LSDG_API lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* batch, double* frame_to_ref_out,
                             lsdg_track_stats* stats);
+/* A batch of Sim3 constraint trackings (a new keyframe against its candidates): both keyframes of
+ * every pair carry depth; poses are 13 doubles.  lsdg_batch_run and lsdg_batch_read work on it as on
+ * an SE3 batch. */
+LSDG_API lsdg_status lsdg_batch_create_sim3(lsdg_ctx* ctx, int n, const int* widths, const int* heights,
+                                            const lsdg_intrinsics* intr, lsdg_batch** out);
+LSDG_API lsdg_status lsdg_batch_load_sim3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
+                                          const float* ref_idepth, const float* ref_idepth_var,
+                                          const float* new_images, const float* new_idepth,
+                                          const float* new_idepth_var, const double* frame_to_ref_init);
+LSDG_API lsdg_status lsdg_batch_track_sim3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
+                                           const float* ref_idepth, const float* ref_idepth_var,
+                                           const float* new_images, const float* new_idepth,
+                                           const float* new_idepth_var, const double* frame_to_ref_init,
+                                           double* frame_to_ref_out, lsdg_track_stats* stats);
 /* load + run + read. */
 LSDG_API lsdg_status lsdg_batch_track_se3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
                                  const float* ref_idepth, const float* ref_idepth_var,

@@ -23,8 +23,9 @@ int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix
                          cudaStream_t s);
 int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cudaStream_t s);
 void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
-cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s);
-int track_max_clusters(int threads, int minblocks, int cluster);
+cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s,
+                         bool sim3);
+int track_max_clusters(int threads, int minblocks, int cluster, bool sim3);
 cudaError_t track_prepare();
 int track_shape_count();
 void track_shape(int i, int* threads, int* minblocks);
@@ -228,7 +229,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
   fs.off_var0 = off;
   for (int i = 0; i < n; ++i) if (depth[i]) { o_var0[i] = off; off += (size_t)w[i] * h[i] * 4; }
   off = al256(off);
-  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], psig[kMaxLevels], blk[kMaxLevels], cnt; };
+  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], psig[kMaxLevels], psigd[kMaxLevels], blk[kMaxLevels], cnt; };
   std::vector<Rest> rest(n);
   for (int i = 0; i < n; ++i) {
     Rest& r = rest[i];
@@ -244,6 +245,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         r.pxyzi[l] = off; off = al256(off + pix * 16);
         r.pvar[l] = off; off = al256(off + pix * 4);
         r.psig[l] = off; off = al256(off + pix * 4);
+        r.psigd[l] = off; off = al256(off + pix * 4);
         r.blk[l] = off; off = al256(off + (size_t)(h[i] >> (levels - 1)) * 4);  // one count per band
       }
     }
@@ -272,6 +274,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         F.pxyzi[l] = (float4*)(base + r.pxyzi[l]);
         F.pvar[l] = (float*)(base + r.pvar[l]);
         F.psig[l] = (float*)(base + r.psig[l]);
+        F.psigd[l] = (float*)(base + r.psigd[l]);
         F.blk_count[l] = (int*)(base + r.blk[l]);
       }
       F.fx[l] = (float)fx; F.fy[l] = (float)fy; F.cx[l] = (float)cx; F.cy[l] = (float)cy;
@@ -323,6 +326,8 @@ TrackArgs make_track_args(const lsdg_params& p) {
   a.stall_eps = p.stall_eps;
   a.min_good_ratio = p.min_good_ratio;
   a.min_usage = p.min_usage;
+  a.sim3_depth_variance = p.sim3_depth_variance;
+  a.sim3_depth_weight = p.sim3_depth_weight;
   return a;
 }
 
@@ -330,10 +335,10 @@ TrackArgs make_track_args(const lsdg_params& p) {
 // cluster (the cluster owns one pair).
 static const int kCandCluster[] = {2, 4, 8, 16};
 
-lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc) {
+lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc, bool sim3) {
   int n_clusters = std::min(a.n_pairs, std::max(1, tc.max_clusters));
   CK(ctx, cudaMemsetAsync(a.work_counter, 0, sizeof(int), ctx->stream));
-  CK(ctx, launch_track(a, tc.threads, tc.minblocks, tc.cluster, n_clusters, ctx->stream));
+  CK(ctx, launch_track(a, tc.threads, tc.minblocks, tc.cluster, n_clusters, ctx->stream, sim3));
   ctx->launches += 1;
   return LSDG_OK;
 }
@@ -342,7 +347,7 @@ lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc)
 // caller's own data (two runs each, best kept).  The choice is cached per context.
 // The environment variable LSDG_TRACK_SHAPE="threads,cluster" pins the shape instead (used to
 // profile one known configuration); it is ignored when that shape does not fit the device.
-lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, TuneChoice* out) {
+lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, TuneChoice* out, bool sim3) {
   auto it = ctx->tune_cache.find(key);
   if (it != ctx->tune_cache.end()) {
     *out = it->second;
@@ -351,7 +356,7 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
   if (const char* env = std::getenv("LSDG_TRACK_SHAPE")) {
     int nt = 0, c = 0, mb = 1;
     if (std::sscanf(env, "%d,%d,%d", &nt, &c, &mb) >= 2) {
-      int mc = track_max_clusters(nt, mb, c);
+      int mc = track_max_clusters(nt, mb, c, sim3);
       if (mc > 0) {
         TuneChoice tc{nt, mb, c, mc, 0.f};
         ctx->tune_cache[key] = tc;
@@ -370,13 +375,13 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
     for (int c : kCandCluster) {
       int nt = 0, mb = 0;
       track_shape(si, &nt, &mb);
-      int mc = track_max_clusters(nt, mb, c);
+      int mc = track_max_clusters(nt, mb, c, sim3);
       if (mc <= 0) continue;
       TuneChoice tc{nt, mb, c, mc, 0.f};
       float t_best = 1e30f;
       for (int rep = 0; rep < 2; ++rep) {
         CK(ctx, cudaEventRecord(e0, ctx->stream));
-        lsdg_status st = run_tracker(ctx, a, tc);
+        lsdg_status st = run_tracker(ctx, a, tc, sim3);
         if (st != LSDG_OK) return st;
         CK(ctx, cudaEventRecord(e1, ctx->stream));
         CK(ctx, cudaEventSynchronize(e1));
@@ -544,17 +549,18 @@ struct SmallLayout {
   PairDev pair;
   int work;
   int pad;
-  double init[12];
-  double out_pose[12];
-  double out_sums[32];
+  double init[13];
+  double out_pose[13];
+  double out_sums[40];
   lsdg_track_stats stats;
 };
 static_assert(sizeof(SmallLayout) <= kSmallBytes, "small staging buffer too small");
 
 static lsdg_status track_one(lsdg_ctx* ctx, const lsdg_frame* ref, const lsdg_frame* cur, const double* init,
                              bool init_is_ref_to_frame, int top, int bottom, bool eval_only, double* pose_out,
-                             lsdg_track_stats* stats, double* sums) {
+                             lsdg_track_stats* stats, double* sums, bool sim3) {
   if (!ref->fs.h_frames[0].has_depth) return ctx_fail(ctx, LSDG_INVALID_ARG, "reference frame has no depth");
+  if (sim3 && !cur->fs.h_frames[0].has_depth) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3: the other keyframe has no depth");
   if (!cur->has_image || !ref->has_image) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame image not uploaded");
   const FrameDev& R = ref->fs.h_frames[0];
   const FrameDev& Cf = cur->fs.h_frames[0];
@@ -563,7 +569,7 @@ static lsdg_status track_one(lsdg_ctx* ctx, const lsdg_frame* ref, const lsdg_fr
   SmallLayout* ds = (SmallLayout*)ctx->d_small;
   hs->pair.ref = ref->fs.d_frames;
   hs->pair.cur = cur->fs.d_frames;
-  std::memcpy(hs->init, init, sizeof(hs->init));
+  std::memcpy(hs->init, init, sizeof(double) * (sim3 ? 13 : 12));
   CK(ctx, cudaMemcpyAsync(ds, hs, offsetof(SmallLayout, out_pose), cudaMemcpyHostToDevice, ctx->stream));
   TrackArgs a = make_track_args(ctx->params);
   a.pairs = &ds->pair;
@@ -580,22 +586,22 @@ static lsdg_status track_one(lsdg_ctx* ctx, const lsdg_frame* ref, const lsdg_fr
   if (eval_only)
     for (int i = 0; i < kMaxLevels; ++i) a.max_iter[i] = 0;
   char key[64];
-  std::snprintf(key, sizeof(key), "one:%dx%d", R.w, R.h);
+  std::snprintf(key, sizeof(key), "%s:%dx%d", sim3 ? "one-sim3" : "one", R.w, R.h);
   TuneChoice tc;
   if (eval_only) {
     tc = TuneChoice{256, 2, 8, 1, 0.f};  // a single pass: any shape, deterministic for the parity tests
   } else {
-    lsdg_status st = autotune(ctx, key, a, &tc);
+    lsdg_status st = autotune(ctx, key, a, &tc, sim3);
     if (st != LSDG_OK) return st;
   }
-  lsdg_status st = run_tracker(ctx, a, tc);
+  lsdg_status st = run_tracker(ctx, a, tc, sim3);
   if (st != LSDG_OK) return st;
   CK(ctx, cudaMemcpyAsync(&hs->out_pose, &ds->out_pose, sizeof(SmallLayout) - offsetof(SmallLayout, out_pose),
                           cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
-  if (pose_out) std::memcpy(pose_out, hs->out_pose, sizeof(hs->out_pose));
+  if (pose_out) std::memcpy(pose_out, hs->out_pose, sizeof(double) * (sim3 ? 13 : 12));
   if (stats) *stats = hs->stats;
-  if (sums) std::memcpy(sums, hs->out_sums, sizeof(hs->out_sums));
+  if (sums) std::memcpy(sums, hs->out_sums, sizeof(double) * (sim3 ? 40 : 32));
   return (lsdg_status)hs->stats.status;
 }
 
@@ -605,11 +611,32 @@ lsdg_status lsdg_se3_normal_equations(lsdg_ctx* ctx, const lsdg_frame* reference
                                       const double ref_to_frame[12], double out[LSDG_NE_SIZE]) {
   if (!ctx || !reference || !frame || !ref_to_frame || !out) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   if (level < 0 || level >= ctx->params.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
-  double sums[32];
-  lsdg_status st = track_one(ctx, reference, frame, ref_to_frame, true, level, level, true, nullptr, nullptr, sums);
+  double sums[40];
+  lsdg_status st = track_one(ctx, reference, frame, ref_to_frame, true, level, level, true, nullptr, nullptr, sums, false);
   if (st != LSDG_OK && st != LSDG_TRACKING_LOST) return st;
   std::memcpy(out, sums, sizeof(double) * LSDG_NE_SIZE);
   return LSDG_OK;
+}
+
+lsdg_status lsdg_sim3_normal_equations(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame, int level,
+                                       const double ref_to_frame[13], double out[LSDG_NE_SIZE_SIM3]) {
+  if (!ctx || !reference || !frame || !ref_to_frame || !out) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (level < 0 || level >= ctx->params.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
+  if (!(ref_to_frame[12] > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 scale must be > 0");
+  double sums[40];
+  lsdg_status st = track_one(ctx, reference, frame, ref_to_frame, true, level, level, true, nullptr, nullptr, sums, true);
+  if (st != LSDG_OK && st != LSDG_TRACKING_LOST) return st;
+  std::memcpy(out, sums, sizeof(double) * LSDG_NE_SIZE_SIM3);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_track_sim3(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame,
+                            const double frame_to_ref_init[13], double frame_to_ref_out[13], lsdg_track_stats* stats) {
+  if (!ctx || !reference || !frame || !frame_to_ref_init || !frame_to_ref_out)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (!(frame_to_ref_init[12] > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 scale must be > 0");
+  return track_one(ctx, reference, frame, frame_to_ref_init, false, ctx->params.levels - 1, 0, false, frame_to_ref_out,
+                   stats, nullptr, true);
 }
 
 lsdg_status lsdg_track_se3(lsdg_ctx* ctx, const lsdg_frame* reference, const lsdg_frame* frame,
@@ -617,7 +644,7 @@ lsdg_status lsdg_track_se3(lsdg_ctx* ctx, const lsdg_frame* reference, const lsd
   if (!ctx || !reference || !frame || !frame_to_ref_init || !frame_to_ref_out)
     return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   return track_one(ctx, reference, frame, frame_to_ref_init, false, ctx->params.levels - 1, 0, false, frame_to_ref_out,
-                   stats, nullptr);
+                   stats, nullptr, false);
 }
 
 }  // extern "C"

@@ -34,6 +34,8 @@ int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cu
 
 struct lsdg_batch {
   int n = 0;
+  bool sim3 = false;  // Sim3 constraint tracking: both keyframes of a pair carry depth
+  int pose_len = 12;  // doubles per pose: 12 (SE3) or 13 (Sim3: R, t, s)
   FrameSet fs;
   PairDev* d_pairs = nullptr;
   int* d_order = nullptr;
@@ -85,6 +87,8 @@ static lsdg_status batch_track_args(lsdg_ctx* ctx, lsdg_batch* b, TrackArgs* a) 
 }
 
 static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, int* launches) {
+  // band pass over all 2n frames (also the depth pyramids of the second keyframes in Sim3 mode);
+  // reference points only for the first n
   const int L = ctx->params.levels;
   int k = launch_frame_pyramid(b->fs.d_frames, 2 * b->n, L, b->fs.max_pix, b->fs.max_h, false, ctx->stream);
   k += launch_frame_points(b->fs.d_frames, b->n, L, b->fs.max_h, ctx->stream);
@@ -93,16 +97,16 @@ static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, int* launches) {
   return LSDG_OK;
 }
 
-extern "C" {
-
-lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
-                              lsdg_batch** out) {
+static lsdg_status batch_create(lsdg_ctx* ctx, int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
+                                bool sim3, lsdg_batch** out) {
   if (!ctx || !widths || !heights || !intr || !out || n <= 0) return ctx_fail(ctx, LSDG_INVALID_ARG, "bad batch arguments");
   *out = nullptr;
   CK(ctx, cudaSetDevice(ctx->device));
   lsdg_batch* b = new (std::nothrow) lsdg_batch();
   if (!b) return LSDG_OUT_OF_MEMORY;
   b->n = n;
+  b->sim3 = sim3;
+  b->pose_len = sim3 ? 13 : 12;
   std::vector<int> w(2 * n), h(2 * n);
   std::vector<lsdg_intrinsics> k(2 * n);
   bool* dep = new bool[2 * n];
@@ -111,7 +115,7 @@ lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int
     h[i] = h[n + i] = heights[i];
     k[i] = k[n + i] = intr[i];
     dep[i] = true;
-    dep[n + i] = false;
+    dep[n + i] = sim3;
   }
   // the tracker samples intensity planes only: no gradient pyramid for batch frames
   lsdg_status st = frameset_alloc(ctx, b->fs, 2 * n, w.data(), h.data(), k.data(), dep, ctx->params.levels, false);
@@ -129,11 +133,11 @@ lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(PairDev) * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_order, sizeof(int) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_init, sizeof(double) * 12 * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_out, sizeof(double) * 12 * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_init, sizeof(double) * b->pose_len * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_stats, sizeof(lsdg_track_stats) * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_work, sizeof(int) * 4);
-  if (e == cudaSuccess) e = cudaMallocHost(&b->h_out, sizeof(double) * 12 * n);
+  if (e == cudaSuccess) e = cudaMallocHost(&b->h_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_stats, sizeof(lsdg_track_stats) * n);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_counts, sizeof(int) * kMaxLevels * n);
   for (auto& ev : b->ev)
@@ -150,7 +154,7 @@ lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int
   std::vector<std::pair<int, int>> sz(n);
   for (int i = 0; i < n; ++i) sz[i] = {widths[i], heights[i]};
   std::sort(sz.begin(), sz.end());
-  std::string key = "batch:";
+  std::string key = sim3 ? "batch-sim3:" : "batch:";
   for (int i = 0; i < n;) {
     int j = i;
     while (j < n && sz[j] == sz[i]) ++j;
@@ -160,6 +164,18 @@ lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int
   b->key = key;
   *out = b;
   return LSDG_OK;
+}
+
+extern "C" {
+
+lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
+                              lsdg_batch** out) {
+  return batch_create(ctx, n, widths, heights, intr, false, out);
+}
+
+lsdg_status lsdg_batch_create_sim3(lsdg_ctx* ctx, int n, const int* widths, const int* heights,
+                                   const lsdg_intrinsics* intr, lsdg_batch** out) {
+  return batch_create(ctx, n, widths, heights, intr, true, out);
 }
 
 lsdg_status lsdg_batch_destroy(lsdg_ctx* ctx, lsdg_batch* b) {
@@ -173,6 +189,7 @@ lsdg_status lsdg_batch_load(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_image
                             const float* ref_var, const float* new_images, const double* init) {
   if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !init)
     return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 batch: use lsdg_batch_load_sim3");
   const size_t half = b->fs.pix_depth * 4;  // the keyframes come first, all with depth
   char* base = (char*)b->fs.arena;
   CK(ctx, cudaMemcpyAsync(b->fs.plane0, ref_images, half, cudaMemcpyHostToDevice, ctx->stream));
@@ -180,6 +197,26 @@ lsdg_status lsdg_batch_load(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_image
   CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
   CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, ctx->stream));
   CK(ctx, cudaMemcpyAsync(b->d_init, init, sizeof(double) * 12 * b->n, cudaMemcpyHostToDevice, ctx->stream));
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_load_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
+                                 const float* ref_var, const float* new_images, const float* new_idepth,
+                                 const float* new_var, const double* init) {
+  if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !new_idepth || !new_var || !init)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (!b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "not a Sim3 batch (lsdg_batch_create_sim3)");
+  for (int i = 0; i < b->n; ++i)
+    if (!(init[13 * i + 12] > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "pair %d: Sim3 scale must be > 0", i);
+  const size_t half = b->fs.pix_depth / 2 * 4;  // both halves carry depth: the keyframes i, then j
+  char* base = (char*)b->fs.arena;
+  CK(ctx, cudaMemcpyAsync(b->fs.plane0, ref_images, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync((char*)b->fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0 + half, new_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0 + half, new_var, half, cudaMemcpyHostToDevice, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(b->d_init, init, sizeof(double) * 13 * b->n, cudaMemcpyHostToDevice, ctx->stream));
   return LSDG_OK;
 }
 
@@ -197,7 +234,7 @@ lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
     ctx->launches += k;
     TrackArgs a;
     batch_track_args(ctx, b, &a);
-    st = autotune(ctx, b->key, a, &b->tc);
+    st = autotune(ctx, b->key, a, &b->tc, b->sim3);
     if (st != LSDG_OK) return st;
     // capture: events, build, tracker
     CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -207,7 +244,7 @@ lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
     st = enqueue_build(ctx, b, &nl);
     cudaEventRecordWithFlags(b->ev[1], ctx->stream, cudaEventRecordExternal);
     int64_t before = ctx->launches;
-    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc);
+    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc, b->sim3);
     nl += (int)(ctx->launches - before);
     ctx->launches = before;
     cudaEventRecordWithFlags(b->ev[2], ctx->stream, cudaEventRecordExternal);
@@ -232,12 +269,22 @@ lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
 
 lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* b, double* out, lsdg_track_stats* stats) {
   if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
-  CK(ctx, cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * 12 * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
-  if (out) std::memcpy(out, b->h_out, sizeof(double) * 12 * b->n);
+  if (out) std::memcpy(out, b->h_out, sizeof(double) * b->pose_len * b->n);
   if (stats) std::memcpy(stats, b->h_stats, sizeof(lsdg_track_stats) * b->n);
   return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_track_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
+                                  const float* ref_var, const float* new_images, const float* new_idepth,
+                                  const float* new_var, const double* init, double* out, lsdg_track_stats* stats) {
+  lsdg_status st = lsdg_batch_load_sim3(ctx, b, ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var, init);
+  if (st != LSDG_OK) return st;
+  st = lsdg_batch_run(ctx, b);
+  if (st != LSDG_OK) return st;
+  return lsdg_batch_read(ctx, b, out, stats);
 }
 
 lsdg_status lsdg_batch_track_se3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
@@ -279,9 +326,13 @@ lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* b, int64_t* passes, doubl
       const double pix = (double)(b->fs.w[i] >> l) * (b->fs.h[i] >> l);
       const int ps = b->h_stats[i].passes[l];
       np += ps;
-      // per pass: points (float4 + float) + the frame level's I, gx, gy + the 27 sums
-      pb += ps * (pts * 20.0 + pix * 12.0 + 27 * 4.0);
-      if (ps > 0) ub += pts * 20.0 + pix * 12.0;
+      // per pass: each point's float4 + its frozen variance (psig; the first pass reads pvar and
+      // writes psig instead), the frame level's intensity plane, the sums.  Sim3 adds the point's
+      // depth variance (psigd) and the other keyframe's inverse depth and variance planes.
+      const double per_pt = b->sim3 ? 24.0 : 20.0, per_px = b->sim3 ? 12.0 : 4.0;
+      const double sums = b->sim3 ? 36 * 4.0 : 28 * 4.0;
+      pb += ps * (pts * per_pt + pix * per_px + sums);
+      if (ps > 0) ub += pts * per_pt + pix * per_px;
     }
   }
   if (passes) *passes = np;

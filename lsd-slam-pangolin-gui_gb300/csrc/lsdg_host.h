@@ -59,5 +59,5 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
                            const bool* depth, int levels, bool grads);
 void frameset_free(FrameSet& fs);
 lsdg::TrackArgs make_track_args(const lsdg_params& p);
-lsdg_status run_tracker(lsdg_ctx* ctx, const lsdg::TrackArgs& a, const TuneChoice& tc);
-lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const lsdg::TrackArgs& a, TuneChoice* out);
+lsdg_status run_tracker(lsdg_ctx* ctx, const lsdg::TrackArgs& a, const TuneChoice& tc, bool sim3);
+lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const lsdg::TrackArgs& a, TuneChoice* out, bool sim3);

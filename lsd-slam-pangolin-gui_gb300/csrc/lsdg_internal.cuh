@@ -33,6 +33,7 @@ struct FrameDev {
   float4* pxyzi[kMaxLevels];
   float* pvar[kMaxLevels];
   float* psig[kMaxLevels];
+  float* psigd[kMaxLevels];      // Sim3 tracker scratch: variance of the inverse-depth residual
   int* pcount;                   // [kMaxLevels]
   int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per band, then offsets
   float fx[kMaxLevels], fy[kMaxLevels], cx[kMaxLevels], cy[kMaxLevels];
@@ -50,15 +51,15 @@ struct TrackArgs {
   const int* order;          // processing order (largest first); nullptr = identity
   int n_pairs;
   int* work_counter;         // zeroed before the launch
-  const double* init;        // 12 per pair: frame_to_ref, or ref_to_frame if init_is_ref_to_frame
+  const double* init;        // 12 or 13 per pair: frame_to_ref, or ref_to_frame if init_is_ref_to_frame
   int init_is_ref_to_frame;
-  double* out_pose;          // 12 per pair: frame_to_ref
+  double* out_pose;          // 12 (SE3) or 13 (Sim3: R, t, s) per pair: frame_to_ref
   lsdg_track_stats* out_stats;
-  double* out_sums;          // optional: 32 per pair, the last accepted pass at the bottom level
+  double* out_sums;          // optional: 32 (SE3) or 40 (Sim3) per pair, the last accepted pass
   int top_level;             // first (coarsest) level to run
   int bottom_level;          // last level to run
   int max_iter[kMaxLevels];
-  float photometric_variance, huber_delta, min_z, border_margin;
+  float photometric_variance, huber_delta, min_z, border_margin, sim3_depth_variance, sim3_depth_weight;
   double lambda0, lambda_up, lambda_down, step_eps, stall_eps;
   float min_good_ratio, min_usage;
 };

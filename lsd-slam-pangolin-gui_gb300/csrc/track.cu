@@ -1,8 +1,12 @@
-// track.cu -- a3/a4/a5/a11 of the hot path: SE3 direct image alignment.
+// track.cu -- a3/a4/a5/a6/a11 of the hot path: SE3 and Sim3 direct image alignment.
 //
-// Upstream: SE3Tracker::trackFrame and its calculateWarpUpdate (lsd-slam fips import, absent from
-// the reference; the call chain starts at lib/App/InputThread.cpp:71).  Method: ECCV 2014 sec. 3.2
-// -- variance-normalised photometric residual, Huber weights, LM on se(3), coarse to fine.
+// Upstream: SE3Tracker::trackFrame and its calculateWarpUpdate, Sim3Tracker::trackFrameSim3
+// (lsd-slam fips import, absent from the reference; the call chain starts at
+// lib/App/InputThread.cpp:71).  Method: ECCV 2014 sec. 3.2 -- variance-normalised photometric
+// residual, Huber weights, LM on se(3), coarse to fine; sec. 3.3 -- Sim3 alignment of two keyframes
+// with an added inverse-depth residual against the other keyframe's depth map, LM on sim(3).
+// The kernel is one template: SIM3 = false tracks 6 parameters with 28 sums per pass, SIM3 = true
+// 7 parameters (log-scale added) with 36 sums.
 //
 // GB300 design.  One persistent kernel tracks any number of pairs.  Each pair is owned by one
 // thread-block cluster (C CTAs of NT threads, C up to 16); clusters pull pairs from an atomic work
@@ -38,7 +42,23 @@ namespace cg = cooperative_groups;
 
 namespace lsdg {
 
-constexpr int kSums = 28;  // 21 (H) + 6 (g) + 1 (energy)
+// Per-mode sizes: DOF parameters, NH entries of the upper triangle of H, NS compensated sums per
+// pass (H, g, energy), REC doubles in the pass record (NS + points used, inliers, outliers,
+// left the image).
+template <bool SIM3>
+struct Mode {
+  static constexpr int DOF = SIM3 ? 7 : 6;
+  static constexpr int NH = DOF * (DOF + 1) / 2;
+  static constexpr int NS = NH + DOF + 1;
+  static constexpr int REC = NS + 4;
+  static constexpr int POSE = SIM3 ? 13 : 12;  // doubles per pose in the API
+};
+constexpr int kMaxSums = 36;
+constexpr int kMaxRec = 40;
+
+// Taylor coefficients 1 / (k! (shift + k)) of the sim(3) exp series, shift = 1..11, k = 0..20
+// (filled by track_prepare).
+__constant__ double c_sim3_tab[11][21];
 
 __device__ __forceinline__ void kadd(float& s, float& c, float x) {
   const float y = x - c;
@@ -78,32 +98,34 @@ struct Ctl {
 };
 
 struct CtaPart {
-  float s[kSums];
-  float c[kSums];
+  float s[kMaxSums];
+  float c[kMaxSums];
   int cnt[3];  // good, bad, out-of-image
 };
 
 enum { PH_INIT = 0, PH_TRY = 1 };
 
 struct LMState {
-  double T[12];     // ref_to_frame, accepted
+  double T[12];     // ref_to_frame [M | t] (M = R, or sR for Sim3), accepted
   double Ttry[12];  // ref_to_frame being evaluated
-  double S[32];     // sums of the last accepted pass
+  double S[kMaxRec];  // record of the last accepted pass
   double E, lambda, gnmax;
   int it, phase, level, pair, have_final, fresh;
   int s_src;  // 0: lm.S holds the sums of the pass just merged, 1: of an earlier pass
   int need_exp;  // try_step chose dx: the warp applies exp(dx) * T and publishes the trial pose
-  double dx[6];
+  double dx[7];
   lsdg_track_stats st;
 };
 
 // ------------------------------------------------------------------------------------------
 // FP64 SE(3) helpers (thread 0 of rank 0 only)
 // ------------------------------------------------------------------------------------------
-__device__ __noinline__ void se3_inv_d(const double* A, double* B) {
+// [M | t]^-1 for M = R (SE3) or M = sR (Sim3: M^-1 = M^T / s^2; s^2 = 1 for a rotation).
+__device__ __noinline__ void se3_inv_d(const double* A, double* B, bool sim3) {
+  const double s2 = sim3 ? (A[0] * A[0] + A[1] * A[1]) + A[2] * A[2] : 1.0;
   double o[12];
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) o[4 * i + j] = A[4 * j + i];
+    for (int j = 0; j < 3; ++j) o[4 * i + j] = sim3 ? A[4 * j + i] / s2 : A[4 * j + i];
   for (int i = 0; i < 3; ++i) o[4 * i + 3] = -((o[4 * i + 0] * A[3] + o[4 * i + 1] * A[7]) + o[4 * i + 2] * A[11]);
   for (int i = 0; i < 12; ++i) B[i] = o[i];
 }
@@ -130,14 +152,81 @@ __device__ __forceinline__ void se3_coeffs(double th2, double& A, double& B, dou
   }
 }
 
+// Coefficients a0, a1, a2 of V = a0 I + a1 K + a2 K^2 in the sim(3) exp (integrals of e^{sigma tau}
+// against 1, sin(theta tau)/theta, (1 - cos(theta tau))/theta^2 over [0, 1]); same rule as the CPU
+// oracle: for theta < 0.05 and |sigma| < 1 the double Taylor series, evaluated with lanes 0..4
+// (a1 terms), 8..12 (a2 terms) and 16 (a0) running one 21-term Horner chain each; otherwise the
+// closed forms.  Every lane must call; all lanes return the same values.
+__device__ __forceinline__ void sim3_coeffs_warp(double th2, double sg, int lane, double& a0, double& a1, double& a2) {
+  if (th2 < 0.0025 && fabs(sg) < 1.0) {
+    const int m = lane & 7;
+    const int shift = lane < 8 ? 2 * m + 2 : lane < 16 ? 2 * m + 3 : 1;
+    const int row = (lane < 16 && m > 4) ? 0 : shift - 1;  // idle lanes read a valid row
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 20; k >= 0; --k) acc = acc * sg + c_sim3_tab[row][k];
+    a0 = __shfl_sync(0xffffffffu, acc, 16);
+    // 1/(2m+1)! and 1/(2m+2)! for m = 0..4
+    const double if1[5] = {1.0, 1.0 / 6.0, 1.0 / 120.0, 1.0 / 5040.0, 1.0 / 362880.0};
+    const double if2[5] = {0.5, 1.0 / 24.0, 1.0 / 720.0, 1.0 / 40320.0, 1.0 / 3628800.0};
+    double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int mm = 4; mm >= 0; --mm) {
+      s1 = s1 * (-th2) + __shfl_sync(0xffffffffu, acc, mm) * if1[mm];
+      s2 = s2 * (-th2) + __shfl_sync(0xffffffffu, acc, 8 + mm) * if2[mm];
+    }
+    a1 = s1;
+    a2 = s2;
+    return;
+  }
+  if (th2 < 0.0025) {
+    // theta < 0.05, |sigma| >= 1 (rare: a scale step of e or more): the theta series with
+    // I_n(sigma) = int_0^1 t^(n-1) e^(sigma t) dt from the upward recurrence
+    // I_n = (e^sigma - (n-1) I_(n-1)) / sigma, whose error growth (n-1)!/|sigma|^(n-1) the series'
+    // 1/(n-1)! cancels.  Every lane computes it.
+    const double es = exp(sg), is = 1.0 / sg;
+    double I[12];
+    I[1] = (es - 1.0) * is;
+#pragma unroll
+    for (int n = 2; n <= 11; ++n) I[n] = (es - (double)(n - 1) * I[n - 1]) * is;
+    const double f1[5] = {1.0, 6.0, 120.0, 5040.0, 362880.0};        // (2m+1)!
+    const double f2[5] = {2.0, 24.0, 720.0, 40320.0, 3628800.0};     // (2m+2)!
+    double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int mm = 4; mm >= 0; --mm) {
+      s1 = s1 * (-th2) + I[2 * mm + 2] / f1[mm];
+      s2 = s2 * (-th2) + I[2 * mm + 3] / f2[mm];
+    }
+    a0 = I[1];
+    a1 = s1;
+    a2 = s2;
+    return;
+  }
+  const double th = sqrt(th2), es = exp(sg);
+  double sn, cs;
+  sincos(th, &sn, &cs);
+  const double D = sg * sg + th2;
+  a0 = fabs(sg) < 1e-8 ? 1.0 + 0.5 * sg : (es - 1.0) / sg;
+  const double S1 = (es * (sg * sn - th * cs) + th) / D;
+  const double C1 = (es * (sg * cs + th * sn) - sg) / D;
+  a1 = S1 / th;
+  a2 = (a0 - C1) / th2;
+}
+
 // Tout = exp(xi) * Tin (3x4 row-major), computed by a whole warp: lane e < 9 builds element e of
-// R and V, lanes 0..2 the translation, lane o < 12 one element of the product.  xi, Tin, Tout are
-// in shared memory; every lane must call.
+// the rotation (times e^sigma for Sim3) and of V, lanes 0..2 the translation, lane o < 12 one element
+// of the product.  xi (6 or 7 doubles), Tin, Tout are in shared memory; every lane must call.
+template <bool SIM3>
 __device__ __forceinline__ void warp_exp_mul(const double* xi, const double* Tin, double* Tout, int lane) {
   const double v0 = xi[0], v1 = xi[1], v2 = xi[2], w0 = xi[3], w1 = xi[4], w2 = xi[5];
   const double th2 = (w0 * w0 + w1 * w1) + w2 * w2;
   double A, B, Cc;
   se3_coeffs(th2, A, B, Cc);
+  double sc = 1.0, a0 = 1.0, a1 = B, a2 = Cc;  // SE3: V = I + B K + C K^2
+  if (SIM3) {
+    sim3_coeffs_warp(th2, xi[6], lane, a0, a1, a2);
+    sc = exp(xi[6]);
+  }
   const int e = lane < 9 ? lane : 0;
   const int i = e / 3, j = e % 3;
   const double wi = i == 0 ? w0 : i == 1 ? w1 : w2;
@@ -146,8 +235,9 @@ __device__ __forceinline__ void warp_exp_mul(const double* xi, const double* Tin
   const double K = e == 1 ? -w2 : e == 2 ? w1 : e == 3 ? w2 : e == 5 ? -w0 : e == 6 ? -w1 : e == 7 ? w0 : 0.0;
   const double I = (i == j) ? 1.0 : 0.0;
   const double K2 = wi * wj - ((i == j) ? th2 : 0.0);
-  const double R = (I + A * K) + B * K2;
-  const double V = (I + B * K) + Cc * K2;
+  double R = (I + A * K) + B * K2;
+  if (SIM3) R = sc * R;
+  const double V = (a0 * I + a1 * K) + a2 * K2;
   // translation t_i = V_i0 v0 + V_i1 v1 + V_i2 v2 (lanes 0..2 gather their row of V)
   const int tr = lane < 3 ? lane : 0;
   const double V0 = __shfl_sync(0xffffffffu, V, 3 * tr + 0);
@@ -216,41 +306,42 @@ __device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, co
   return ok;
 }
 
-// Solves computed ahead of the LM decision by warp 0, four systems at once (lanes 8g .. 8g+5 own
+// Solves computed ahead of the LM decision by warp 0, four systems at once (lanes 8g .. 8g+N-1 own
 // the rows of system g): [0] undamped step of the pass just merged, [1] damped step if that pass is
 // accepted (or is a level's first pass), [2] and [3] damped steps on the kept linearisation after
 // one or two rejections.  The decision logic takes an entry only when source and lambda match.
 struct SolveCache {
-  double x[4][6];
+  double x[4][8];
   double lambda[4];
   int src[4];  // 0: the sums of the pass just merged, 1: the sums kept from an earlier pass
   int ok[4];
   int valid[4];
-  double Ls[4][6][6];  // per-group L of the factorisation (row-major), for the back substitution
+  double Ls[4][8][8];  // per-group L of the factorisation (row-major), for the back substitution
 };
 
-// Row-per-lane LDL^T solve of (H + lambda diag H) x = -g for the group of 8 lanes starting at
-// `base` (rows 0..5; lanes 6, 7 mirror row 5 and their results are dropped).  hu: upper triangle of
-// H (row-major), g: right-hand side, both in shared memory.  About 25 FP64 warp instructions plus
-// six reciprocals, whatever the group count.
-__device__ __forceinline__ void warp_solve6(const double* __restrict__ hu, const double* __restrict__ g, double lambda,
-                                            int lane, double (*Ls)[6], double* xout, int* okout) {
+// Row-per-lane LDL^T solve of (H + lambda diag H) x = -g (N <= 7) for the group of 8 lanes starting
+// at `base` (rows 0..N-1; the other lanes of the group mirror row N-1 and their results are dropped).
+// hu: upper triangle of H (row-major), g: right-hand side, both in shared memory.  About 4N FP64 warp
+// instructions plus N reciprocals, whatever the number of groups.
+template <int N>
+__device__ __forceinline__ void warp_solve(const double* __restrict__ hu, const double* __restrict__ g, double lambda,
+                                           int lane, double (*Ls)[8], double* xout, int* okout) {
   const int base = lane & ~7;
-  const int r = (lane & 7) < 6 ? (lane & 7) : 5;
-  double a[6], l[6], wv[6], inv[6];
+  const int r = (lane & 7) < N ? (lane & 7) : N - 1;
+  double a[N], l[N], wv[N], inv[N];
 #pragma unroll
-  for (int j = 0; j < 6; ++j) {
+  for (int j = 0; j < N; ++j) {
     const int lo = r < j ? r : j, hi = r < j ? j : r;
-    a[j] = hu[lo * 6 - (lo * (lo - 1)) / 2 + (hi - lo)];
+    a[j] = hu[lo * N - (lo * (lo - 1)) / 2 + (hi - lo)];
     l[j] = 0.0;
     wv[j] = 0.0;
   }
 #pragma unroll
-  for (int j = 0; j < 6; ++j)
+  for (int j = 0; j < N; ++j)
     if (j == r) a[j] = a[j] * (1.0 + lambda);
   bool ok = true;
 #pragma unroll
-  for (int j = 0; j < 6; ++j) {
+  for (int j = 0; j < N; ++j) {
     double t = a[j];
 #pragma unroll
     for (int k = 0; k < j; ++k) t = t - l[k] * __shfl_sync(0xffffffffu, wv[k], base + j);  // L_rk * (L_jk d_k)
@@ -265,28 +356,28 @@ __device__ __forceinline__ void warp_solve6(const double* __restrict__ hu, const
   // forward: y_r = -g_r - sum_{k<r} L_rk y_k, column by column
   double y = -g[r];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) {
+  for (int k = 0; k < N; ++k) {
     const double yk = __shfl_sync(0xffffffffu, y, base + k);
     if (r > k) y = y - l[k] * yk;
   }
   double ir = inv[0];
 #pragma unroll
-  for (int j = 1; j < 6; ++j)
+  for (int j = 1; j < N; ++j)
     if (j == r) ir = inv[j];
   y = y * ir;
   // backward: x_r = y_r - sum_{k>r} L_kr x_k (L rows exchanged through shared memory)
-  if ((lane & 7) < 6) {
+  if ((lane & 7) < N) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) Ls[r][k] = l[k];
+    for (int k = 0; k < N; ++k) Ls[r][k] = l[k];
   }
   __syncwarp();
   double x = y;
 #pragma unroll
-  for (int k = 5; k >= 0; --k) {
+  for (int k = N - 1; k >= 0; --k) {
     const double xk = __shfl_sync(0xffffffffu, x, base + k);
     if (r < k) x = x - Ls[k][r] * xk;
   }
-  if ((lane & 7) < 6) xout[r] = x;
+  if ((lane & 7) < N) xout[r] = x;
   if ((lane & 7) == 0) *okout = ok ? 1 : 0;
 }
 
@@ -319,34 +410,49 @@ __device__ bool start_level(const TrackArgs& a, LMState& lm, Ctl& ctl, int level
   return false;
 }
 
+template <bool SIM3>
 __device__ __noinline__ void finish_pair(const TrackArgs& a, LMState& lm) {
+  using Md = Mode<SIM3>;
   const int p = lm.pair;
   lsdg_track_stats& st = lm.st;
   double out[12];
-  se3_inv_d(lm.T, out);
-  for (int i = 0; i < 12; ++i) a.out_pose[12 * p + i] = out[i];
+  se3_inv_d(lm.T, out, SIM3);
+  double* dst = a.out_pose + (size_t)Md::POSE * p;
+  if (SIM3) {  // {R, t, s}
+    const double sc = sqrt((out[0] * out[0] + out[1] * out[1]) + out[2] * out[2]);
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 3; ++j) dst[3 * i + j] = out[4 * i + j] / sc;
+      dst[9 + i] = out[4 * i + 3];
+    }
+    dst[12] = sc;
+  } else {
+    for (int i = 0; i < 12; ++i) dst[i] = out[i];
+  }
   int tot = 0;
   for (int l = 0; l < kMaxLevels; ++l) tot += st.passes[l];
   st.total_passes = tot;
   st.n_points = level_points(a, p, 0);
   const double* S = lm.S;
+  const int iN = Md::NS;
   if (lm.have_final) {
-    st.n_valid = (int)S[28];
-    st.n_good = (int)S[29];
-    st.mean_energy = S[28] > 0 ? (float)(S[27] / S[28]) : 0.f;
-    st.good_ratio = S[28] > 0 ? (float)(S[29] / S[28]) : 0.f;
-    st.usage = st.n_points > 0 ? (float)(S[28] / st.n_points) : 0.f;
-    for (int i = 0; i < 21; ++i) st.hessian[i] = S[i];
+    st.n_valid = (int)S[iN];
+    st.n_good = (int)S[iN + 1];
+    st.mean_energy = S[iN] > 0 ? (float)(S[iN - 1] / S[iN]) : 0.f;
+    st.good_ratio = S[iN] > 0 ? (float)(S[iN + 1] / S[iN]) : 0.f;
+    st.usage = st.n_points > 0 ? (float)(S[iN] / st.n_points) : 0.f;
+    for (int i = 0; i < Md::NH; ++i) st.hessian[i] = S[i];
   }
   const bool lost = !lm.have_final || st.good_ratio < a.min_good_ratio || st.usage < a.min_usage;
   st.status = lost ? LSDG_TRACKING_LOST : LSDG_OK;
   a.out_stats[p] = st;
   if (a.out_sums)
-    for (int i = 0; i < 32; ++i) a.out_sums[32 * p + i] = S[i];
+    for (int i = 0; i < Md::REC; ++i) a.out_sums[(size_t)Md::REC * p + i] = S[i];
 }
 
 // Takes pairs off the queue until one has a level to run; publishes it (or pair = -1).
+template <bool SIM3>
 __device__ __noinline__ void fetch_pair(const TrackArgs& a, LMState& lm, Ctl& ctl) {
+  using Md = Mode<SIM3>;
   for (;;) {
     const int k = atomicAdd(a.work_counter, 1);
     if (k >= a.n_pairs) {
@@ -361,49 +467,64 @@ __device__ __noinline__ void fetch_pair(const TrackArgs& a, LMState& lm, Ctl& ct
     lm.it = 0;
     lm.E = 0;
     lm.lambda = a.lambda0;
-    for (int i = 0; i < 32; ++i) lm.S[i] = 0;
+    for (int i = 0; i < kMaxRec; ++i) lm.S[i] = 0;
     char* sp = reinterpret_cast<char*>(&lm.st);
     for (int i = 0; i < (int)sizeof(lsdg_track_stats); ++i) sp[i] = 0;
-    if (a.init_is_ref_to_frame) {
-      for (int i = 0; i < 12; ++i) lm.T[i] = a.init[12 * p + i];
+    const double* in = a.init + (size_t)Md::POSE * p;
+    double Tin[12];
+    if (SIM3) {  // {R, t, s} -> [sR | t]
+      for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) Tin[4 * i + j] = in[12] * in[3 * i + j];
+        Tin[4 * i + 3] = in[9 + i];
+      }
     } else {
-      se3_inv_d(a.init + 12 * p, lm.T);
+      for (int i = 0; i < 12; ++i) Tin[i] = in[i];
+    }
+    if (a.init_is_ref_to_frame) {
+      for (int i = 0; i < 12; ++i) lm.T[i] = Tin[i];
+    } else {
+      se3_inv_d(Tin, lm.T, SIM3);
     }
     if (start_level(a, lm, ctl, a.top_level)) return;
-    finish_pair(a, lm);
+    finish_pair<SIM3>(a, lm);
   }
 }
 
+template <bool SIM3>
 __device__ void next_level(const TrackArgs& a, LMState& lm, Ctl& ctl) {
   if (lm.level > a.bottom_level && start_level(a, lm, ctl, lm.level - 1)) return;
-  finish_pair(a, lm);
-  fetch_pair(a, lm, ctl);
+  finish_pair<SIM3>(a, lm);
+  fetch_pair<SIM3>(a, lm, ctl);
 }
 
+template <bool SIM3>
 __device__ __forceinline__ bool cached_solve(LMState& lm, SolveCache& sc, double lambda, double* x) {
+  constexpr int D = Mode<SIM3>::DOF;
 #pragma unroll 1
   for (int k = 0; k < 4; ++k) {
     if (sc.valid[k] && sc.src[k] == lm.s_src && sc.lambda[k] == lambda) {
-      for (int i = 0; i < 6; ++i) x[i] = sc.x[k][i];
+      for (int i = 0; i < D; ++i) x[i] = sc.x[k][i];
       sc.valid[k] = 0;
       return sc.ok[k] != 0;
     }
   }
-  return ldlt_solve_reg<6>(lm.S, lm.S + 21, lambda, x);
+  return ldlt_solve_reg<D>(lm.S, lm.S + Mode<SIM3>::NH, lambda, x);
 }
 
 // One LM iteration decision on the current linearisation lm.S (same rules as the CPU oracle):
 // converged when the undamped Gauss-Newton step is below step_eps * 2^level; otherwise solve the
-// damped system and publish the trial pose, unless the level's iteration budget is spent.
+// damped system and ask the warp for the trial pose, unless the level's iteration budget is spent.
+template <bool SIM3>
 __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& sc) {
+  constexpr int D = Mode<SIM3>::DOF;
   const double thr = a.step_eps * (double)(1 << lm.level);
   for (;;) {
     if (lm.fresh) {
-      double gn[6];
+      double gn[D];
       lm.gnmax = 1e300;
-      if (cached_solve(lm, sc, 0.0, gn)) {
+      if (cached_solve<SIM3>(lm, sc, 0.0, gn)) {
         double m = 0;
-        for (int i = 0; i < 6; ++i) m = fmax(m, fabs(gn[i]));
+        for (int i = 0; i < D; ++i) m = fmax(m, fabs(gn[i]));
         lm.gnmax = m;
         if (m < thr) break;
       }
@@ -411,12 +532,12 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& 
     }
     if (lm.it >= a.max_iter[lm.level]) break;
     lm.it++;
-    double dx[6];
-    if (!cached_solve(lm, sc, lm.lambda, dx)) {
+    double dx[D];
+    if (!cached_solve<SIM3>(lm, sc, lm.lambda, dx)) {
       lm.lambda *= a.lambda_up;
       continue;
     }
-    for (int i = 0; i < 6; ++i) lm.dx[i] = dx[i];
+    for (int i = 0; i < D; ++i) lm.dx[i] = dx[i];
     lm.need_exp = 1;  // the warp computes lm.Ttry = exp(dx) * lm.T and publishes it
     lm.phase = PH_TRY;
     ctl.pair = lm.pair;
@@ -424,48 +545,53 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& 
     ctl.first = 0;
     return;
   }
-  next_level(a, lm, ctl);
+  next_level<SIM3>(a, lm, ctl);
 }
 
+template <bool SIM3>
 __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ctl, const double* tot, SolveCache& sc) {
+  using Md = Mode<SIM3>;
   lm.st.passes[lm.level]++;
-  const double N = tot[28];
+  const double N = tot[Md::NS];
+  const double En = tot[Md::NS - 1];
   if (lm.phase == PH_INIT) {
     if (N > 0) {
-      for (int i = 0; i < 32; ++i) lm.S[i] = tot[i];
+      for (int i = 0; i < Md::REC; ++i) lm.S[i] = tot[i];
       lm.s_src = 0;
-      lm.E = tot[27] / N;
+      lm.E = En / N;
       lm.lambda = a.lambda0;
       lm.it = 0;
       lm.fresh = 1;
       if (lm.level == a.bottom_level) lm.have_final = 1;
-      try_step(a, lm, ctl, sc);
+      try_step<SIM3>(a, lm, ctl, sc);
     } else {
-      next_level(a, lm, ctl);
+      next_level<SIM3>(a, lm, ctl);
     }
     return;
   }
-  if (N > 0 && tot[27] / N < lm.E) {
+  if (N > 0 && En / N < lm.E) {
     for (int i = 0; i < 12; ++i) lm.T[i] = lm.Ttry[i];
-    for (int i = 0; i < 32; ++i) lm.S[i] = tot[i];
+    for (int i = 0; i < Md::REC; ++i) lm.S[i] = tot[i];
     lm.s_src = 0;
-    lm.E = tot[27] / N;
+    lm.E = En / N;
     lm.lambda *= a.lambda_down;
     lm.fresh = 1;
   } else {
     lm.s_src = 1;
     if (lm.gnmax < a.stall_eps * (double)(1 << lm.level)) {  // noise floor of this level
-      next_level(a, lm, ctl);
+      next_level<SIM3>(a, lm, ctl);
       return;
     }
     lm.lambda *= a.lambda_up;
   }
-  try_step(a, lm, ctl, sc);
+  try_step<SIM3>(a, lm, ctl, sc);
 }
 
 // Warp 0 of cluster rank 0 solves the four systems the decision may need (see SolveCache).
+template <bool SIM3>
 __device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm, const double* tot, SolveCache& sc,
                                           int lane) {
+  using Md = Mode<SIM3>;
   const int grp = lane >> 3;
   const bool init = lm.phase == PH_INIT;
   const double* S = grp >= 2 ? lm.S : tot;
@@ -473,11 +599,11 @@ __device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm,
                    : grp == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down)
                    : grp == 2 ? lm.lambda * a.lambda_up
                               : (lm.lambda * a.lambda_up) * a.lambda_up;
-  warp_solve6(S, S + 21, lam, lane, sc.Ls[grp], sc.x[grp], &sc.ok[grp]);
+  warp_solve<Md::DOF>(S, S + Md::NH, lam, lane, sc.Ls[grp], sc.x[grp], &sc.ok[grp]);
   if ((lane & 7) == 0) {
     sc.lambda[grp] = lam;
     sc.src[grp] = grp >= 2 ? 1 : 0;
-    sc.valid[grp] = (tot[28] > 0 && (grp < 2 || !init)) ? 1 : 0;
+    sc.valid[grp] = (tot[Md::NS] > 0 && (grp < 2 || !init)) ? 1 : 0;
   }
 }
 
@@ -505,20 +631,31 @@ __device__ __forceinline__ void warp_reduce_scatter(float (&s)[32], float (&c)[3
   }
 }
 
-template <int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) {
+// Butterfly merge of a few compensated sums across the warp (every lane ends with the totals).
+template <int K>
+__device__ __forceinline__ void warp_butterfly(float (&s)[K], float (&c)[K]) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < K; ++i) kmerge(s[i], c[i], __shfl_xor_sync(0xffffffffu, s[i], o), __shfl_xor_sync(0xffffffffu, c[i], o));
+}
+
+template <int NT, int MINB, bool SIM3>
+__global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
+  using Md = Mode<SIM3>;
   constexpr int NW = NT / 32;
+  constexpr int D = Md::DOF, NH = Md::NH, NS = Md::NS;
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank();
   const unsigned C = cluster.num_blocks();
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
-  __shared__ float ws[NW][kSums];
-  __shared__ float wc[NW][kSums];
+  __shared__ float ws[NW][NS];
+  __shared__ float wc[NW][NS];
   __shared__ int wn[NW][3];
   __shared__ CtaPart allpart[kMaxCluster];  // rank 0's copy receives every rank's partial
   __shared__ Ctl ctl;                       // every rank's copy is written by rank 0
-  __shared__ double tot[32];
+  __shared__ double tot[kMaxRec];
   __shared__ LMState lm;
   __shared__ SolveCache sc;
 
@@ -533,7 +670,7 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
   };
 
   if (rank == 0 && wid == 0) {
-    if (lane == 0) fetch_pair(a, lm, ctl);
+    if (lane == 0) fetch_pair<SIM3>(a, lm, ctl);
     __syncwarp();
     push_ctl();
   }
@@ -551,7 +688,10 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
     const float4* __restrict__ pts = R->pxyzi[level];
     const float* __restrict__ pvar = R->pvar[level];
     float* __restrict__ psig = R->psig[level];
+    float* __restrict__ psigd = R->psigd[level];
     const float* __restrict__ img = Fc->plane[level];
+    const float* __restrict__ Dj = SIM3 ? Fc->idepth[level] : nullptr;
+    const float* __restrict__ Vj = SIM3 ? Fc->ivar[level] : nullptr;
     const int w = Fc->w >> level, h = Fc->h >> level;
     const float fx = Fc->fx[level], fy = Fc->fy[level], cx = Fc->cx[level], cy = Fc->cy[level];
     const float umax = (float)(w - 2), vmax = (float)(h - 2);
@@ -563,12 +703,13 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
     const float R20 = ctl.R[6], R21 = ctl.R[7], R22 = ctl.R[8];
     const float t0 = ctl.t[0], t1 = ctl.t[1], t2 = ctl.t[2];
     const float pvr = a.photometric_variance, delta = a.huber_delta, minz = a.min_z;
+    const float dfloor = a.sim3_depth_variance, wdep = a.sim3_depth_weight;
 
-    float hs[21], hc[21], gs[6], gc[6], es = 0.f, ec = 0.f;
+    float hs[NH], hc[NH], gs[D], gc[D], es = 0.f, ec = 0.f;
 #pragma unroll
-    for (int i = 0; i < 21; ++i) { hs[i] = 0.f; hc[i] = 0.f; }
+    for (int i = 0; i < NH; ++i) { hs[i] = 0.f; hc[i] = 0.f; }
 #pragma unroll
-    for (int i = 0; i < 6; ++i) { gs[i] = 0.f; gc[i] = 0.f; }
+    for (int i = 0; i < D; ++i) { gs[i] = 0.f; gc[i] = 0.f; }
     int good = 0, bad = 0, oob = 0;
 
     for (int k = (int)rank * NT + tid; k < n; k += (int)C * NT) {
@@ -584,7 +725,10 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
       const float Rpz = (R20 * X + R21 * Y) + R22 * Z;
       const float Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
       if (!(Zp > minz)) {
-        if (first) psig[k] = 0.f;
+        if (first) {
+          psig[k] = 0.f;
+          if (SIM3) psigd[k] = 0.f;
+        }
         ++oob;
         continue;
       }
@@ -594,6 +738,7 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
       if (first) {
         if (!(u >= ulo && v >= vlo && u < uhi && v < vhi)) {
           psig[k] = 0.f;
+          if (SIM3) psigd[k] = 0.f;
           ++oob;
           continue;
         }
@@ -622,13 +767,14 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
       const float gxs = Gx * fx, gys = Gy * fy;
       const float a0 = gxs * iz, a1 = gys * iz;
       const float a2 = -((a0 * Xp + a1 * Yp) * iz);
-      float J[6];
+      float J[D];
       J[0] = a0;
       J[1] = a1;
       J[2] = a2;
       J[3] = Yp * a2 - Zp * a1;
       J[4] = Zp * a0 - Xp * a2;
       J[5] = Xp * a1 - Yp * a0;
+      if (SIM3) J[D - 1] = (a0 * Xp + a1 * Yp) + a2 * Zp;
       if (first) {
         const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
         s2 = pvr + (drd * drd) * __ldg(&pvar[k]);
@@ -640,38 +786,120 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
       if (ae <= delta) { wh = 1.f; rho = e2; ++good; }
       else { wh = delta / ae; rho = delta * (2.f * ae - delta); ++bad; }
       const float wgt = wh / s2;
-      float wJ[6];
+      float wJ[D];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) wJ[i] = wgt * J[i];
-      int q2 = 0;
+      for (int i = 0; i < D; ++i) wJ[i] = wgt * J[i];
+      if (!SIM3) {
+        int q2 = 0;
 #pragma unroll
-      for (int i = 0; i < 6; ++i)
+        for (int i = 0; i < D; ++i)
 #pragma unroll
-        for (int j = i; j < 6; ++j) { kadd(hs[q2], hc[q2], wJ[i] * J[j]); ++q2; }
+          for (int j = i; j < D; ++j) { kadd(hs[q2], hc[q2], wJ[i] * J[j]); ++q2; }
 #pragma unroll
-      for (int i = 0; i < 6; ++i) kadd(gs[i], gc[i], wJ[i] * r);
-      kadd(es, ec, rho);
+        for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJ[i] * r);
+        kadd(es, ec, rho);
+      } else {
+        // inverse-depth residual against the other keyframe's depth map (4 valid bilinear corners)
+        float Jd[D], rd = 0.f, wgd = 0.f, rhod = 0.f;
+#pragma unroll
+        for (int i = 0; i < D; ++i) Jd[i] = 0.f;
+        const size_t i00 = (size_t)iy * w + ix;
+        const float D00 = __ldg(&Dj[i00]), D10 = __ldg(&Dj[i00 + 1]), D01 = __ldg(&Dj[i00 + w]), D11 = __ldg(&Dj[i00 + w + 1]);
+        bool dok = D00 > 0.f && D10 > 0.f && D01 > 0.f && D11 > 0.f;
+        float s2d = 0.f;
+        if (!first) {
+          s2d = psigd[k];
+          if (!(s2d > 0.f)) dok = false;
+        }
+        if (dok) {
+          const float bx = 1.f - ax, by = 1.f - ay;
+          const float w00 = bx * by, w10 = ax * by, w01 = bx * ay, w11 = ax * ay;
+          const float Dv = ((w00 * D00 + w10 * D10) + w01 * D01) + w11 * D11;
+          const float Ddx = by * (D10 - D00) + ay * (D11 - D01);
+          const float Ddy = bx * (D01 - D00) + ax * (D11 - D10);
+          rd = iz - Dv;
+          const float c0 = (Ddx * fx) * iz, c1 = (Ddy * fy) * iz;
+          const float c2 = -((c0 * Xp + c1 * Yp) * iz);
+          const float b0 = -c0, b1 = -c1, b2 = -(iz * iz) - c2;
+          Jd[0] = b0;
+          Jd[1] = b1;
+          Jd[2] = b2;
+          Jd[3] = Yp * b2 - Zp * b1;
+          Jd[4] = Zp * b0 - Xp * b2;
+          Jd[5] = Xp * b1 - Yp * b0;
+          Jd[D - 1] = (b0 * Xp + b1 * Yp) + b2 * Zp;
+          if (first) {
+            const float Vv = ((w00 * __ldg(&Vj[i00]) + w10 * __ldg(&Vj[i00 + 1])) + w01 * __ldg(&Vj[i00 + w])) +
+                             w11 * __ldg(&Vj[i00 + w + 1]);
+            const float bdd = -(((b0 * Rpx + b1 * Rpy) + b2 * Rpz) * Z);
+            float sd = Vv + (bdd * bdd) * __ldg(&pvar[k]);
+            if (sd < dfloor) sd = dfloor;
+            psigd[k] = sd;
+            s2d = sd;
+          }
+          const float e2d = (rd * rd) / s2d;
+          const float aed = sqrtf(e2d);
+          if (aed <= delta) { wgd = wdep / s2d; rhod = e2d; }
+          else { wgd = (wdep * (delta / aed)) / s2d; rhod = delta * (2.f * aed - delta); }
+        } else if (first) {
+          psigd[k] = 0.f;
+        }
+        int q2 = 0;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = i; j < D; ++j) { kadd(hs[q2], hc[q2], wJ[i] * J[j] + (wgd * Jd[i]) * Jd[j]); ++q2; }
+#pragma unroll
+        for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJ[i] * r + (wgd * Jd[i]) * rd);
+        kadd(es, ec, rho + wdep * rhod);
+      }
     }
 
-    // warp merge (reduce-scatter: lane l ends with sum l), then a fixed-order merge over warps
+    // warp merge: the first 32 sums by reduce-scatter (lane l ends with sum l), the rest (Sim3: 4)
+    // by butterfly; then a fixed-order merge over warps
     {
       float S[32], Cc[32];
 #pragma unroll
-      for (int i = 0; i < 21; ++i) { S[i] = hs[i]; Cc[i] = hc[i]; }
+      for (int i = 0; i < 32; ++i) {
+        const int src = i;
+        float sv = 0.f, cv = 0.f;
+        if (src < NH) { sv = hs[src]; cv = hc[src]; }
+        else if (src < NH + D) { sv = gs[src - NH]; cv = gc[src - NH]; }
+        else if (src == NH + D) { sv = es; cv = ec; }
+        S[i] = sv;
+        Cc[i] = cv;
+      }
+      constexpr int EXTRA = NS > 32 ? NS - 32 : 1;
+      float XS[EXTRA], XC[EXTRA];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) { S[21 + i] = gs[i]; Cc[21 + i] = gc[i]; }
-      S[27] = es;
-      Cc[27] = ec;
-#pragma unroll
-      for (int i = 28; i < 32; ++i) { S[i] = 0.f; Cc[i] = 0.f; }
+      for (int i = 0; i < EXTRA; ++i) {
+        const int src = 32 + i;
+        float sv = 0.f, cv = 0.f;
+        if (src < NH) { sv = hs[src]; cv = hc[src]; }
+        else if (src < NH + D) { sv = gs[src - NH]; cv = gc[src - NH]; }
+        else if (src == NH + D) { sv = es; cv = ec; }
+        XS[i] = sv;
+        XC[i] = cv;
+      }
       warp_reduce_scatter(S, Cc, lane);
+      if (NS > 32) warp_butterfly<EXTRA>(XS, XC);
       good = __reduce_add_sync(0xffffffffu, good);
       bad = __reduce_add_sync(0xffffffffu, bad);
       oob = __reduce_add_sync(0xffffffffu, oob);
-      if (lane < kSums) {
+      if (lane < NS && lane < 32) {
         ws[wid][lane] = S[0];
         wc[wid][lane] = Cc[0];
-      } else if (lane == kSums) {
+      }
+      if (NS > 32 && lane == 0) {
+#pragma unroll
+        for (int i = 0; i < EXTRA; ++i) {
+          if (32 + i < NS) {
+            ws[wid][(32 + i) % NS] = XS[i];
+            wc[wid][(32 + i) % NS] = XC[i];
+          }
+        }
+      }
+      if (lane == 31) {
         wn[wid][0] = good;
         wn[wid][1] = bad;
         wn[wid][2] = oob;
@@ -679,39 +907,39 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
     }
     __syncthreads();
     // this CTA's partial goes straight into rank 0's shared memory
-    if (tid < kSums) {
+    if (tid < NS) {
       float s = 0.f, c = 0.f;
       for (int k = 0; k < NW; ++k) kmerge(s, c, ws[k][tid], wc[k][tid]);
       CtaPart* dst = cluster.map_shared_rank(&allpart[rank], 0u);
       dst->s[tid] = s;
       dst->c[tid] = c;
-    } else if (tid < kSums + 3) {
+    } else if (tid < NS + 3) {
       int v = 0;
-      for (int k = 0; k < NW; ++k) v += wn[k][tid - kSums];
-      cluster.map_shared_rank(&allpart[rank], 0u)->cnt[tid - kSums] = v;
+      for (int k = 0; k < NW; ++k) v += wn[k][tid - NS];
+      cluster.map_shared_rank(&allpart[rank], 0u)->cnt[tid - NS] = v;
     }
     cluster.sync();
 
     if (rank == 0) {
-      if (tid < kSums) {
+      if (tid < NS) {
         float s = 0.f, c = 0.f;
         for (unsigned r = 0; r < C; ++r) kmerge(s, c, allpart[r].s[tid], allpart[r].c[tid]);
         tot[tid] = (double)s - (double)c;
-      } else if (tid < kSums + 3) {
+      } else if (tid < NS + 3) {
         int v = 0;
-        for (unsigned r = 0; r < C; ++r) v += allpart[r].cnt[tid - kSums];
-        tot[tid + 1] = (double)v;  // 29 good, 30 bad, 31 out of image
+        for (unsigned r = 0; r < C; ++r) v += allpart[r].cnt[tid - NS];
+        tot[tid + 1] = (double)v;  // NS+1 inliers, NS+2 outliers, NS+3 left the image
       }
       __syncthreads();
       if (wid == 0) {
-        if (lane == 0) tot[28] = tot[29] + tot[30];
+        if (lane == 0) tot[NS] = tot[NS + 1] + tot[NS + 2];
         __syncwarp();
-        speculate(a, lm, tot, sc, lane);
+        speculate<SIM3>(a, lm, tot, sc, lane);
         __syncwarp();
-        if (lane == 0) lm_advance(a, lm, ctl, tot, sc);
+        if (lane == 0) lm_advance<SIM3>(a, lm, ctl, tot, sc);
         __syncwarp();
         if (lm.need_exp) {
-          warp_exp_mul(lm.dx, lm.T, lm.Ttry, lane);
+          warp_exp_mul<SIM3>(lm.dx, lm.T, lm.Ttry, lane);
           __syncwarp();
           if (lane < 12) {  // publish the trial pose as float, one element per lane
             const float f = (float)lm.Ttry[lane];
@@ -734,7 +962,7 @@ __global__ void __launch_bounds__(NT, MINB) track_se3_kernel(const TrackArgs a) 
 // Host side: launch with a cluster shape.  Shapes are (threads per CTA, CTAs the register budget
 // must leave room for on one SM); the autotuner picks one together with the cluster size.
 // ------------------------------------------------------------------------------------------
-template <int NT, int MINB>
+template <int NT, int MINB, bool SIM3>
 static cudaError_t launch_nt(const TrackArgs& a, int cluster, int n_clusters, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster * n_clusters);
@@ -748,10 +976,10 @@ static cudaError_t launch_nt(const TrackArgs& a, int cluster, int n_clusters, cu
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, track_se3_kernel<NT, MINB>, a);
+  return cudaLaunchKernelEx(&cfg, track_kernel<NT, MINB, SIM3>, a);
 }
 
-template <int NT, int MINB>
+template <int NT, int MINB, bool SIM3>
 static int max_clusters_nt(int cluster) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster);
@@ -764,7 +992,7 @@ static int max_clusters_nt(int cluster) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, track_se3_kernel<NT, MINB>, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveClusters(&n, track_kernel<NT, MINB, SIM3>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -773,15 +1001,23 @@ static int max_clusters_nt(int cluster) {
 
 #define LSDG_TRACK_SHAPES(X) X(128, 4) X(128, 8) X(256, 2) X(256, 4) X(512, 1) X(512, 2)
 
-// Allows clusters of up to 16 CTAs (non-portable size) for every instantiation.  Called once
-// per context, outside any stream capture.
+// Per context, outside any stream capture: allows clusters of up to 16 CTAs (non-portable size)
+// for every instantiation and uploads the sim(3) series coefficients.
 cudaError_t track_prepare() {
   cudaError_t e = cudaSuccess;
-#define X(nt, mb) \
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(track_se3_kernel<nt, mb>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+#define X(nt, mb)                                                                                                      \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(track_kernel<nt, mb, false>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1); \
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(track_kernel<nt, mb, true>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   LSDG_TRACK_SHAPES(X)
 #undef X
-  return e;
+  double tab[11][21];
+  double fact[21];
+  fact[0] = 1.0;
+  for (int k = 1; k <= 20; ++k) fact[k] = fact[k - 1] * k;
+  for (int sh = 1; sh <= 11; ++sh)
+    for (int k = 0; k <= 20; ++k) tab[sh - 1][k] = 1.0 / (fact[k] * (double)(sh + k));
+  const cudaError_t e2 = cudaMemcpyToSymbol(c_sim3_tab, tab, sizeof(tab));
+  return e != cudaSuccess ? e : e2;
 }
 
 int track_shape_count() {
@@ -803,17 +1039,19 @@ void track_shape(int i, int* threads, int* minblocks) {
 #undef X
 }
 
-cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s) {
-#define X(nt, mb) \
-  if (threads == nt && minblocks == mb) return launch_nt<nt, mb>(a, cluster, n_clusters, s);
+cudaError_t launch_track(const TrackArgs& a, int threads, int minblocks, int cluster, int n_clusters, cudaStream_t s,
+                         bool sim3) {
+#define X(nt, mb)                                                                                            \
+  if (threads == nt && minblocks == mb)                                                                      \
+    return sim3 ? launch_nt<nt, mb, true>(a, cluster, n_clusters, s) : launch_nt<nt, mb, false>(a, cluster, n_clusters, s);
   LSDG_TRACK_SHAPES(X)
 #undef X
   return cudaErrorInvalidValue;
 }
 
-int track_max_clusters(int threads, int minblocks, int cluster) {
+int track_max_clusters(int threads, int minblocks, int cluster, bool sim3) {
 #define X(nt, mb) \
-  if (threads == nt && minblocks == mb) return max_clusters_nt<nt, mb>(cluster);
+  if (threads == nt && minblocks == mb) return sim3 ? max_clusters_nt<nt, mb, true>(cluster) : max_clusters_nt<nt, mb, false>(cluster);
   LSDG_TRACK_SHAPES(X)
 #undef X
   return 0;

@@ -68,6 +68,11 @@ def lib():
     _sig(L, "lsdg_frame_get_points", st, [_vp, _vp, C.c_int, _f32p, _f32p, C.c_int, C.POINTER(C.c_int)])
     _sig(L, "lsdg_se3_normal_equations", st, [_vp, _vp, _vp, C.c_int, _f64p, _f64p])
     _sig(L, "lsdg_track_se3", st, [_vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
+    _sig(L, "lsdg_sim3_normal_equations", st, [_vp, _vp, _vp, C.c_int, _f64p, _f64p])
+    _sig(L, "lsdg_track_sim3", st, [_vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
+    _sig(L, "lsdg_batch_create_sim3", st, [_vp, C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
+    _sig(L, "lsdg_batch_load_sim3", st, [_vp, _vp] + [_vp] * 6 + [_f64p])
+    _sig(L, "lsdg_batch_track_sim3", st, [_vp, _vp] + [_vp] * 6 + [_f64p, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_create", st, [_vp, C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
     _sig(L, "lsdg_batch_destroy", st, [_vp, _vp])
     _sig(L, "lsdg_batch_load", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p])
@@ -230,6 +235,26 @@ def se3_normal_equations(ctx: Context, reference: Frame, frame: Frame, level: in
     return out
 
 
+def _pose13(p) -> np.ndarray:
+    """A Sim3 pose as 13 doubles {R (row-major), t, s}; accepts (R|t 3x4, s) tuples or 13 values."""
+    if isinstance(p, tuple):
+        M = np.asarray(p[0], np.float64).reshape(3, 4)
+        a = np.concatenate([M[:, :3].ravel(), M[:, 3], [float(p[1])]])
+    else:
+        a = np.asarray(p, np.float64).reshape(-1)
+    a = np.ascontiguousarray(a)
+    assert a.size == 13
+    return a
+
+
+def sim3_normal_equations(ctx: Context, reference: Frame, frame: Frame, level: int, ref_to_frame) -> np.ndarray:
+    """One Sim3 residual pass at a fixed pose: the LSDG_NE_SIZE_SIM3 record (see include/lsdg.h)."""
+    out = np.zeros(T.NE_SIZE_SIM3, np.float64)
+    ctx.check(lib().lsdg_sim3_normal_equations(ctx.handle, reference.handle, frame.handle, level,
+                                               _pose13(ref_to_frame), out))
+    return out
+
+
 class SE3Tracker:
     """Upstream SE3Tracker: trackFrame(reference, frame, frameToReference_initialEstimate)."""
 
@@ -247,18 +272,42 @@ class SE3Tracker:
         return out.reshape(3, 4), st
 
 
-class Batch:
-    """Many independent trackFrame calls of mixed size in one persistent launch (graph-captured)."""
+class Sim3Tracker:
+    """Upstream Sim3Tracker: trackFrameSim3(reference, frame, frameToReference_initialEstimate).
 
-    def __init__(self, ctx: Context, widths, heights, intrs):
+    Poses are (R|t 3x4, scale) tuples; both keyframes need depth (Frame.set_depth)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.last_stats = T.TrackStats()
+
+    def trackFrameSim3(self, reference: Frame, frame: Frame, frame_to_ref_init=None):
+        init = _pose13((np.eye(3, 4), 1.0) if frame_to_ref_init is None else frame_to_ref_init)
+        out = np.zeros(13, np.float64)
+        st = T.TrackStats()
+        self.ctx.check(lib().lsdg_track_sim3(self.ctx.handle, reference.handle, frame.handle, init, out, C.byref(st)),
+                       allow=(T.OK, T.TRACKING_LOST))
+        self.last_stats = st
+        return (out[:12].reshape(3, 4), float(out[12])), st
+
+
+class Batch:
+    """Many independent trackFrame calls of mixed size in one persistent launch (graph-captured).
+
+    sim3=True makes a batch of Sim3 constraint trackings (both keyframes with depth, 13-double poses)."""
+
+    def __init__(self, ctx: Context, widths, heights, intrs, sim3: bool = False):
         self.ctx = ctx
         self.n = len(widths)
+        self.sim3 = sim3
         self.widths = np.ascontiguousarray(widths, np.int32)
         self.heights = np.ascontiguousarray(heights, np.int32)
         self._k = (T.Intrinsics * self.n)(*[intrinsics(k) for k in intrs])
         self._h = _vp()
-        ctx.check(lib().lsdg_batch_create(ctx.handle, self.n, self.widths, self.heights, self._k, C.byref(self._h)))
+        create = lib().lsdg_batch_create_sim3 if sim3 else lib().lsdg_batch_create
+        ctx.check(create(ctx.handle, self.n, self.widths, self.heights, self._k, C.byref(self._h)))
         self.npix = int(np.sum(self.widths.astype(np.int64) * self.heights))
+        self.plen = 13 if sim3 else 12
 
     @staticmethod
     def _ptr(a: np.ndarray):
@@ -274,13 +323,24 @@ class Batch:
                                              self._ptr(ref_var), self._ptr(new_images),
                                              np.ascontiguousarray(init, np.float64).reshape(-1)))
 
+    def load_sim3(self, ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var, init):
+        """Sim3 batch: init is (n, 13) {R, t, s} per pair."""
+        arrs = (ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var)
+        for a in arrs:
+            assert a.size == self.npix, (a.size, self.npix)
+        self._keep = arrs
+        self.ctx.check(lib().lsdg_batch_load_sim3(self.ctx.handle, self._h, *[self._ptr(a) for a in arrs],
+                                                  np.ascontiguousarray(init, np.float64).reshape(-1)))
+
     def run(self):
         self.ctx.check(lib().lsdg_batch_run(self.ctx.handle, self._h))
 
     def read(self):
-        out = np.zeros(12 * self.n, np.float64)
+        out = np.zeros(self.plen * self.n, np.float64)
         stats = (T.TrackStats * self.n)()
         self.ctx.check(lib().lsdg_batch_read(self.ctx.handle, self._h, out, stats))
+        if self.sim3:
+            return out.reshape(self.n, 13), stats
         return out.reshape(self.n, 3, 4), stats
 
     def track(self, ref_images, ref_idepth, ref_var, new_images, init):
@@ -387,6 +447,13 @@ def pack_pairs(pairs):
     """Concatenate synth.TrackingPair inputs into the back-to-back layout lsdg_batch_load expects."""
     cat = lambda name: np.ascontiguousarray(np.concatenate([getattr(q, name).ravel() for q in pairs]), np.float32)
     return cat("ref_image"), cat("ref_idepth"), cat("ref_idepth_var"), cat("new_image")
+
+
+def pack_sim3_pairs(pairs):
+    """Concatenate synth.Sim3Pair inputs into the layout lsdg_batch_load_sim3 expects."""
+    cat = lambda name: np.ascontiguousarray(np.concatenate([getattr(q, name).ravel() for q in pairs]), np.float32)
+    return (cat("ref_image"), cat("ref_idepth"), cat("ref_idepth_var"), cat("new_image"), cat("new_idepth"),
+            cat("new_idepth_var"))
 
 
 def declared_symbols(header: str = HEADER):

@@ -345,3 +345,44 @@ def depth_sequence(seed: int = 0, w: int = BASE_W, h: int = BASE_H, n_refs: int 
     id0 = (init_idepth * (1.0 + rng.uniform(-init_spread, init_spread, (h, w)))).astype(np.float32)
     v0 = np.full((h, w), init_var, dtype=np.float32)
     return DepthSequence(w, h, intr, key_img, 1.0 / key_depth, id0, v0, refs, poses, imn, Tn)
+
+
+@dataclasses.dataclass
+class Sim3Pair:
+    """Two keyframes with their own semi-dense inverse depth; keyframe j's map is in its own scale
+    (depths multiplied by `scale`), so the true j-to-i transform is a similarity."""
+    w: int
+    h: int
+    intr: Intrinsics
+    ref_image: np.ndarray
+    ref_idepth: np.ndarray
+    ref_idepth_var: np.ndarray
+    new_image: np.ndarray
+    new_idepth: np.ndarray
+    new_idepth_var: np.ndarray
+    frame_to_ref13: np.ndarray   # 13 doubles: R (9), t (3), s -- x_i = s R x_j + t
+
+
+def _semi_dense(rng, img, depth, scale, grad_thresh, rel_noise, var):
+    gx, gy = central_gradient(img.astype(np.float64))
+    sel = (gx * gx + gy * gy) > grad_thresh * grad_thresh
+    idepth = np.full(img.shape, -1.0)
+    idepth[sel] = (1.0 / (depth[sel] * scale)) * (1.0 + rel_noise * rng.normal(size=int(sel.sum())))
+    return idepth.astype(np.float32), np.where(sel, var, -1.0).astype(np.float32)
+
+
+def sim3_pair(seed: int = 0, w: int = BASE_W, h: int = BASE_H, scale: float = 1.3, noise_sigma: float = 2.0,
+              rel_noise: float = 0.05, idepth_var: float = 0.01) -> Sim3Pair:
+    rng = np.random.default_rng(seed)
+    intr = Intrinsics.for_size(w, h)
+    patches = make_scene(rng)
+    T = random_motion(rng)                        # frame j's camera in keyframe i (metric)
+    img0, depth0 = render(patches, intr, w, h, pose(np.eye(3), np.zeros(3)))
+    img1, depth1 = render(patches, intr, w, h, T)
+    img0 = (img0 + rng.normal(0.0, noise_sigma, img0.shape)).astype(np.float32)
+    img1 = (img1 + rng.normal(0.0, noise_sigma, img1.shape)).astype(np.float32)
+    id0, v0 = _semi_dense(rng, img0, depth0, 1.0, 5.0, rel_noise, idepth_var)
+    id1, v1 = _semi_dense(rng, img1, depth1, scale, 5.0, rel_noise, idepth_var / (scale * scale))
+    # a point of j's scaled map is x_j' = scale * x_j; x_i = R x_j + t = (1/scale) R x_j' + t
+    f2r = np.concatenate([T[:, :3].ravel(), T[:, 3], [1.0 / scale]])
+    return Sim3Pair(w, h, intr, img0, id0, v0, img1, id1, v1, f2r)

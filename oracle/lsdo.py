@@ -59,6 +59,13 @@ def lib():
             f.argtypes = [C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(T.Params), _f32p, _f32p, _f32p, C.c_int,
                           _f32p, _f64p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
             f.restype = C.c_int
+        L.lsdo_sim3_normal_equations.argtypes = [C.c_int] + [_f32p] * 6 + [C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                                                             C.POINTER(T.Params), C.c_int, _f64p, _f64p]
+        L.lsdo_sim3_normal_equations.restype = C.c_int
+        L.lsdo_track_sim3.argtypes = [C.c_int] + [_f32p] * 6 + [C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                                                C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats)]
+        L.lsdo_track_sim3.restype = C.c_int
+        L.lsdo_sim3_exp.argtypes = [_f64p, _f64p]
         L.lsdo_hardware_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -237,3 +244,43 @@ def _inv(T_):
     out[:, :3] = R.T
     out[:, 3] = -R.T @ t
     return out
+
+
+def _sim3_inputs(pair):
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    return (f(pair.ref_image), f(pair.ref_idepth), f(pair.ref_idepth_var), f(pair.new_image), f(pair.new_idepth),
+            f(pair.new_idepth_var))
+
+
+def sim3_normal_equations(pair, ref_to_frame13, level, params=None, double=False):
+    p = params or default_params()
+    out = np.zeros(T.NE_SIZE_SIM3, np.float64)
+    rc = lib().lsdo_sim3_normal_equations(int(double), *_sim3_inputs(pair), pair.w, pair.h, C.byref(_intr(pair.intr)),
+                                          C.byref(p), level, np.ascontiguousarray(ref_to_frame13, np.float64), out)
+    assert rc == 0
+    return out
+
+
+def track_sim3(pair, init13=None, params=None, double=False):
+    p = params or default_params()
+    init13 = np.concatenate([np.eye(3).ravel(), np.zeros(3), [1.0]]) if init13 is None else init13
+    out = np.zeros(13, np.float64)
+    st = T.TrackStats()
+    rc = lib().lsdo_track_sim3(int(double), *_sim3_inputs(pair), pair.w, pair.h, C.byref(_intr(pair.intr)),
+                               C.byref(p), np.ascontiguousarray(init13, np.float64), out, C.byref(st))
+    return rc, out, st
+
+
+def sim3_exp(xi):
+    out = np.zeros(12, np.float64)
+    lib().lsdo_sim3_exp(np.ascontiguousarray(xi, np.float64), out)
+    return out.reshape(3, 4)
+
+
+def sim3_error(a13, b13):
+    """(rotation angle, translation distance, |scale ratio - 1|) between two 13-double Sim3 poses."""
+    import synth
+    A = np.zeros((3, 4)); A[:, :3] = np.reshape(a13[:9], (3, 3)); A[:, 3] = a13[9:12]
+    B = np.zeros((3, 4)); B[:, :3] = np.reshape(b13[:9], (3, 3)); B[:, 3] = b13[9:12]
+    ang, dist = synth.pose_error(A, B)
+    return ang, dist, abs(a13[12] / b13[12] - 1.0)

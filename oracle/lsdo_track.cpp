@@ -165,46 +165,6 @@ void build_points(const std::vector<std::vector<T>>& I, const std::vector<std::v
 }
 
 // ------------------------------------------------------------------------------------------
-// Kahan-compensated sum (value = s - c)
-// ------------------------------------------------------------------------------------------
-template <class T>
-struct KSum {
-  T s = 0, c = 0;
-  inline void add(T x) {
-    T y = x - c;
-    T t = s + y;
-    c = (t - s) - y;
-    s = t;
-  }
-  inline void merge(const KSum& o) {  // (s,c) + (o.s,o.c) with an exact TwoSum of the heads
-    T t = s + o.s;
-    T bp = t - s;
-    T err = (s - (t - bp)) + (o.s - bp);
-    s = t;
-    c = (c + o.c) - err;
-  }
-  inline double value() const { return (double)s - (double)c; }
-};
-
-// ------------------------------------------------------------------------------------------
-// Catmull-Rom cubic (C1, interpolating): weights of taps -1, 0, 1, 2 at fraction t and their
-// derivatives.  At t = 0 the derivative weights are (-1/2, 0, 1/2, 0): the central difference.
-// ------------------------------------------------------------------------------------------
-template <class T>
-static inline void catmull_rom(T t, T w[4], T d[4]) {
-  const T t2 = t * t, t3 = t2 * t;
-  const T h = (T)0.5;
-  w[0] = h * (((T)2 * t2 - t3) - t);
-  w[1] = h * (((T)3 * t3 - (T)5 * t2) + (T)2);
-  w[2] = h * (((T)4 * t2 - (T)3 * t3) + t);
-  w[3] = h * (t3 - t2);
-  d[0] = h * (((T)4 * t - (T)3 * t2) - (T)1);
-  d[1] = h * ((T)9 * t2 - (T)10 * t);
-  d[2] = h * (((T)8 * t - (T)9 * t2) + (T)1);
-  d[3] = h * ((T)3 * t2 - (T)2 * t);
-}
-
-// ------------------------------------------------------------------------------------------
 // a3 + a4: one residual pass (calculateWarpUpdate) over [begin, end) of a level's points
 // ------------------------------------------------------------------------------------------
 template <class T>

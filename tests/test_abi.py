@@ -66,3 +66,13 @@ def test_create_without_gpu_fails_cleanly():
     rc = lsdg.lib().lsdg_create(C.byref(h), None, 0)
     assert rc in (T.CUDA_ERROR, T.NOT_SUPPORTED)
     assert not h.value
+
+
+def test_sim3_pose_packing():
+    """(R|t, s) tuples map onto the ABI's 13-double {R, t, s} layout."""
+    import lsdg
+    M = np.arange(12, dtype=np.float64).reshape(3, 4)
+    a = lsdg._pose13((M, 2.5))
+    np.testing.assert_array_equal(a[:9], M[:, :3].ravel())
+    np.testing.assert_array_equal(a[9:12], M[:, 3])
+    assert a[12] == 2.5
