@@ -126,7 +126,9 @@ typedef struct lsdg_params {
   int32_t fill_min_support; /* a hole with at least this many valid neighbours is filled */
   float fill_var_factor;    /* variance of a filled pixel = factor * neighbours' harmonic mean */
 
-  int32_t reserved[8];
+  /* inverse-depth refinement (lsdg_energy_refine) */
+  float refine_prior_weight; /* weight of the Gaussian prior (rho - rho0)^2 / var of each point; 0 = none */
+  int32_t reserved[7];
 } lsdg_params;
 
 typedef struct lsdg_track_stats {
@@ -146,6 +148,7 @@ typedef struct lsdg_ctx lsdg_ctx;
 typedef struct lsdg_frame lsdg_frame;
 typedef struct lsdg_batch lsdg_batch;
 typedef struct lsdg_depthmap lsdg_depthmap;
+typedef struct lsdg_energy lsdg_energy;
 
 /* ------------------------------------------------------------------------------------------ */
 /* Context                                                                                     */
@@ -355,6 +358,61 @@ LSDG_API lsdg_status lsdg_depth_propagate_noalloc(void* stream, int width, int h
 LSDG_API lsdg_status lsdg_depth_get(lsdg_ctx* ctx, lsdg_depthmap* dm, float* idepth, float* idepth_var,
                                     float* idepth_smoothed, float* var_smoothed, int32_t* validity,
                                     int32_t* blacklist);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Differentiable photometric energy (forward / adjoint) and inverse-depth refinement          */
+/* ------------------------------------------------------------------------------------------ */
+
+/* The energy of a keyframe level's points against a frame, as a function of the pose and of every
+ * point's inverse depth rho_i (no upstream counterpart; the residual model is the tracker's):
+ *   p_i = q_i / rho_i (q_i = ((x - cx)/fx, (y - cy)/fy, 1) from the point's pixel), p'_i = M p_i + t,
+ *   r_i = I_frame(pi(p'_i)) - I_keyframe(x_i, y_i)   (Catmull-Rom sampling of the frame level),
+ *   E   = sum_i h(r_i^2 / s_i),  h(e2) = e2 if sqrt(e2) <= huber_delta else delta (2 sqrt(e2) - delta),
+ * s_i = photometric_variance or a per-point value (lsdg_energy_set_sigma2).  A point takes part when
+ * z' > min_z and its projection lies inside border_margin.  The pose is [M | t] (ref_to_frame, M = R,
+ * or sR for dof 7) perturbed by a left increment exp(xi): the gradient with respect to xi at 0 is
+ * 2 x the sum w J^T r of lsdg_se3_normal_equations (same points, same weights).
+ *
+ * The object follows the contract of an autograd Function: lsdg_energy_forward computes E and saves
+ * what the backward needs (frame, pose, dof, the inverse depths' version); lsdg_energy_backward
+ * takes dL/dE and returns dL/dxi and dL/drho, recomputing every residual instead of storing it.
+ * Changing the inverse depths after the forward makes the backward fail (LSDG_INVALID_ARG), as a
+ * modified saved tensor does.
+ *
+ * The energy binds the keyframe's point set of `level` at creation (a copy: later set_depth calls
+ * on the keyframe do not change it); its points are those of lsdg_frame_get_points, in order. */
+LSDG_API lsdg_status lsdg_energy_create(lsdg_ctx* ctx, const lsdg_frame* keyframe, int level, lsdg_energy** out);
+LSDG_API lsdg_status lsdg_energy_destroy(lsdg_ctx* ctx, lsdg_energy* e);
+/* Number of points (the length of every per-point array below). */
+LSDG_API lsdg_status lsdg_energy_size(lsdg_ctx* ctx, const lsdg_energy* e, int* n_points);
+/* Pixel index (row-major, in the level) of every point. */
+LSDG_API lsdg_status lsdg_energy_pixels(lsdg_ctx* ctx, const lsdg_energy* e, int32_t* pixels);
+/* Host copies of the points' inverse depths (NULL restores the keyframe's). */
+LSDG_API lsdg_status lsdg_energy_set_idepth(lsdg_ctx* ctx, lsdg_energy* e, const float* idepth);
+LSDG_API lsdg_status lsdg_energy_get_idepth(lsdg_ctx* ctx, const lsdg_energy* e, float* idepth);
+/* Per-point residual variance s_i (NULL: photometric_variance for every point). */
+LSDG_API lsdg_status lsdg_energy_set_sigma2(lsdg_ctx* ctx, lsdg_energy* e, const float* sigma2);
+/* E at ref_to_frame (12 doubles) with dof 6 (SE3) or 7 (Sim3, M = sR); n_active: points taking part. */
+LSDG_API lsdg_status lsdg_energy_forward(lsdg_ctx* ctx, lsdg_energy* e, const lsdg_frame* frame,
+                                         const double ref_to_frame[12], int dof, double* energy, int* n_active);
+/* Adjoint of the last forward: grad_xi[dof] = grad_energy * dE/dxi, grad_idepth[i] (host, may be
+ * NULL) = grad_energy * dE/drho_i (0 for points that do not take part). */
+LSDG_API lsdg_status lsdg_energy_backward(lsdg_ctx* ctx, lsdg_energy* e, double grad_energy, double* grad_xi,
+                                          float* grad_idepth);
+/* Photometric inverse-depth refinement over n_frames frames at fixed poses (ref_to_frame, 12 doubles
+ * each, n_frames <= LSDG_MAX_REFS): every point independently runs `steps` damped Newton steps of its
+ * energy sum_j h(r_ij^2 / s_i) + refine_prior_weight (rho - rho0)^2 / var_i (rho0: its inverse depth
+ * at the call, var_i: the keyframe's variance), with the frames it is seen in fixed by the margin test
+ * at rho0, a trial that leaves a frame's sampling box rejected, rho clamped to
+ * [min_idepth, max_idepth] and the tracker's lambda schedule.  Every step recomputes the point's
+ * residuals in all frames; nothing is stored per residual.  The refined inverse depths replace the
+ * energy's (lsdg_energy_get_idepth); energy_before / energy_after: the summed point energies. */
+LSDG_API lsdg_status lsdg_energy_refine(lsdg_ctx* ctx, lsdg_energy* e, int n_frames, const lsdg_frame* const* frames,
+                                        const double* ref_to_frames, int steps, double* energy_before,
+                                        double* energy_after, int* n_refined);
+/* Device time (ms) of the last forward, backward and refine kernels, from CUDA events. */
+LSDG_API lsdg_status lsdg_energy_timing(lsdg_ctx* ctx, const lsdg_energy* e, float* forward_ms, float* backward_ms,
+                                        float* refine_ms);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                   */

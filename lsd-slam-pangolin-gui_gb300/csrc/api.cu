@@ -106,6 +106,7 @@ void lsdg_default_params(lsdg_params* p) {
   p->reg_min_support = 2;
   p->fill_min_support = 8;
   p->fill_var_factor = 2.0f;
+  p->refine_prior_weight = 1.0f;
 }
 
 static lsdg_status check_params(lsdg_ctx* ctx, const lsdg_params* p) {
@@ -115,6 +116,7 @@ static lsdg_status check_params(lsdg_ctx* ctx, const lsdg_params* p) {
   if (!(p->photometric_variance > 0) || !(p->huber_delta > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "variance and huber_delta must be > 0");
   if (p->reg_radius < 0 || p->reg_radius > 4) return ctx_fail(ctx, LSDG_INVALID_ARG, "reg_radius must be in 0..4");
   if (!(p->max_search_len > 0) || p->max_search_len > 1024) return ctx_fail(ctx, LSDG_INVALID_ARG, "max_search_len must be in (0, 1024]");
+  if (!(p->refine_prior_weight >= 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "refine_prior_weight must be >= 0");
   return LSDG_OK;
 }
 
@@ -229,7 +231,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
   fs.off_var0 = off;
   for (int i = 0; i < n; ++i) if (depth[i]) { o_var0[i] = off; off += (size_t)w[i] * h[i] * 4; }
   off = al256(off);
-  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], psig[kMaxLevels], psigd[kMaxLevels], blk[kMaxLevels], cnt; };
+  struct Rest { size_t plane[kMaxLevels], pyr[kMaxLevels], id[kMaxLevels], var[kMaxLevels], pxyzi[kMaxLevels], pvar[kMaxLevels], psig[kMaxLevels], psigd[kMaxLevels], ppix[kMaxLevels], blk[kMaxLevels], cnt; };
   std::vector<Rest> rest(n);
   for (int i = 0; i < n; ++i) {
     Rest& r = rest[i];
@@ -246,6 +248,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         r.pvar[l] = off; off = al256(off + pix * 4);
         r.psig[l] = off; off = al256(off + pix * 4);
         r.psigd[l] = off; off = al256(off + pix * 4);
+        if (grads) { r.ppix[l] = off; off = al256(off + pix * 4); }
         r.blk[l] = off; off = al256(off + (size_t)(h[i] >> (levels - 1)) * 4);  // one count per band
       }
     }
@@ -275,6 +278,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         F.pvar[l] = (float*)(base + r.pvar[l]);
         F.psig[l] = (float*)(base + r.psig[l]);
         F.psigd[l] = (float*)(base + r.psigd[l]);
+        F.ppix[l] = grads ? (int*)(base + r.ppix[l]) : nullptr;
         F.blk_count[l] = (int*)(base + r.blk[l]);
       }
       F.fx[l] = (float)fx; F.fy[l] = (float)fy; F.cx[l] = (float)cx; F.cy[l] = (float)cy;

@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __res
         const float Y = (((float)y - cy) * fyi) * z;
         F.pxyzi[l][pos] = make_float4(X, Y, z, F.plane[l][idx]);
         F.pvar[l][pos] = v;
+        if (F.ppix[l]) F.ppix[l][pos] = (int)idx;
       }
       pos0 += chunk_total;
       __syncthreads();  // woff / chunk_total are rewritten by the next chunk

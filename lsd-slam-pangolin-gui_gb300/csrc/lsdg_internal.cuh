@@ -9,6 +9,9 @@
 //   pvar[l]    float  [n_l]         inverse-depth variance of each point
 //   psig[l]    float  [n_l]         tracker scratch: residual variance of each point, fixed by the
 //                                   first pass of a level (0 = the point sits out the level)
+//   psigd[l]   float  [n_l]         Sim3 tracker scratch: variance of the inverse-depth residual
+//   ppix[l]    int    [n_l]         row-major pixel index of each point (single frames only; the
+//                                   photometric energy maps its points back to pixels with it)
 //   pcount[l]  int                  n_l, written on the device by the compaction
 // All per-pixel planes are row-major and 256-byte aligned.
 #pragma once
@@ -34,6 +37,7 @@ struct FrameDev {
   float* pvar[kMaxLevels];
   float* psig[kMaxLevels];
   float* psigd[kMaxLevels];      // Sim3 tracker scratch: variance of the inverse-depth residual
+  int* ppix[kMaxLevels];         // pixel index of each point, or nullptr (batch frames)
   int* pcount;                   // [kMaxLevels]
   int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per band, then offsets
   float fx[kMaxLevels], fy[kMaxLevels], cx[kMaxLevels], cy[kMaxLevels];
@@ -63,5 +67,37 @@ struct TrackArgs {
   double lambda0, lambda_up, lambda_down, step_eps, stall_eps;
   float min_good_ratio, min_usage;
 };
+
+// Kahan-compensated float sum (value = s - c) and the merge of two of them (an exact TwoSum of the
+// heads; the CPU oracle's KSum performs the same operations).
+__device__ __forceinline__ void kadd(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+__device__ __forceinline__ void kmerge(float& s, float& c, float os, float oc) {
+  const float t = s + os;
+  const float bp = t - s;
+  const float err = (s - (t - bp)) + (os - bp);
+  s = t;
+  c = (c + oc) - err;
+}
+
+// Catmull-Rom cubic (C1, interpolating): weights of taps -1, 0, 1, 2 at fraction t and their
+// derivatives; at t = 0 the derivative weights are the central difference (-1/2, 0, 1/2, 0).
+// The tracker and the photometric energy sample the frame with it (the CPU oracle spells out the
+// same operations).
+__device__ __forceinline__ void catmull_rom(float t, float w[4], float d[4]) {
+  const float t2 = t * t, t3 = t2 * t;
+  w[0] = 0.5f * ((2.f * t2 - t3) - t);
+  w[1] = 0.5f * ((3.f * t3 - 5.f * t2) + 2.f);
+  w[2] = 0.5f * ((4.f * t2 - 3.f * t3) + t);
+  w[3] = 0.5f * (t3 - t2);
+  d[0] = 0.5f * ((4.f * t - 3.f * t2) - 1.f);
+  d[1] = 0.5f * (9.f * t2 - 10.f * t);
+  d[2] = 0.5f * ((8.f * t - 9.f * t2) + 1.f);
+  d[3] = 0.5f * (3.f * t2 - 2.f * t);
+}
 
 }  // namespace lsdg

@@ -60,33 +60,6 @@ constexpr int kMaxRec = 40;
 // (filled by track_prepare).
 __constant__ double c_sim3_tab[11][21];
 
-__device__ __forceinline__ void kadd(float& s, float& c, float x) {
-  const float y = x - c;
-  const float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-__device__ __forceinline__ void kmerge(float& s, float& c, float os, float oc) {
-  const float t = s + os;
-  const float bp = t - s;
-  const float err = (s - (t - bp)) + (os - bp);
-  s = t;
-  c = (c + oc) - err;
-}
-
-// Catmull-Rom cubic (C1, interpolating): weights of taps -1, 0, 1, 2 at fraction t and their
-// derivatives; at t = 0 the derivative weights are the central difference (-1/2, 0, 1/2, 0).
-__device__ __forceinline__ void catmull_rom(float t, float w[4], float d[4]) {
-  const float t2 = t * t, t3 = t2 * t;
-  w[0] = 0.5f * ((2.f * t2 - t3) - t);
-  w[1] = 0.5f * ((3.f * t3 - 5.f * t2) + 2.f);
-  w[2] = 0.5f * ((4.f * t2 - 3.f * t3) + t);
-  w[3] = 0.5f * (t3 - t2);
-  d[0] = 0.5f * ((4.f * t - 3.f * t2) - 1.f);
-  d[1] = 0.5f * (9.f * t2 - 10.f * t);
-  d[2] = 0.5f * ((8.f * t - 9.f * t2) + 1.f);
-  d[3] = 0.5f * (3.f * t2 - 2.f * t);
-}
 
 struct Ctl {
   float R[9];

@@ -91,6 +91,18 @@ def lib():
     _sig(L, "lsdg_depth_regularize", st, [_vp, _vp])
     _sig(L, "lsdg_depth_create_keyframe", st, [_vp, _vp, _f32p, _f64p, C.c_int])
     _sig(L, "lsdg_depth_get", st, [_vp, _vp] + [C.c_void_p] * 6)
+    _sig(L, "lsdg_energy_create", st, [_vp, _vp, C.c_int, C.POINTER(_vp)])
+    _sig(L, "lsdg_energy_destroy", st, [_vp, _vp])
+    _sig(L, "lsdg_energy_size", st, [_vp, _vp, C.POINTER(C.c_int)])
+    _sig(L, "lsdg_energy_pixels", st, [_vp, _vp, _i32p])
+    _sig(L, "lsdg_energy_set_idepth", st, [_vp, _vp, _vp])
+    _sig(L, "lsdg_energy_get_idepth", st, [_vp, _vp, _f32p])
+    _sig(L, "lsdg_energy_set_sigma2", st, [_vp, _vp, _vp])
+    _sig(L, "lsdg_energy_forward", st, [_vp, _vp, _vp, _f64p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)])
+    _sig(L, "lsdg_energy_backward", st, [_vp, _vp, C.c_double, _f64p, _vp])
+    _sig(L, "lsdg_energy_refine", st, [_vp, _vp, C.c_int, _vp, _f64p, C.c_int, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int)])
+    _sig(L, "lsdg_energy_timing", st, [_vp, _vp] + [C.POINTER(C.c_float)] * 3)
     _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
     _lib = L
     return L
@@ -434,6 +446,83 @@ class DepthMap:
     def close(self):
         if self._h and self.ctx.handle:
             lib().lsdg_depth_destroy(self.ctx.handle, self._h)
+        self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PhotometricEnergy:
+    """The photometric energy of a keyframe level against a frame, as an autograd Function:
+    forward(frame, ref_to_frame, dof) -> E saves the pose and the inverse depths' version;
+    backward(grad_E) -> (dL/dxi, dL/drho) recomputes the residuals.  refine() runs the per-point
+    inverse-depth refinement over several frames."""
+
+    def __init__(self, ctx: Context, keyframe: Frame, level: int = 0):
+        self.ctx = ctx
+        self._h = _vp()
+        ctx.check(lib().lsdg_energy_create(ctx.handle, keyframe.handle, level, C.byref(self._h)))
+        n = C.c_int()
+        ctx.check(lib().lsdg_energy_size(ctx.handle, self._h, C.byref(n)))
+        self.n = n.value
+        self.dof = 6
+
+    def pixels(self) -> np.ndarray:
+        out = np.zeros(max(self.n, 1), np.int32)
+        self.ctx.check(lib().lsdg_energy_pixels(self.ctx.handle, self._h, out))
+        return out[:self.n]
+
+    def idepth(self) -> np.ndarray:
+        out = np.zeros(max(self.n, 1), np.float32)
+        self.ctx.check(lib().lsdg_energy_get_idepth(self.ctx.handle, self._h, out))
+        return out[:self.n]
+
+    def set_idepth(self, rho=None):
+        a = None if rho is None else np.ascontiguousarray(rho, np.float32)
+        if a is not None:
+            assert a.size == self.n
+        self.ctx.check(lib().lsdg_energy_set_idepth(self.ctx.handle, self._h, None if a is None else a.ctypes.data))
+
+    def set_sigma2(self, sigma2=None):
+        a = None if sigma2 is None else np.ascontiguousarray(sigma2, np.float32)
+        if a is not None:
+            assert a.size == self.n
+        self.ctx.check(lib().lsdg_energy_set_sigma2(self.ctx.handle, self._h, None if a is None else a.ctypes.data))
+
+    def forward(self, frame: Frame, ref_to_frame, dof: int = 6):
+        E, na = C.c_double(), C.c_int()
+        self.ctx.check(lib().lsdg_energy_forward(self.ctx.handle, self._h, frame.handle, _pose12(ref_to_frame), dof,
+                                                 C.byref(E), C.byref(na)))
+        self.dof = dof
+        self.n_active = na.value
+        return E.value
+
+    def backward(self, grad_energy: float = 1.0, want_idepth: bool = True):
+        gxi = np.zeros(7)
+        grho = np.zeros(max(self.n, 1), np.float32) if want_idepth else None
+        self.ctx.check(lib().lsdg_energy_backward(self.ctx.handle, self._h, float(grad_energy), gxi,
+                                                  None if grho is None else grho.ctypes.data))
+        return gxi[:self.dof], (None if grho is None else grho[:self.n])
+
+    def refine(self, frames, ref_to_frames, steps: int = 50):
+        arr = (_vp * len(frames))(*[f.handle for f in frames])
+        poses = np.ascontiguousarray(np.stack([np.asarray(T_, np.float64).reshape(3, 4) for T_ in ref_to_frames]))
+        e0, e1, nr = C.c_double(), C.c_double(), C.c_int()
+        self.ctx.check(lib().lsdg_energy_refine(self.ctx.handle, self._h, len(frames), arr, poses.ravel(), steps,
+                                                C.byref(e0), C.byref(e1), C.byref(nr)))
+        return e0.value, e1.value, nr.value
+
+    def timing(self):
+        a, b, c = C.c_float(), C.c_float(), C.c_float()
+        self.ctx.check(lib().lsdg_energy_timing(self.ctx.handle, self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().lsdg_energy_destroy(self.ctx.handle, self._h)
         self._h = _vp()
 
     def __del__(self):

@@ -65,7 +65,8 @@ class Params(C.Structure):
         ("reg_min_support", C.c_int32),
         ("fill_min_support", C.c_int32),
         ("fill_var_factor", C.c_float),
-        ("reserved", C.c_int32 * 8),
+        ("refine_prior_weight", C.c_float),
+        ("reserved", C.c_int32 * 7),
     ]
 
     def copy(self) -> "Params":

@@ -386,3 +386,33 @@ def sim3_pair(seed: int = 0, w: int = BASE_W, h: int = BASE_H, scale: float = 1.
     # a point of j's scaled map is x_j' = scale * x_j; x_i = R x_j + t = (1/scale) R x_j' + t
     f2r = np.concatenate([T[:, :3].ravel(), T[:, 3], [1.0 / scale]])
     return Sim3Pair(w, h, intr, img0, id0, v0, img1, id1, v1, f2r)
+
+
+@dataclasses.dataclass
+class RefineProblem:
+    """A keyframe with noisy semi-dense inverse depth and frames observing it from known poses."""
+    w: int
+    h: int
+    intr: Intrinsics
+    key_image: np.ndarray        # float32 [h,w]
+    key_idepth: np.ndarray       # float32 [h,w]: truth x (1 + rel_noise N(0,1)) where |grad| > thresh, else -1
+    key_idepth_var: np.ndarray   # float32 [h,w]
+    true_idepth: np.ndarray      # float64 [h,w]
+    frame_images: list           # float32 [h,w] each
+    ref_to_frame: list           # 3x4: keyframe camera -> frame camera
+
+
+def refine_problem(seed: int = 0, w: int = BASE_W, h: int = BASE_H, n_frames: int = 8, rel_noise: float = 0.05,
+                   grad_thresh: float = 5.0) -> RefineProblem:
+    """The depth_sequence scene (frames on a smooth 10 cm arc) with the keyframe depth of a tracking
+    pair: semi-dense, 5 % multiplicative noise."""
+    s = depth_sequence(seed, w, h, n_refs=n_frames)
+    rng = np.random.default_rng(seed + 7919)
+    gx, gy = central_gradient(s.key_image.astype(np.float64))
+    sel = (gx * gx + gy * gy) > grad_thresh * grad_thresh
+    idepth = np.full((h, w), -1.0)
+    idepth[sel] = s.key_true_idepth[sel] * (1.0 + rel_noise * rng.normal(size=int(sel.sum())))
+    # the keyframe's variance is that of its noise (a depth filter's estimate of it)
+    var = np.where(sel, (rel_noise * s.key_true_idepth) ** 2, -1.0)
+    return RefineProblem(w, h, s.intr, s.key_image, idepth.astype(np.float32), var.astype(np.float32),
+                         s.key_true_idepth, list(s.ref_images), [pose_inv(T) for T in s.ref_frame_to_key])

@@ -30,6 +30,7 @@ template <class T>
 struct Points {
   std::vector<T> xyzi;  // 4 per point
   std::vector<T> var;
+  std::vector<int> pix;  // row-major pixel index of each point in its level
 };
 
 template <class T>
@@ -80,6 +81,7 @@ inline void catmull_rom(T t, T w[4], T d[4]) {
 }
 
 void default_params(lsdg_params* p);
+
 void level_intrinsics(const lsdg_intrinsics& k0, int levels, LevelCam* out, int w0, int h0);
 void se3_exp(const double xi[6], double T[12]);
 void se3_mul(const double A[12], const double B[12], double C[12]);

@@ -66,6 +66,19 @@ def lib():
                                                                 C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats)]
         L.lsdo_track_sim3.restype = C.c_int
         L.lsdo_sim3_exp.argtypes = [_f64p, _f64p]
+        _vp = C.c_void_p
+        L.lsdo_energy_points.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                         C.POINTER(T.Params), C.c_int, _vp, _vp]
+        L.lsdo_energy_points.restype = C.c_int
+        L.lsdo_energy.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                  C.POINTER(T.Params), C.c_int, _f64p, C.c_int] + [_vp] * 8 + \
+                                 [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.lsdo_energy.restype = C.c_int
+        L.lsdo_energy_refine.argtypes = [C.c_int, _f32p, _f32p, _f32p, C.c_int, _f32p, C.c_int, C.c_int,
+                                         C.POINTER(T.Intrinsics), C.POINTER(T.Params), C.c_int, _f64p, C.c_int, _vp,
+                                         _f32p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_long),
+                                         C.c_int]
+        L.lsdo_energy_refine.restype = C.c_int
         L.lsdo_hardware_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -284,3 +297,66 @@ def sim3_error(a13, b13):
     B = np.zeros((3, 4)); B[:, :3] = np.reshape(b13[:9], (3, 3)); B[:, 3] = b13[9:12]
     ang, dist = synth.pose_error(A, B)
     return ang, dist, abs(a13[12] / b13[12] - 1.0)
+
+
+# ------------------------------------------------------------------------------------------
+# Differentiable photometric energy (forward / adjoint) and the inverse-depth refinement
+# ------------------------------------------------------------------------------------------
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def energy_points(key_image, key_idepth, key_var, intr, w, h, level=0, params=None):
+    """(pixel index, initial inverse depth) of every energy point of a keyframe level."""
+    p = params or default_params()
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    npx = (w >> level) * (h >> level)
+    pix = np.zeros(npx, np.int32)
+    rho0 = np.zeros(npx, np.float32)
+    n = lib().lsdo_energy_points(f(key_image), f(key_idepth), f(key_var), w, h, C.byref(_intr(intr)), C.byref(p),
+                                 level, pix.ctypes.data, rho0.ctypes.data)
+    return pix[:n].copy(), rho0[:n].copy()
+
+
+def energy(key_image, key_idepth, key_var, frame_image, intr, w, h, ref_to_frame, level=0, dof=6, rho=None,
+           sigma2=None, fixed_active=None, grad=True, params=None, double=False):
+    """E, dE/dxi (dof), dE/drho (per point), per-point energy terms, participation, broken count."""
+    p = params or default_params()
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    n = len(energy_points(key_image, key_idepth, key_var, intr, w, h, level, p)[0])
+    rho = None if rho is None else f(rho)
+    sigma2 = None if sigma2 is None else f(sigma2)
+    fixed_active = None if fixed_active is None else np.ascontiguousarray(fixed_active, np.uint8)
+    gxi = np.zeros(7) if grad else None
+    grho = np.zeros(n) if grad else None
+    ept = np.zeros(n)
+    act = np.zeros(n, np.uint8)
+    E = np.zeros(1)
+    na, nb = C.c_int(), C.c_int()
+    rc = lib().lsdo_energy(int(double), f(key_image), f(key_idepth), f(key_var), f(frame_image), w, h,
+                           C.byref(_intr(intr)), C.byref(p), level,
+                           np.ascontiguousarray(ref_to_frame, np.float64).ravel(), dof, _ptr(rho), _ptr(sigma2),
+                           _ptr(fixed_active), E.ctypes.data, _ptr(gxi), _ptr(grho), ept.ctypes.data, act.ctypes.data,
+                           C.byref(na), C.byref(nb))
+    assert rc == 0
+    return dict(E=float(E[0]), gxi=None if gxi is None else gxi[:dof], grho=grho, e_point=ept, active=act,
+                n_active=na.value, broken=nb.value)
+
+
+def energy_refine(key_image, key_idepth, key_var, frame_images, ref_to_frames, intr, w, h, level=0, steps=50,
+                  rho=None, sigma2=None, params=None, double=False, threads=None):
+    """Per-point inverse-depth refinement over the frames; returns (rho, E_before, E_after, refined)."""
+    p = params or default_params()
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    if rho is None:
+        rho = energy_points(key_image, key_idepth, key_var, intr, w, h, level, p)[1]
+    rho = f(rho).copy()
+    imgs = f(np.stack(frame_images))
+    poses = np.ascontiguousarray(np.stack([np.asarray(T_, np.float64).reshape(3, 4) for T_ in ref_to_frames]))
+    sigma2 = None if sigma2 is None else f(sigma2)
+    e0, e1, cnt = C.c_double(), C.c_double(), C.c_long()
+    rc = lib().lsdo_energy_refine(int(double), f(key_image), f(key_idepth), f(key_var), len(frame_images), imgs, w, h,
+                                  C.byref(_intr(intr)), C.byref(p), level, poses.ravel(), steps, _ptr(sigma2), rho,
+                                  C.byref(e0), C.byref(e1), C.byref(cnt), threads or hardware_threads())
+    assert rc == 0
+    return rho, e0.value, e1.value, cnt.value

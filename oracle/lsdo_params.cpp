@@ -53,6 +53,7 @@ void default_params(lsdg_params* p) {
   p->reg_min_support = 2;
   p->fill_min_support = 8;
   p->fill_var_factor = 2.0f;
+  p->refine_prior_weight = 1.0f;
 }
 
 }  // namespace lsdo

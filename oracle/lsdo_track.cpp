@@ -160,6 +160,7 @@ void build_points(const std::vector<std::vector<T>>& I, const std::vector<std::v
         P.xyzi.push_back(z);
         P.xyzi.push_back(I[l][i]);
         P.var.push_back(v);
+        P.pix.push_back((int)i);
       }
   }
 }
