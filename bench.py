@@ -38,6 +38,8 @@ UNIT = "pairs/s"
 N_PAIRS = 64
 W, H = 640, 480
 MIXED = [(320, 240)] * 20 + [(640, 480)] * 32 + [(1280, 960)] * 12
+N_SIM3 = 10        # Sim3 constraint search: a new keyframe against 10 candidate keyframes
+REFINE_STEPS = 50  # inverse-depth refinement steps over 8 observing frames
 
 
 def _gen(seed, w, h):
@@ -48,6 +50,16 @@ def _gen(seed, w, h):
 def _gen_depth(seed, w, h):
     import synth
     return synth.depth_sequence(seed, w, h)
+
+
+def _gen_refine(seed, w, h):
+    import synth
+    return synth.refine_problem(seed, w, h)
+
+
+def _gen_sim3(seed, w, h):
+    import synth
+    return synth.sim3_pair(seed, w, h)
 
 
 def gen_pairs(specs, workers):
@@ -187,8 +199,11 @@ def run_ours(args, rank, world, local_rank):
     # all host-side generation happens before the first CUDA call
     pairs = gen_pairs([(1000 * rank + i, W, H) for i in range(N_PAIRS)], workers)
     mixed = gen_pairs([(5000 + 1000 * rank + i, w, h) for i, (w, h) in enumerate(MIXED)], workers) if not args.quick else []
-    with mp.get_context("spawn").Pool(1) as pool:
-        dseq = pool.apply(_gen_depth, (7 + rank, W, H))
+    with mp.get_context("spawn").Pool(min(workers, 12)) as pool:
+        dseq_r = pool.apply_async(_gen_depth, (7 + rank, W, H))
+        rprob_r = pool.apply_async(_gen_refine, (rank, W, H))
+        sim3_r = pool.starmap_async(_gen_sim3, [(2000 + 1000 * rank + i, W, H) for i in range(N_SIM3)])
+        dseq, rprob, sim3_pairs = dseq_r.get(), rprob_r.get(), sim3_r.get()
 
     torch.cuda.set_device(local_rank)
     dist = None
@@ -329,6 +344,8 @@ def run_ours(args, rank, world, local_rank):
         mb.close()
 
     depth_res = bench_depth(ctx, stream, dseq, args)
+    energy_res = bench_energy(ctx, stream, pairs[0], rprob, args)
+    sim3_res = bench_sim3(ctx, stream, sim3_pairs, args)
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -357,12 +374,15 @@ def run_ours(args, rank, world, local_rank):
                   "batched_over_plain": value / plain_value},
         "mixed_batch": mixed_res,
         "keyframe_update": depth_res,
+        "energy": energy_res,
+        "sim3_constraint_batch": sim3_res,
         "accuracy": {"max_gt_rot_err_rad": max(e[0] for e in errs), "max_gt_trans_err_m": max(e[1] for e in errs),
                      "lost": lost},
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(pairs, args)
         depth_res["cpu_ms"], depth_res["cpu_cores"] = cpu_depth_baseline(dseq)
+        energy_res["refine_cpu_ms"], energy_res["refine_cpu_cores"] = cpu_refine_baseline(rprob)
     if rank == 0:
         print(json.dumps(result), flush=True)
     batch.close()
@@ -418,6 +438,106 @@ def bench_depth(ctx, stream, seq, args):
             "e2e_api": "lsdg_depth_update + lsdg_depth_get (reference upload, update, state read-back)",
             "create_keyframe_ms_e2e": statistics.median(prop),
             "well_observed_pixels": int(good.sum()), "median_rel_idepth_err_vs_truth": float(np.median(rel))}
+
+
+def bench_energy(ctx, stream, pair, rp, args):
+    """Photometric energy of the 640x480 tracking pair: forward and backward (adjoint w.r.t. the
+    twist and every keyframe inverse depth), then 50 steps of per-point inverse-depth refinement
+    over 8 observing frames (residuals recomputed every step).  Device times from CUDA events
+    around each kernel."""
+    import lsdg
+    import synth
+
+    T = synth.pose_inv(pair.frame_to_ref)
+    kf = lsdg.Frame(ctx, pair.w, pair.h, pair.intr).upload(pair.ref_image).set_depth(pair.ref_idepth,
+                                                                                     pair.ref_idepth_var)
+    fr = lsdg.Frame(ctx, pair.w, pair.h, pair.intr).upload(pair.new_image)
+    en = lsdg.PhotometricEnergy(ctx, kf, 0)
+    fw, bw = [], []
+    for it in range(max(3, args.warmup) + max(10, args.steps)):
+        en.forward(fr, T)
+        en.backward(1.0, want_idepth=False)
+        f_ms, b_ms, _ = en.timing()
+        if it >= max(3, args.warmup):
+            fw.append(f_ms)
+            bw.append(b_ms)
+    t0 = time.perf_counter()
+    E = en.forward(fr, T)
+    gxi, grho = en.backward(1.0)
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    n_pts = en.n
+    en.close()
+    # refinement on the 8-frame problem
+    kr = lsdg.Frame(ctx, rp.w, rp.h, rp.intr).upload(rp.key_image).set_depth(rp.key_idepth, rp.key_idepth_var)
+    frs = [lsdg.Frame(ctx, rp.w, rp.h, rp.intr).upload(im) for im in rp.frame_images]
+    er = lsdg.PhotometricEnergy(ctx, kr, 0)
+    pix = er.pixels()
+    truth = rp.true_idepth.ravel()[pix]
+    rho0 = er.idepth()
+    rf = []
+    for it in range(max(3, args.warmup) + 5):
+        er.set_idepth(None)
+        e0_, e1_, nref = er.refine(frs, rp.ref_to_frame, REFINE_STEPS)
+        rf.append(er.timing()[2])
+    rho = er.idepth()
+    er.close()
+    ref_ms = statistics.median(rf[max(3, args.warmup):])
+    evals = float(nref) * len(frs) * (REFINE_STEPS + 1)
+    # forward/backward bytes per point: ray float4 + inverse depth (+ gradient out) + 16 taps of the
+    # frame level (L2/L1 reads of a 1.2 MB plane)
+    fw_ms, bw_ms = statistics.median(fw), statistics.median(bw)
+    return {"workload": "photometric energy of the 640x480 pair (level 0, %d points): forward, backward "
+                        "(dE/dxi + %d dE/drho); refinement: %d steps x 8 frames" % (n_pts, n_pts, REFINE_STEPS),
+            "forward_ms": fw_ms, "backward_ms": bw_ms, "forward_backward_e2e_ms": e2e_ms,
+            "points": n_pts, "energy": E,
+            "algorithmic_GBps_backward": n_pts * (16 + 4 + 4 + 16 * 4) / (bw_ms / 1e3) / 1e9,
+            "refine_ms": ref_ms, "refine_points": int(nref),
+            "refine_residual_evals_per_s": evals / (ref_ms / 1e3),
+            "refine_energy_before_after": [e0_, e1_],
+            "refine_median_rel_idepth_err_vs_truth_before_after": [float(np.median(np.abs(rho0 / truth - 1))),
+                                                                   float(np.median(np.abs(rho / truth - 1)))]}
+
+
+def bench_sim3(ctx, stream, sps, args):
+    """Sim3 constraint search of one new keyframe against its candidates: one batched persistent
+    launch (graph-captured) of 10 Sim3 trackings at 640x480, both keyframes with depth."""
+    import torch
+
+    import lsdg
+
+    b = lsdg.Batch(ctx, [q.w for q in sps], [q.h for q in sps], [q.intr for q in sps], sim3=True)
+    init = np.tile(np.concatenate([np.eye(3).ravel(), np.zeros(3), [1.0]]), (len(sps), 1))
+    b.load_sim3(*lsdg.pack_sim3_pairs(sps), init)
+    b.run()
+    for _ in range(max(3, args.warmup)):
+        b.run()
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = max(10, args.steps)
+    e0.record(stream)
+    for _ in range(k):
+        b.run()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / k
+    out, stats = b.read()
+    scale_err = [abs(out[i][12] / sps[i].frame_to_ref13[12] - 1.0) for i in range(len(sps))]
+    res = {"workload": "%d Sim3 trackings 640x480 (7-dof, FP64 7x7 solve) in one launch" % len(sps),
+           "ms_per_batch": ms, "trackings_per_s": len(sps) / (ms / 1e3), "shape": b.shape(),
+           "max_gt_scale_err": float(max(scale_err)), "lost": sum(1 for s in stats if s.status != 0)}
+    b.close()
+    return res
+
+
+def cpu_refine_baseline(rp):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lsdo
+
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    lsdo.energy_refine(rp.key_image, rp.key_idepth, rp.key_idepth_var, rp.frame_images, rp.ref_to_frame, rp.intr,
+                       rp.w, rp.h, steps=REFINE_STEPS, threads=cores)
+    return (time.perf_counter() - t0) * 1e3, cores
 
 
 def cpu_depth_baseline(seq):

@@ -7,8 +7,11 @@
 //   SlamSystem::nextImage builds a Frame           -> lsdg::Frame(ctx, w, h, K).upload(img)
 //   Frame::idepth(lvl) / idepthVar(lvl)            -> Frame::depth(lvl, idepth, var)
 //   SE3Tracker::trackFrame(ref, frame, initial)    -> SE3Tracker::trackFrame(ref, frame, initial)
+//   Sim3Tracker::trackFrameSim3(ref, frame, init)  -> Sim3Tracker::trackFrameSim3(ref, frame, initial)
 //   DepthMap::updateKeyframe(referenceFrames)      -> DepthMap::updateKeyframe(images, poses)
 //   DepthMap::createKeyFrame(newKeyframe)          -> DepthMap::createKeyFrame(image, keyToNew)
+// New (no upstream counterpart): PhotometricEnergy, the energy of a keyframe against a frame with
+// the forward / backward pair of an autograd Function (SavedContext = what forward saves).
 #pragma once
 
 #include <array>
@@ -115,6 +118,114 @@ class SE3Tracker {
 
  private:
   Context& ctx_;
+};
+
+// Sim3 pose: x_b = s R x_a + t.
+struct Sim3 {
+  std::array<double, 9> R{1, 0, 0, 0, 1, 0, 0, 0, 1};
+  std::array<double, 3> t{0, 0, 0};
+  double s = 1.0;
+  std::array<double, 13> packed() const {
+    std::array<double, 13> p;
+    std::copy(R.begin(), R.end(), p.begin());
+    std::copy(t.begin(), t.end(), p.begin() + 9);
+    p[12] = s;
+    return p;
+  }
+  static Sim3 unpack(const double* p) {
+    Sim3 x;
+    std::copy(p, p + 9, x.R.begin());
+    std::copy(p + 9, p + 12, x.t.begin());
+    x.s = p[12];
+    return x;
+  }
+};
+
+class Sim3Tracker {
+ public:
+  explicit Sim3Tracker(Context& ctx) : ctx_(ctx) {}
+  // Aligns keyframe `frame` (with depth) to keyframe `reference`; returns frameToReference.
+  Sim3 trackFrameSim3(const Frame& reference, const Frame& frame, const Sim3& frameToReference_initialEstimate) {
+    const std::array<double, 13> in = frameToReference_initialEstimate.packed();
+    std::array<double, 13> out;
+    ctx_.check(lsdg_track_sim3(ctx_.get(), reference.get(), frame.get(), in.data(), out.data(), &lastStats),
+               LSDG_TRACKING_LOST);
+    return Sim3::unpack(out.data());
+  }
+  bool trackingWasGood() const { return lastStats.status == LSDG_OK; }
+  lsdg_track_stats lastStats{};
+
+ private:
+  Context& ctx_;
+};
+
+// E(xi, rho) = sum_i h(r_i^2 / s_i) of a keyframe level's points against a frame (see
+// lsdg_energy_forward).  Usage, as with an autograd Function:
+//   PhotometricEnergy::SavedContext sc(ctx, keyframe, level);
+//   double E = PhotometricEnergy::forward(sc, frame, refToFrame);
+//   PhotometricEnergy::Grad g = PhotometricEnergy::backward(sc, dLdE);
+class PhotometricEnergy {
+ public:
+  class SavedContext {
+   public:
+    SavedContext(Context& ctx, const Frame& keyframe, int level = 0) : ctx_(ctx) {
+      ctx_.check(lsdg_energy_create(ctx_.get(), keyframe.get(), level, &e_));
+      ctx_.check(lsdg_energy_size(ctx_.get(), e_, &n_));
+    }
+    ~SavedContext() {
+      if (e_) lsdg_energy_destroy(ctx_.get(), e_);
+    }
+    SavedContext(const SavedContext&) = delete;
+    SavedContext& operator=(const SavedContext&) = delete;
+    int size() const { return n_; }
+    std::vector<float> idepth() const {
+      std::vector<float> r((size_t)n_);
+      ctx_.check(lsdg_energy_get_idepth(ctx_.get(), e_, r.data()));
+      return r;
+    }
+    void setIdepth(const std::vector<float>& rho) {
+      if ((int)rho.size() != n_) throw Error(LSDG_INVALID_ARG, "one inverse depth per point");
+      ctx_.check(lsdg_energy_set_idepth(ctx_.get(), e_, rho.data()));
+    }
+    // Photometric inverse-depth refinement over frames at fixed poses (see lsdg_energy_refine).
+    void refine(const std::vector<const Frame*>& frames, const std::vector<Pose>& refToFrames, int steps = 50) {
+      if (frames.size() != refToFrames.size()) throw Error(LSDG_INVALID_ARG, "one pose per frame");
+      std::vector<const lsdg_frame*> fs;
+      std::vector<double> poses;
+      for (size_t j = 0; j < frames.size(); ++j) {
+        fs.push_back(frames[j]->get());
+        poses.insert(poses.end(), refToFrames[j].begin(), refToFrames[j].end());
+      }
+      ctx_.check(lsdg_energy_refine(ctx_.get(), e_, (int)fs.size(), fs.data(), poses.data(), steps, &energyBefore,
+                                    &energyAfter, &refined));
+    }
+    double energyBefore = 0, energyAfter = 0;
+    int refined = 0;
+    int dof = 6;
+
+   private:
+    friend class PhotometricEnergy;
+    Context& ctx_;
+    lsdg_energy* e_ = nullptr;
+    int n_ = 0;
+  };
+  struct Grad {
+    std::vector<double> xi;      // dL/dxi (6, or 7 for Sim3)
+    std::vector<float> idepth;   // dL/drho per point
+  };
+  static double forward(SavedContext& sc, const Frame& frame, const Pose& refToFrame, int dof = 6) {
+    double E = 0;
+    sc.ctx_.check(lsdg_energy_forward(sc.ctx_.get(), sc.e_, frame.get(), refToFrame.data(), dof, &E, nullptr));
+    sc.dof = dof;
+    return E;
+  }
+  static Grad backward(SavedContext& sc, double grad_output) {
+    Grad g;
+    g.xi.resize((size_t)sc.dof);
+    g.idepth.resize((size_t)sc.n_);
+    sc.ctx_.check(lsdg_energy_backward(sc.ctx_.get(), sc.e_, grad_output, g.xi.data(), g.idepth.data()));
+    return g;
+  }
 };
 
 class DepthMap {

@@ -259,6 +259,15 @@ def _pose13(p) -> np.ndarray:
     return a
 
 
+def unpack13(p):
+    """13 doubles {R (row-major), t, s} -> ([R | t] 3x4, s)."""
+    p = np.asarray(p, np.float64).reshape(-1)
+    M = np.zeros((3, 4))
+    M[:, :3] = p[:9].reshape(3, 3)
+    M[:, 3] = p[9:12]
+    return M, float(p[12])
+
+
 def sim3_normal_equations(ctx: Context, reference: Frame, frame: Frame, level: int, ref_to_frame) -> np.ndarray:
     """One Sim3 residual pass at a fixed pose: the LSDG_NE_SIZE_SIM3 record (see include/lsdg.h)."""
     out = np.zeros(T.NE_SIZE_SIM3, np.float64)
@@ -300,7 +309,7 @@ class Sim3Tracker:
         self.ctx.check(lib().lsdg_track_sim3(self.ctx.handle, reference.handle, frame.handle, init, out, C.byref(st)),
                        allow=(T.OK, T.TRACKING_LOST))
         self.last_stats = st
-        return (out[:12].reshape(3, 4), float(out[12])), st
+        return unpack13(out), st
 
 
 class Batch:

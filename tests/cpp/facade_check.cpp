@@ -1,6 +1,6 @@
 // Exercises the C++ facade (include/lsdg/lsdg.hpp) the way SlamSystem's threads would: a tracking
 // thread aligning a frame to a keyframe, a mapping thread updating and propagating the keyframe's
-// depth.  Input planes are raw float32 files written by the Python test; prints one line of results.
+// depth, the photometric energy's forward / backward, and a constraint-search Sim3 tracking.  Input planes are raw float32 files written by the Python test; prints one line of results.
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -47,6 +47,28 @@ int main(int argc, char** argv) {
     size_t valid = 0;
     for (float x : d) valid += x > 0;
     std::printf("depth_valid %zu\n", valid);
+    // differentiable energy at the tracked pose: forward / backward as an autograd Function
+    lsdg::PhotometricEnergy::SavedContext sc(ctx, kf, 0);
+    const double E = lsdg::PhotometricEnergy::forward(sc, fr, lsdg::inverse(T));
+    const lsdg::PhotometricEnergy::Grad g = lsdg::PhotometricEnergy::backward(sc, 1.0);
+    size_t nz = 0;
+    for (float x : g.idepth) nz += x != 0.f;
+    std::printf("energy %.17g", E);
+    for (double v : g.xi) std::printf(" %.17g", v);
+    std::printf(" points %d nonzero %zu\n", sc.size(), nz);
+    // Sim3 constraint tracking between two keyframes with depth
+    auto sk = load((dir + "/s_key.f32").c_str(), n), skd = load((dir + "/s_kid.f32").c_str(), n),
+         skv = load((dir + "/s_kvar.f32").c_str(), n), sn = load((dir + "/s_new.f32").c_str(), n),
+         snd = load((dir + "/s_nid.f32").c_str(), n), snv = load((dir + "/s_nvar.f32").c_str(), n);
+    lsdg::Frame ki(ctx, w, h, K), kj(ctx, w, h, K);
+    ki.upload(sk.data()).setDepth(skd.data(), skv.data());
+    kj.upload(sn.data()).setDepth(snd.data(), snv.data());
+    lsdg::Sim3Tracker st(ctx);
+    const lsdg::Sim3 S = st.trackFrameSim3(ki, kj, lsdg::Sim3{});
+    const auto sp = S.packed();
+    std::printf("sim3");
+    for (double v : sp) std::printf(" %.17g", v);
+    std::printf(" good %d\n", st.trackingWasGood() ? 1 : 0);
   } catch (const lsdg::Error& e) {
     std::printf("error %d %s\n", (int)e.status, e.what());
     return 1;

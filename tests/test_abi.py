@@ -76,3 +76,11 @@ def test_sim3_pose_packing():
     np.testing.assert_array_equal(a[:9], M[:, :3].ravel())
     np.testing.assert_array_equal(a[9:12], M[:, 3])
     assert a[12] == 2.5
+
+
+def test_sim3_pose_unpacking_inverts_packing():
+    import lsdg
+    M = np.arange(12, dtype=np.float64).reshape(3, 4)
+    M2, s = lsdg.unpack13(lsdg._pose13((M, 1.7)))
+    np.testing.assert_array_equal(M2, M)
+    assert s == 1.7

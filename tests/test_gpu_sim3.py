@@ -81,7 +81,7 @@ def test_track_sim3_matches_fp64_oracle(ctx, seed):
     assert st.status == 0
     rc, o, ost = lsdo.track_sim3(sp, double=True)
     assert rc == 0
-    got = np.concatenate([Tg.ravel(), [sg]])
+    got = lsdg._pose13((Tg, sg))
     ang, dist, ds = lsdo.sim3_error(got, o)
     assert ang < 1e-4 and dist < 1e-4 and ds < 1e-4, (ang, dist, ds)
     # and both recover the synthetic similarity to the accuracy the 5 % depth noise allows
@@ -97,7 +97,7 @@ def test_track_sim3_from_truth_stays(ctx):
         [np.reshape(sp.frame_to_ref13[:9], (3, 3)), np.reshape(sp.frame_to_ref13[9:12], (3, 1))], 1),
         sp.frame_to_ref13[12]))
     rc, o, _ = lsdo.track_sim3(sp, init13=sp.frame_to_ref13, double=True)
-    ang, dist, ds = lsdo.sim3_error(np.concatenate([Tg.ravel(), [sg]]), o)
+    ang, dist, ds = lsdo.sim3_error(lsdg._pose13((Tg, sg)), o)
     assert ang < 1e-4 and dist < 1e-4 and ds < 1e-4, (ang, dist, ds)
 
 
