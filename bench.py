@@ -619,6 +619,35 @@ def run_reference(args, rank, world):
     print(json.dumps(res), flush=True)
 
 
+def run_profile_energy(args):
+    """Lean driver for ncu: the 640x480 pair's energy forward + backward and the 8-frame refinement,
+    W + K times each."""
+    import lsdg
+    import synth
+
+    with mp.get_context("spawn").Pool(2) as pool:
+        pr = pool.apply_async(_gen, (0, W, H))
+        rr = pool.apply_async(_gen_refine, (0, W, H))
+        pair, rp = pr.get(), rr.get()
+    ctx = lsdg.Context()
+    T = synth.pose_inv(pair.frame_to_ref)
+    kf = lsdg.Frame(ctx, W, H, pair.intr).upload(pair.ref_image).set_depth(pair.ref_idepth, pair.ref_idepth_var)
+    fr = lsdg.Frame(ctx, W, H, pair.intr).upload(pair.new_image)
+    en = lsdg.PhotometricEnergy(ctx, kf, 0)
+    kr = lsdg.Frame(ctx, W, H, rp.intr).upload(rp.key_image).set_depth(rp.key_idepth, rp.key_idepth_var)
+    frs = [lsdg.Frame(ctx, W, H, rp.intr).upload(im) for im in rp.frame_images]
+    er = lsdg.PhotometricEnergy(ctx, kr, 0)
+    for _ in range(args.warmup + args.steps):
+        en.forward(fr, T)
+        en.backward(1.0, want_idepth=False)
+        er.set_idepth(None)
+        er.refine(frs, rp.ref_to_frame, REFINE_STEPS)
+    print(json.dumps({"profile_energy": True, "points": en.n, "timing_ms": en.timing()[:2] + er.timing()[2:]}))
+    en.close()
+    er.close()
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -630,12 +659,15 @@ def main():
     ap.add_argument("--profile", action="store_true", help="lean run for ncu captures")
     ap.add_argument("--pairs", type=int, default=16, help="pairs in the --profile batch")
     ap.add_argument("--profile-depth", action="store_true", help="lean depth-update run for ncu captures")
+    ap.add_argument("--profile-energy", action="store_true", help="lean energy / refinement run for ncu captures")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.profile_depth:
+    if args.profile_energy:
+        run_profile_energy(args)
+    elif args.profile_depth:
         run_profile_depth(args)
     elif args.profile:
         run_profile(args)
