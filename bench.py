@@ -31,6 +31,8 @@ PKG = os.path.join(ROOT, "lsd-slam-pangolin-gui_gb300")
 if PKG not in sys.path:
     sys.path.insert(0, PKG)
 
+import shard  # noqa: E402  (pair partition and the host-side collectives)
+
 import numpy as np  # noqa: E402
 
 METRIC = "tracked frame pairs/s @640x480"
@@ -198,7 +200,9 @@ def run_ours(args, rank, world, local_rank):
     workers = os.cpu_count() or 8
     # all host-side generation happens before the first CUDA call
     pairs = gen_pairs([(1000 * rank + i, W, H) for i in range(N_PAIRS)], workers)
-    mixed = gen_pairs([(5000 + 1000 * rank + i, w, h) for i, (w, h) in enumerate(MIXED)], workers) if not args.quick else []
+    # the mixed batch is one fixed set of 64 pairs partitioned across the ranks (shard.partition)
+    mixed_idx = shard.my_share([shard.pair_cost(w, h) for w, h in MIXED], rank, world)
+    mixed = gen_pairs([(5000 + i, MIXED[i][0], MIXED[i][1]) for i in mixed_idx], workers) if not args.quick else []
     with mp.get_context("spawn").Pool(min(workers, 12)) as pool:
         dseq_r = pool.apply_async(_gen_depth, (7 + rank, W, H))
         rprob_r = pool.apply_async(_gen_refine, (rank, W, H))
@@ -232,11 +236,7 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return shard.max_over_ranks(x, dist, device="cuda")
 
     clocks = Clocks(local_rank)
     clocks.start()
@@ -336,11 +336,13 @@ def run_ours(args, rank, world, local_rank):
         me1.record(stream)
         me1.synchronize()
         mo, ms_ = mb.read()
-        m_ms = me0.elapsed_time(me1) / k_mixed
-        merr = [synth.pose_error(mo[i], mixed[i].frame_to_ref) for i in range(len(mixed))]
-        mixed_res = {"pairs": len(mixed), "ms_per_batch": m_ms, "pairs_per_s": len(mixed) / (m_ms / 1e3),
-                     "shape": mb.shape(), "max_gt_rot_err_rad": max(e[0] for e in merr),
-                     "lost": sum(1 for s in ms_ if s.status != 0)}
+        m_ms = max_over_ranks(me0.elapsed_time(me1) / k_mixed)
+        merr = np.array([synth.pose_error(mo[i], mixed[i].frame_to_ref) for i in range(len(mixed))])
+        merr = shard.gather_rows(mixed_idx, merr, len(MIXED), dist)
+        mlost = shard.gather_rows(mixed_idx, np.array([s.status != 0 for s in ms_], np.int64), len(MIXED), dist)
+        mixed_res = {"pairs": len(MIXED), "ms_per_batch": m_ms, "pairs_per_s": len(MIXED) / (m_ms / 1e3),
+                     "pairs_this_rank": len(mixed), "shape": mb.shape(), "max_gt_rot_err_rad": float(merr[:, 0].max()),
+                     "lost": int(mlost.sum()), "scaling": "strong (one 64-pair set split across ranks)"}
         mb.close()
 
     depth_res = bench_depth(ctx, stream, dseq, args)
@@ -376,8 +378,9 @@ def run_ours(args, rank, world, local_rank):
         "keyframe_update": depth_res,
         "energy": energy_res,
         "sim3_constraint_batch": sim3_res,
-        "accuracy": {"max_gt_rot_err_rad": max(e[0] for e in errs), "max_gt_trans_err_m": max(e[1] for e in errs),
-                     "lost": lost},
+        "accuracy": {"max_gt_rot_err_rad": max_over_ranks(max(e[0] for e in errs)),
+                     "max_gt_trans_err_m": max_over_ranks(max(e[1] for e in errs)),
+                     "lost": int(shard.sum_over_ranks(lost, dist, device="cuda")), "pairs": N_PAIRS * world},
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(pairs, args)
@@ -662,9 +665,7 @@ def main():
     ap.add_argument("--profile-energy", action="store_true", help="lean energy / refinement run for ncu captures")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    rank, world, local_rank = shard.rank_env()
     if args.profile_energy:
         run_profile_energy(args)
     elif args.profile_depth:
