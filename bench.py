@@ -435,12 +435,25 @@ def bench_depth(ctx, stream, seq, args):
             prop.append((time.perf_counter() - t0) * 1e3)
     good = (st["validity"] > 0) & (st["var"] < 0.01)
     rel = np.abs(st["idepth"][good] - seq.key_true_idepth[good]) / seq.key_true_idepth[good]
+    # the viewer's point cloud of the new keyframe (Keyframe::computeVbo), into a device buffer
+    vbuf = torch.empty(seq.w * seq.h * 4, dtype=torch.float32, device="cuda")
+    cl = []
+    for it in range(max(3, args.warmup) + 10):
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        n_vertices = dm.cloud_to_device(vbuf.data_ptr())
+        c1.record(stream)
+        c1.synchronize()
+        if it >= max(3, args.warmup):
+            cl.append(c0.elapsed_time(c1))
     dm.close()
     return {"workload": "updateKeyframe: 1 keyframe 640x480, 8 references on a 10 cm arc, observe + regularize",
             "ms_device": statistics.median(dev), "ms_e2e": statistics.median(e2e),
             "e2e_api": "lsdg_depth_update + lsdg_depth_get (reference upload, update, state read-back)",
             "create_keyframe_ms_e2e": statistics.median(prop),
-            "well_observed_pixels": int(good.sum()), "median_rel_idepth_err_vs_truth": float(np.median(rel))}
+            "well_observed_pixels": int(good.sum()), "median_rel_idepth_err_vs_truth": float(np.median(rel)),
+            "cloud_ms": statistics.median(cl), "cloud_vertices": int(n_vertices),
+            "cloud_api": "lsdg_cloud_from_depthmap (Keyframe::computeVbo into a device buffer; call incl. count read-back)"}
 
 
 def bench_energy(ctx, stream, pair, rp, args):

@@ -150,6 +150,29 @@ typedef struct lsdg_batch lsdg_batch;
 typedef struct lsdg_depthmap lsdg_depthmap;
 typedef struct lsdg_energy lsdg_energy;
 
+/* Wire formats of the viewer path, byte-compatible with the reference's structs:
+ * InputPointDense (lib/Pangolin_IOWrapper/Keyframe.h:16-21): what publishKeyframe copies per pixel,
+ * Keyframe::MyVertex (Keyframe.h:50-54): one point of the keyframe's cloud, colour stored B, G, R, A. */
+typedef struct lsdg_input_point_dense {
+  float idepth;
+  float idepth_var;
+  uint8_t color[4];
+} lsdg_input_point_dense;
+
+typedef struct lsdg_cloud_vertex {
+  float point[3];
+  uint8_t color[4];
+} lsdg_cloud_vertex;
+
+/* Keyframe::computeVbo's filter constants (Keyframe.h:78-82); lsdg_cloud_default_params gives
+ * scaled_th 1e-3, abs_th 1e-1, min_near_support 9 (the sparsify factor is 1 there: no sampling). */
+typedef struct lsdg_cloud_params {
+  float scaled_th;        /* drop a point when idepth_var * depth^4 > scaled_th */
+  float abs_th;           /* ... or when idepth_var * depth^4 * scale^2 > abs_th */
+  int32_t min_near_support; /* 3x3 neighbours (centre included) within sqrt(2 var) of its idepth */
+  int32_t reserved;
+} lsdg_cloud_params;
+
 /* ------------------------------------------------------------------------------------------ */
 /* Context                                                                                     */
 /* ------------------------------------------------------------------------------------------ */
@@ -413,6 +436,35 @@ LSDG_API lsdg_status lsdg_energy_refine(lsdg_ctx* ctx, lsdg_energy* e, int n_fra
 /* Device time (ms) of the last forward, backward and refine kernels, from CUDA events. */
 LSDG_API lsdg_status lsdg_energy_timing(lsdg_ctx* ctx, const lsdg_energy* e, float* forward_ms, float* backward_ms,
                                         float* refine_ms);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Keyframe point cloud (the viewer's data path, headless)                                      */
+/* ------------------------------------------------------------------------------------------ */
+
+LSDG_API void lsdg_cloud_default_params(lsdg_cloud_params* p);
+
+/* PangolinOutputIOWrapper::publishKeyframe's per-pixel copy
+ * (lib/Pangolin_IOWrapper/PangolinOutputIOWrapper.cpp:79-89) of the depth map's keyframe:
+ * {idepth, idepth_var} = the smoothed state (what Frame::idepth(0) / idepthVar(0) hold), every colour
+ * byte = the keyframe intensity converted to uint8 (truncated; values outside [0, 255] saturate).
+ * out: host array of w * h. */
+LSDG_API lsdg_status lsdg_depth_export_points(lsdg_ctx* ctx, lsdg_depthmap* dm, lsdg_input_point_dense* out);
+
+/* Keyframe::computeVbo (lib/Pangolin_IOWrapper/Keyframe.h:66-143) without OpenGL: the points of a
+ * w x h InputPointDense array (host) that pass the variance and neighbour-support filter,
+ * back-projected with (fx, fy, cx, cy) and the keyframe's Sim3 scale, in row-major order into `out`
+ * (host, capacity w * h vertices); *count = the number of vertices (Keyframe::points). */
+LSDG_API lsdg_status lsdg_cloud_build(lsdg_ctx* ctx, int w, int h, float fx, float fy, float cx, float cy,
+                                      float scale, const lsdg_cloud_params* params,
+                                      const lsdg_input_point_dense* points, lsdg_cloud_vertex* out,
+                                      int* count);
+
+/* The same from the depth map's keyframe straight into a caller-owned DEVICE buffer (the VBO the
+ * GL viewer would upload, kept on the GPU): export + filter + back-projection on the device, only the
+ * count comes back.  out_device: capacity w * h vertices. */
+LSDG_API lsdg_status lsdg_cloud_from_depthmap(lsdg_ctx* ctx, lsdg_depthmap* dm, float scale,
+                                              const lsdg_cloud_params* params, lsdg_cloud_vertex* out_device,
+                                              int* count);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                   */

@@ -462,6 +462,18 @@ struct lsdg_depthmap {
   bool has_key = false;
 };
 
+bool depth_key_planes(const lsdg_depthmap* dm, const float** idepth, const float** var, const float** image,
+                      int* w, int* h, lsdg_intrinsics* K) {
+  if (!dm || !dm->has_key) return false;
+  *K = dm->intr;
+  *idepth = dm->cur.sm;
+  *var = dm->cur.vsm;
+  *image = dm->key.h_frames[0].plane[0];
+  *w = dm->w;
+  *h = dm->h;
+  return true;
+}
+
 static DepthPlanes carve_planes(char*& p, size_t n) {
   DepthPlanes s;
   s.d = (float*)p; p += n * 4;

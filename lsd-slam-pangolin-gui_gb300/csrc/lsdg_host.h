@@ -54,6 +54,11 @@ struct lsdg_frame {
 };
 
 lsdg_status ctx_fail(lsdg_ctx* ctx, lsdg_status st, const char* fmt, ...);
+
+// The depth map's current keyframe as the viewer reads it (depth.cu): smoothed inverse depth and
+// variance, keyframe intensity (device planes, row-major w x h).  False when no keyframe is set.
+bool depth_key_planes(const lsdg_depthmap* dm, const float** idepth, const float** var, const float** image,
+                      int* w, int* h, lsdg_intrinsics* K);
 lsdg_status ctx_cuda(lsdg_ctx* ctx, cudaError_t e, const char* what);
 lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, const int* h, const lsdg_intrinsics* intr,
                            const bool* depth, int levels, bool grads);

@@ -103,6 +103,11 @@ def lib():
     _sig(L, "lsdg_energy_refine", st, [_vp, _vp, C.c_int, _vp, _f64p, C.c_int, C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.POINTER(C.c_int)])
     _sig(L, "lsdg_energy_timing", st, [_vp, _vp] + [C.POINTER(C.c_float)] * 3)
+    _sig(L, "lsdg_cloud_default_params", None, [C.POINTER(T.CloudParams)])
+    _sig(L, "lsdg_depth_export_points", st, [_vp, _vp, _vp])
+    _sig(L, "lsdg_cloud_build", st, [_vp, C.c_int, C.c_int] + [C.c_float] * 5 + [C.POINTER(T.CloudParams), _vp, _vp,
+                                                                                 C.POINTER(C.c_int)])
+    _sig(L, "lsdg_cloud_from_depthmap", st, [_vp, _vp, C.c_float, C.POINTER(T.CloudParams), _vp, C.POINTER(C.c_int)])
     _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
     _lib = L
     return L
@@ -440,6 +445,21 @@ class DepthMap:
     def regularize(self):
         self.ctx.check(lib().lsdg_depth_regularize(self.ctx.handle, self._h))
 
+    def export_points(self):
+        """publishKeyframe's InputPointDense array (h, w) of the current keyframe."""
+        out = np.zeros(self.w * self.h, POINT_DENSE)
+        self.ctx.check(lib().lsdg_depth_export_points(self.ctx.handle, self._h, out.ctypes.data))
+        return out.reshape(self.h, self.w)
+
+    def cloud_to_device(self, device_ptr: int, scale: float = 1.0, params=None) -> int:
+        """Keyframe::computeVbo of the current keyframe into a device buffer (w * h vertices of
+        16 bytes, 16-byte aligned); returns the vertex count."""
+        n = C.c_int()
+        self.ctx.check(lib().lsdg_cloud_from_depthmap(self.ctx.handle, self._h, scale,
+                                                      None if params is None else C.byref(params),
+                                                      C.c_void_p(device_ptr), C.byref(n)))
+        return n.value
+
     def createKeyFrame(self, new_image, key_to_new, regularize=True):
         self.ctx.check(lib().lsdg_depth_create_keyframe(self.ctx.handle, self._h, np.ascontiguousarray(new_image, np.float32),
                                                         _pose12(key_to_new), int(regularize)))
@@ -539,6 +559,29 @@ class PhotometricEnergy:
             self.close()
         except Exception:
             pass
+
+
+POINT_DENSE = np.dtype([("idepth", "<f4"), ("idepth_var", "<f4"), ("color", "u1", (4,))])  # InputPointDense
+CLOUD_VERTEX = np.dtype([("point", "<f4", (3,)), ("color", "u1", (4,))])                     # Keyframe::MyVertex
+
+
+def cloud_default_params() -> T.CloudParams:
+    p = T.CloudParams()
+    lib().lsdg_cloud_default_params(C.byref(p))
+    return p
+
+
+def cloud_build(ctx: Context, points, w: int, h: int, fx, fy, cx, cy, scale: float = 1.0, params=None):
+    """Keyframe::computeVbo on the GPU: vertices (structured CLOUD_VERTEX array) of a w x h
+    InputPointDense array."""
+    pts = np.ascontiguousarray(points, POINT_DENSE).reshape(-1)
+    assert pts.size == w * h
+    out = np.zeros(w * h, CLOUD_VERTEX)
+    n = C.c_int()
+    ctx.check(lib().lsdg_cloud_build(ctx.handle, w, h, fx, fy, cx, cy, scale,
+                                     None if params is None else C.byref(params), pts.ctypes.data, out.ctypes.data,
+                                     C.byref(n)))
+    return out[:n.value].copy()
 
 
 def pack_pairs(pairs):

@@ -104,3 +104,9 @@ class TrackStats(C.Structure):
             "good_ratio": self.good_ratio,
             "usage": self.usage,
         }
+
+
+class CloudParams(C.Structure):
+    """lsdg_cloud_params (include/lsdg.h)."""
+    _fields_ = [("scaled_th", C.c_float), ("abs_th", C.c_float), ("min_near_support", C.c_int32),
+                ("reserved", C.c_int32)]

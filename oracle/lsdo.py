@@ -79,6 +79,9 @@ def lib():
                                          _f32p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_long),
                                          C.c_int]
         L.lsdo_energy_refine.restype = C.c_int
+        L.lsdo_cloud_build.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                       _vp, _vp, _vp]
+        L.lsdo_cloud_build.restype = C.c_int
         L.lsdo_hardware_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -360,3 +363,20 @@ def energy_refine(key_image, key_idepth, key_var, frame_images, ref_to_frames, i
                                   C.byref(e0), C.byref(e1), C.byref(cnt), threads or hardware_threads())
     assert rc == 0
     return rho, e0.value, e1.value, cnt.value
+
+
+# ------------------------------------------------------------------------------------------
+# Keyframe point cloud (Keyframe::computeVbo)
+# ------------------------------------------------------------------------------------------
+POINT_DENSE = np.dtype([("idepth", "<f4"), ("idepth_var", "<f4"), ("color", "u1", (4,))])
+CLOUD_VERTEX = np.dtype([("point", "<f4", (3,)), ("color", "u1", (4,))])
+
+
+def cloud_build(points, w, h, fx, fy, cx, cy, scale=1.0, scaled_th=1e-3, abs_th=1e-1, min_near_support=9):
+    """Vertices (structured array) of a w x h InputPointDense array (structured, POINT_DENSE)."""
+    pts = np.ascontiguousarray(points, POINT_DENSE).reshape(-1)
+    assert pts.size == w * h
+    out = np.zeros(w * h, CLOUD_VERTEX)
+    p = T.CloudParams(scaled_th, abs_th, min_near_support, 0)
+    n = lib().lsdo_cloud_build(w, h, fx, fy, cx, cy, scale, C.addressof(p), pts.ctypes.data, out.ctypes.data)
+    return out[:n].copy()
