@@ -285,6 +285,23 @@ LSDG_API lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* batch);
 /* Device -> host results (synchronises the context stream). */
 LSDG_API lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* batch, double* frame_to_ref_out,
                             lsdg_track_stats* stats);
+/* Pipelined form: lsdg_batch_submit_* enqueues one step (the upload of its inputs on the batch's
+ * copy stream into whichever of the batch's two input slots the previous step is not using, the
+ * step's graph behind the upload, the read-back of its poses and stats behind the graph) and
+ * returns; lsdg_batch_collect waits for the oldest submitted step and copies its results out.  At
+ * most two steps are in flight (a third submit fails with LSDG_INVALID_ARG); results come back in
+ * submission order.  For the copies to overlap the tracking, the host arrays must be pinned
+ * (page-locked) and stay untouched until the step is collected.  The synchronous calls
+ * (load / run / read / track) refuse while steps are in flight. */
+LSDG_API lsdg_status lsdg_batch_submit_se3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
+                                           const float* ref_idepth, const float* ref_idepth_var,
+                                           const float* new_images, const double* frame_to_ref_init);
+LSDG_API lsdg_status lsdg_batch_submit_sim3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
+                                            const float* ref_idepth, const float* ref_idepth_var,
+                                            const float* new_images, const float* new_idepth,
+                                            const float* new_idepth_var, const double* frame_to_ref_init);
+LSDG_API lsdg_status lsdg_batch_collect(lsdg_ctx* ctx, lsdg_batch* batch, double* frame_to_ref_out,
+                                        lsdg_track_stats* stats);
 /* A batch of Sim3 constraint trackings (a new keyframe against its candidates): both keyframes of
  * every pair carry depth; poses are 13 doubles.  lsdg_batch_run and lsdg_batch_read work on it as on
  * an SE3 batch. */

@@ -1,12 +1,17 @@
 // batch.cu -- batched alignment of many independent frame pairs of mixed size (a11).
 //
-// A batch owns one arena with 2n frames: frames 0..n-1 are the keyframes (with depth), n..2n-1 the
-// frames to track.  The level-0 inputs of all pairs sit back to back per kind, so a batch upload is
-// four host->device copies.  lsdg_batch_run is one CUDA graph: image pyramids of all 2n frames,
-// depth pyramids + point compaction of the keyframes, then ONE persistent cluster launch that runs
-// every pair's full coarse-to-fine LM loop on the device (pairs taken largest first from an atomic
-// queue).  The graph is captured after the autotuner has picked the (threads, cluster) shape for
-// the batch's size mix, and it is recaptured when the parameters change.
+// A batch slot owns one arena with 2n frames: frames 0..n-1 are the keyframes (with depth), n..2n-1
+// the frames to track.  The level-0 inputs of all pairs sit back to back per kind, so a batch upload
+// is four host->device copies.  A run is one CUDA graph: image pyramids of all 2n frames, depth
+// pyramids + point compaction of the keyframes, then ONE persistent cluster launch that runs every
+// pair's full coarse-to-fine LM loop on the device (pairs taken largest first from an atomic queue).
+// The graph is captured after the autotuner has picked the (threads, cluster) shape for the batch's
+// size mix, and it is recaptured when the parameters change.
+//
+// Two slots make the pipelined form (lsdg_batch_submit_* / lsdg_batch_collect): step k+1's inputs
+// are uploaded into the other slot on a copy stream while step k's graph runs, and each step's
+// poses come back on the context stream behind its graph, so the host<->device copies overlap the
+// tracking.  The synchronous calls (load / run / read / track) use slot 0.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -32,68 +37,216 @@ int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cu
     if (_s != LSDG_OK) return _s;                             \
   } while (0)
 
-struct lsdg_batch {
-  int n = 0;
-  bool sim3 = false;  // Sim3 constraint tracking: both keyframes of a pair carry depth
-  int pose_len = 12;  // doubles per pose: 12 (SE3) or 13 (Sim3: R, t, s)
+namespace {
+
+struct BatchSlot {
+  bool ready = false;  // allocated
   FrameSet fs;
   PairDev* d_pairs = nullptr;
-  int* d_order = nullptr;
   double* d_init = nullptr;
   double* d_out = nullptr;
   lsdg_track_stats* d_stats = nullptr;
   int* d_work = nullptr;
-  double* h_out = nullptr;
+  double* h_out = nullptr;            // pinned staging of the results
   lsdg_track_stats* h_stats = nullptr;
-  int* h_counts = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_epoch = -1;
-  int launches_per_run = 0;
-  TuneChoice tc;
-  std::string key;
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // run start, build done, track done
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // run start, build done, track done (timing)
+  cudaEvent_t copied = nullptr;       // inputs are in the arena (copy stream)
+  cudaEvent_t done = nullptr;         // graph + result read-back finished (context stream)
   bool ran = false;
 };
 
-static void batch_free(lsdg_batch* b) {
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  frameset_free(b->fs);
-  if (b->d_pairs) cudaFree(b->d_pairs);
-  if (b->d_order) cudaFree(b->d_order);
-  if (b->d_init) cudaFree(b->d_init);
-  if (b->d_out) cudaFree(b->d_out);
-  if (b->d_stats) cudaFree(b->d_stats);
-  if (b->d_work) cudaFree(b->d_work);
-  if (b->h_out) cudaFreeHost(b->h_out);
-  if (b->h_stats) cudaFreeHost(b->h_stats);
-  if (b->h_counts) cudaFreeHost(b->h_counts);
-  for (auto& e : b->ev)
+}  // namespace
+
+struct lsdg_batch {
+  int n = 0;
+  bool sim3 = false;  // Sim3 constraint tracking: both keyframes of a pair carry depth
+  int pose_len = 12;  // doubles per pose: 12 (SE3) or 13 (Sim3: R, t, s)
+  std::vector<int> w, h;
+  std::vector<lsdg_intrinsics> intr;
+  BatchSlot slot[2];
+  int last = 0;                 // slot of the last run (timing / work)
+  int* d_order = nullptr;
+  int* h_counts = nullptr;
+  cudaStream_t copy = nullptr;  // upload stream of the pipelined form
+  int inflight[2] = {-1, -1};   // slots of the submitted, not yet collected steps (oldest first)
+  int n_inflight = 0;
+  int next = 0;                 // slot of the next submit
+  int launches_per_run = 0;
+  int tune_epoch = -1;          // params epoch the shape was tuned for
+  TuneChoice tc;
+  std::string key;
+};
+
+static void slot_free(BatchSlot& s) {
+  if (s.exec) cudaGraphExecDestroy(s.exec);
+  frameset_free(s.fs);
+  if (s.d_pairs) cudaFree(s.d_pairs);
+  if (s.d_init) cudaFree(s.d_init);
+  if (s.d_out) cudaFree(s.d_out);
+  if (s.d_stats) cudaFree(s.d_stats);
+  if (s.d_work) cudaFree(s.d_work);
+  if (s.h_out) cudaFreeHost(s.h_out);
+  if (s.h_stats) cudaFreeHost(s.h_stats);
+  for (auto& e : s.ev)
     if (e) cudaEventDestroy(e);
+  if (s.copied) cudaEventDestroy(s.copied);
+  if (s.done) cudaEventDestroy(s.done);
+  s = BatchSlot{};
+}
+
+static void batch_free(lsdg_batch* b) {
+  for (auto& s : b->slot) slot_free(s);
+  if (b->d_order) cudaFree(b->d_order);
+  if (b->h_counts) cudaFreeHost(b->h_counts);
+  if (b->copy) cudaStreamDestroy(b->copy);
   delete b;
 }
 
-static lsdg_status batch_track_args(lsdg_ctx* ctx, lsdg_batch* b, TrackArgs* a) {
-  *a = make_track_args(ctx->params);
-  a->pairs = b->d_pairs;
-  a->order = b->d_order;
-  a->n_pairs = b->n;
-  a->work_counter = b->d_work;
-  a->init = b->d_init;
-  a->init_is_ref_to_frame = 0;
-  a->out_pose = b->d_out;
-  a->out_stats = b->d_stats;
-  a->out_sums = nullptr;
+static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
+  const int n = b->n;
+  std::vector<int> w(2 * n), h(2 * n);
+  std::vector<lsdg_intrinsics> k(2 * n);
+  bool* dep = new (std::nothrow) bool[2 * n];
+  if (!dep) return LSDG_OUT_OF_MEMORY;
+  for (int i = 0; i < n; ++i) {
+    w[i] = w[n + i] = b->w[i];
+    h[i] = h[n + i] = b->h[i];
+    k[i] = k[n + i] = b->intr[i];
+    dep[i] = true;
+    dep[n + i] = b->sim3;
+  }
+  // the tracker samples intensity planes only: no gradient pyramid for batch frames
+  lsdg_status st = frameset_alloc(ctx, s.fs, 2 * n, w.data(), h.data(), k.data(), dep, ctx->params.levels, false);
+  delete[] dep;
+  if (st != LSDG_OK) return st;
+  std::vector<PairDev> pairs(n);
+  for (int i = 0; i < n; ++i) pairs[i] = PairDev{s.fs.d_frames + i, s.fs.d_frames + n + i};
+  cudaError_t e = cudaMalloc(&s.d_pairs, sizeof(PairDev) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_init, sizeof(double) * b->pose_len * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_out, sizeof(double) * b->pose_len * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_stats, sizeof(lsdg_track_stats) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_work, sizeof(int) * 4);
+  if (e == cudaSuccess) e = cudaMallocHost(&s.h_out, sizeof(double) * b->pose_len * n);
+  if (e == cudaSuccess) e = cudaMallocHost(&s.h_stats, sizeof(lsdg_track_stats) * n);
+  for (auto& ev : s.ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&ev);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s.d_pairs, pairs.data(), sizeof(PairDev) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return ctx_cuda(ctx, e, "batch slot allocation");
+  s.ready = true;
   return LSDG_OK;
 }
 
-static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, int* launches) {
+static TrackArgs slot_track_args(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
+  TrackArgs a = make_track_args(ctx->params);
+  a.pairs = s.d_pairs;
+  a.order = b->d_order;
+  a.n_pairs = b->n;
+  a.work_counter = s.d_work;
+  a.init = s.d_init;
+  a.init_is_ref_to_frame = 0;
+  a.out_pose = s.d_out;
+  a.out_stats = s.d_stats;
+  a.out_sums = nullptr;
+  return a;
+}
+
+static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, int* launches) {
   // band pass over all 2n frames (also the depth pyramids of the second keyframes in Sim3 mode);
   // reference points only for the first n
   const int L = ctx->params.levels;
-  int k = launch_frame_pyramid(b->fs.d_frames, 2 * b->n, L, b->fs.max_pix, b->fs.max_h, false, ctx->stream);
-  k += launch_frame_points(b->fs.d_frames, b->n, L, b->fs.max_h, ctx->stream);
+  int k = launch_frame_pyramid(s.fs.d_frames, 2 * b->n, L, s.fs.max_pix, s.fs.max_h, false, ctx->stream);
+  k += launch_frame_points(s.fs.d_frames, b->n, L, s.fs.max_h, ctx->stream);
   CK(ctx, cudaGetLastError());
   *launches = k;
+  return LSDG_OK;
+}
+
+// Launch slot si's graph on the context stream, tuning the shape (once per parameter set) and
+// capturing the slot's graph first when needed.
+static lsdg_status slot_run(lsdg_ctx* ctx, lsdg_batch* b, int si) {
+  BatchSlot& s = b->slot[si];
+  if (!s.exec || s.graph_epoch != ctx->params_epoch) {
+    if (s.exec) {
+      cudaGraphExecDestroy(s.exec);
+      s.exec = nullptr;
+    }
+    TrackArgs a = slot_track_args(ctx, b, s);
+    if (b->tune_epoch != ctx->params_epoch) {
+      // eager build so that the autotuner times the tracker on this batch's real points
+      int k = 0;
+      lsdg_status st = enqueue_build(ctx, b, s, &k);
+      if (st != LSDG_OK) return st;
+      ctx->launches += k;
+      st = autotune(ctx, b->key, a, &b->tc, b->sim3);
+      if (st != LSDG_OK) return st;
+      b->tune_epoch = ctx->params_epoch;
+    }
+    // capture: events, build, tracker
+    CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int nl = 0;
+    // external records become event-record nodes of the graph (timed on every replay)
+    cudaEventRecordWithFlags(s.ev[0], ctx->stream, cudaEventRecordExternal);
+    lsdg_status st = enqueue_build(ctx, b, s, &nl);
+    cudaEventRecordWithFlags(s.ev[1], ctx->stream, cudaEventRecordExternal);
+    int64_t before = ctx->launches;
+    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc, b->sim3);
+    nl += (int)(ctx->launches - before);
+    ctx->launches = before;
+    cudaEventRecordWithFlags(s.ev[2], ctx->stream, cudaEventRecordExternal);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (st != LSDG_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    CK(ctx, e);
+    e = cudaGraphInstantiate(&s.exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ctx, e);
+    b->launches_per_run = nl;
+    s.graph_epoch = ctx->params_epoch;
+  }
+  CK(ctx, cudaGraphLaunch(s.exec, ctx->stream));
+  ctx->launches += b->launches_per_run;
+  s.ran = true;
+  b->last = si;
+  return LSDG_OK;
+}
+
+// Host -> device copies of one step's inputs into slot s on stream `st` (new_idepth / new_var:
+// Sim3 batches only).
+static lsdg_status slot_upload(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, cudaStream_t st, const float* ref_images,
+                               const float* ref_idepth, const float* ref_var, const float* new_images,
+                               const float* new_idepth, const float* new_var, const double* init) {
+  // keyframes first; all keyframes carry depth (and, for Sim3, the second half too)
+  const size_t half = (b->sim3 ? s.fs.pix_depth / 2 : s.fs.pix_depth) * 4;
+  char* base = (char*)s.fs.arena;
+  CK(ctx, cudaMemcpyAsync(s.fs.plane0, ref_images, half, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpyAsync((char*)s.fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpyAsync(base + s.fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, st));
+  CK(ctx, cudaMemcpyAsync(base + s.fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, st));
+  if (b->sim3) {
+    CK(ctx, cudaMemcpyAsync(base + s.fs.off_id0 + half, new_idepth, half, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync(base + s.fs.off_var0 + half, new_var, half, cudaMemcpyHostToDevice, st));
+  }
+  CK(ctx, cudaMemcpyAsync(s.d_init, init, sizeof(double) * b->pose_len * b->n, cudaMemcpyHostToDevice, st));
+  return LSDG_OK;
+}
+
+static lsdg_status check_sim3_init(lsdg_ctx* ctx, const lsdg_batch* b, const double* init) {
+  for (int i = 0; i < b->n; ++i)
+    if (!(init[13 * i + 12] > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "pair %d: Sim3 scale must be > 0", i);
+  return LSDG_OK;
+}
+
+static lsdg_status no_pipeline(lsdg_ctx* ctx, const lsdg_batch* b) {
+  if (b->n_inflight) return ctx_fail(ctx, LSDG_INVALID_ARG, "collect the submitted steps first");
   return LSDG_OK;
 }
 
@@ -107,42 +260,20 @@ static lsdg_status batch_create(lsdg_ctx* ctx, int n, const int* widths, const i
   b->n = n;
   b->sim3 = sim3;
   b->pose_len = sim3 ? 13 : 12;
-  std::vector<int> w(2 * n), h(2 * n);
-  std::vector<lsdg_intrinsics> k(2 * n);
-  bool* dep = new bool[2 * n];
-  for (int i = 0; i < n; ++i) {
-    w[i] = w[n + i] = widths[i];
-    h[i] = h[n + i] = heights[i];
-    k[i] = k[n + i] = intr[i];
-    dep[i] = true;
-    dep[n + i] = sim3;
-  }
-  // the tracker samples intensity planes only: no gradient pyramid for batch frames
-  lsdg_status st = frameset_alloc(ctx, b->fs, 2 * n, w.data(), h.data(), k.data(), dep, ctx->params.levels, false);
-  delete[] dep;
+  b->w.assign(widths, widths + n);
+  b->h.assign(heights, heights + n);
+  b->intr.assign(intr, intr + n);
+  lsdg_status st = slot_alloc(ctx, b, b->slot[0]);
   if (st != LSDG_OK) {
     batch_free(b);
     return st;
   }
-  std::vector<PairDev> pairs(n);
-  for (int i = 0; i < n; ++i) pairs[i] = PairDev{b->fs.d_frames + i, b->fs.d_frames + n + i};
   std::vector<int> order(n);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int c) { return (long)widths[a] * heights[a] > (long)widths[c] * heights[c]; });
-  cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_pairs, sizeof(PairDev) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_order, sizeof(int) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_init, sizeof(double) * b->pose_len * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_out, sizeof(double) * b->pose_len * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_stats, sizeof(lsdg_track_stats) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_work, sizeof(int) * 4);
-  if (e == cudaSuccess) e = cudaMallocHost(&b->h_out, sizeof(double) * b->pose_len * n);
-  if (e == cudaSuccess) e = cudaMallocHost(&b->h_stats, sizeof(lsdg_track_stats) * n);
+  cudaError_t e = cudaMalloc(&b->d_order, sizeof(int) * n);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_counts, sizeof(int) * kMaxLevels * n);
-  for (auto& ev : b->ev)
-    if (e == cudaSuccess) e = cudaEventCreate(&ev);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_pairs, pairs.data(), sizeof(PairDev) * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
@@ -166,6 +297,41 @@ static lsdg_status batch_create(lsdg_ctx* ctx, int n, const int* widths, const i
   return LSDG_OK;
 }
 
+// One pipelined step: upload into the free slot on the copy stream, run its graph behind the
+// upload, read the results back behind the graph.
+static lsdg_status batch_submit(lsdg_ctx* ctx, lsdg_batch* b, const float* ri, const float* rd, const float* rv,
+                                const float* ni, const float* nd, const float* nv, const double* init) {
+  if (b->n_inflight >= 2) return ctx_fail(ctx, LSDG_INVALID_ARG, "two steps in flight: collect one first");
+  const int si = b->next;
+  BatchSlot& s = b->slot[si];
+  if (!s.ready) {
+    lsdg_status st = slot_alloc(ctx, b, s);
+    if (st != LSDG_OK) return st;
+  }
+  if (!b->copy) CK(ctx, cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
+  if (!s.exec || s.graph_epoch != ctx->params_epoch) {
+    // first use of this slot (or new parameters): upload on the context stream, then tune/capture
+    lsdg_status st = slot_upload(ctx, b, s, ctx->stream, ri, rd, rv, ni, nd, nv, init);
+    if (st == LSDG_OK) st = slot_run(ctx, b, si);
+    if (st != LSDG_OK) return st;
+  } else {
+    // the slot's arena is free once its previous step has finished (event `done`)
+    CK(ctx, cudaStreamWaitEvent(b->copy, s.done, 0));
+    lsdg_status st = slot_upload(ctx, b, s, b->copy, ri, rd, rv, ni, nd, nv, init);
+    if (st != LSDG_OK) return st;
+    CK(ctx, cudaEventRecord(s.copied, b->copy));
+    CK(ctx, cudaStreamWaitEvent(ctx->stream, s.copied, 0));
+    st = slot_run(ctx, b, si);
+    if (st != LSDG_OK) return st;
+  }
+  CK(ctx, cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(s.h_stats, s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaEventRecord(s.done, ctx->stream));
+  b->inflight[b->n_inflight++] = si;
+  b->next = si ^ 1;
+  return LSDG_OK;
+}
+
 extern "C" {
 
 lsdg_status lsdg_batch_create(lsdg_ctx* ctx, int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
@@ -181,6 +347,7 @@ lsdg_status lsdg_batch_create_sim3(lsdg_ctx* ctx, int n, const int* widths, cons
 lsdg_status lsdg_batch_destroy(lsdg_ctx* ctx, lsdg_batch* b) {
   if (!ctx || !b) return LSDG_INVALID_ARG;
   cudaStreamSynchronize(ctx->stream);
+  if (b->copy) cudaStreamSynchronize(b->copy);
   batch_free(b);
   return LSDG_OK;
 }
@@ -190,14 +357,10 @@ lsdg_status lsdg_batch_load(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_image
   if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !init)
     return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   if (b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 batch: use lsdg_batch_load_sim3");
-  const size_t half = b->fs.pix_depth * 4;  // the keyframes come first, all with depth
-  char* base = (char*)b->fs.arena;
-  CK(ctx, cudaMemcpyAsync(b->fs.plane0, ref_images, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync((char*)b->fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(b->d_init, init, sizeof(double) * 12 * b->n, cudaMemcpyHostToDevice, ctx->stream));
-  return LSDG_OK;
+  lsdg_status st = no_pipeline(ctx, b);
+  if (st != LSDG_OK) return st;
+  return slot_upload(ctx, b, b->slot[0], ctx->stream, ref_images, ref_idepth, ref_var, new_images, nullptr, nullptr,
+                     init);
 }
 
 lsdg_status lsdg_batch_load_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
@@ -206,74 +369,63 @@ lsdg_status lsdg_batch_load_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_
   if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !new_idepth || !new_var || !init)
     return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   if (!b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "not a Sim3 batch (lsdg_batch_create_sim3)");
-  for (int i = 0; i < b->n; ++i)
-    if (!(init[13 * i + 12] > 0)) return ctx_fail(ctx, LSDG_INVALID_ARG, "pair %d: Sim3 scale must be > 0", i);
-  const size_t half = b->fs.pix_depth / 2 * 4;  // both halves carry depth: the keyframes i, then j
-  char* base = (char*)b->fs.arena;
-  CK(ctx, cudaMemcpyAsync(b->fs.plane0, ref_images, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync((char*)b->fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(base + b->fs.off_id0 + half, new_idepth, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(base + b->fs.off_var0 + half, new_var, half, cudaMemcpyHostToDevice, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(b->d_init, init, sizeof(double) * 13 * b->n, cudaMemcpyHostToDevice, ctx->stream));
-  return LSDG_OK;
+  lsdg_status st = check_sim3_init(ctx, b, init);
+  if (st == LSDG_OK) st = no_pipeline(ctx, b);
+  if (st != LSDG_OK) return st;
+  return slot_upload(ctx, b, b->slot[0], ctx->stream, ref_images, ref_idepth, ref_var, new_images, new_idepth,
+                     new_var, init);
 }
 
 lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
   if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
-  if (!b->exec || b->graph_epoch != ctx->params_epoch) {
-    if (b->exec) {
-      cudaGraphExecDestroy(b->exec);
-      b->exec = nullptr;
-    }
-    // eager build so that the autotuner times the tracker on this batch's real points
-    int k = 0;
-    lsdg_status st = enqueue_build(ctx, b, &k);
-    if (st != LSDG_OK) return st;
-    ctx->launches += k;
-    TrackArgs a;
-    batch_track_args(ctx, b, &a);
-    st = autotune(ctx, b->key, a, &b->tc, b->sim3);
-    if (st != LSDG_OK) return st;
-    // capture: events, build, tracker
-    CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int nl = 0;
-    // external records become event-record nodes of the graph (timed on every replay)
-    cudaEventRecordWithFlags(b->ev[0], ctx->stream, cudaEventRecordExternal);
-    st = enqueue_build(ctx, b, &nl);
-    cudaEventRecordWithFlags(b->ev[1], ctx->stream, cudaEventRecordExternal);
-    int64_t before = ctx->launches;
-    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc, b->sim3);
-    nl += (int)(ctx->launches - before);
-    ctx->launches = before;
-    cudaEventRecordWithFlags(b->ev[2], ctx->stream, cudaEventRecordExternal);
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-    if (st != LSDG_OK) {
-      if (g) cudaGraphDestroy(g);
-      return st;
-    }
-    CK(ctx, e);
-    e = cudaGraphInstantiate(&b->exec, g, 0);
-    cudaGraphDestroy(g);
-    CK(ctx, e);
-    b->launches_per_run = nl;
-    b->graph_epoch = ctx->params_epoch;
-  }
-  CK(ctx, cudaGraphLaunch(b->exec, ctx->stream));
-  ctx->launches += b->launches_per_run;
-  b->ran = true;
-  return LSDG_OK;
+  lsdg_status st = no_pipeline(ctx, b);
+  if (st != LSDG_OK) return st;
+  return slot_run(ctx, b, 0);
 }
 
 lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* b, double* out, lsdg_track_stats* stats) {
   if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
-  CK(ctx, cudaMemcpyAsync(b->h_out, b->d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  lsdg_status st = no_pipeline(ctx, b);
+  if (st != LSDG_OK) return st;
+  BatchSlot& s = b->slot[0];
+  CK(ctx, cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(s.h_stats, s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
-  if (out) std::memcpy(out, b->h_out, sizeof(double) * b->pose_len * b->n);
-  if (stats) std::memcpy(stats, b->h_stats, sizeof(lsdg_track_stats) * b->n);
+  if (out) std::memcpy(out, s.h_out, sizeof(double) * b->pose_len * b->n);
+  if (stats) std::memcpy(stats, s.h_stats, sizeof(lsdg_track_stats) * b->n);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_submit_se3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
+                                  const float* ref_var, const float* new_images, const double* init) {
+  if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !init)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 batch: use lsdg_batch_submit_sim3");
+  return batch_submit(ctx, b, ref_images, ref_idepth, ref_var, new_images, nullptr, nullptr, init);
+}
+
+lsdg_status lsdg_batch_submit_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
+                                   const float* ref_var, const float* new_images, const float* new_idepth,
+                                   const float* new_var, const double* init) {
+  if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !new_idepth || !new_var || !init)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (!b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "not a Sim3 batch (lsdg_batch_create_sim3)");
+  lsdg_status st = check_sim3_init(ctx, b, init);
+  if (st != LSDG_OK) return st;
+  return batch_submit(ctx, b, ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var, init);
+}
+
+lsdg_status lsdg_batch_collect(lsdg_ctx* ctx, lsdg_batch* b, double* out, lsdg_track_stats* stats) {
+  if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (!b->n_inflight) return ctx_fail(ctx, LSDG_INVALID_ARG, "no submitted step to collect");
+  const int si = b->inflight[0];
+  BatchSlot& s = b->slot[si];
+  CK(ctx, cudaEventSynchronize(s.done));
+  if (out) std::memcpy(out, s.h_out, sizeof(double) * b->pose_len * b->n);
+  if (stats) std::memcpy(stats, s.h_stats, sizeof(lsdg_track_stats) * b->n);
+  b->inflight[0] = b->inflight[1];
+  b->inflight[1] = -1;
+  --b->n_inflight;
   return LSDG_OK;
 }
 
@@ -300,31 +452,34 @@ lsdg_status lsdg_batch_track_se3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_
 // Device time of the last run's two phases (pyramids + points, tracker), from the events the
 // graph records on the context stream.  Synchronises.
 lsdg_status lsdg_batch_timing(lsdg_ctx* ctx, lsdg_batch* b, float* build_ms, float* track_ms) {
-  if (!ctx || !b || !b->ran) return ctx_fail(ctx, LSDG_INVALID_ARG, "no run to time");
-  CK(ctx, cudaEventSynchronize(b->ev[2]));
+  if (!ctx || !b || !b->slot[b->last].ran) return ctx_fail(ctx, LSDG_INVALID_ARG, "no run to time");
+  BatchSlot& s = b->slot[b->last];
+  CK(ctx, cudaEventSynchronize(s.ev[2]));
   float a = 0, c = 0;
-  CK(ctx, cudaEventElapsedTime(&a, b->ev[0], b->ev[1]));
-  CK(ctx, cudaEventElapsedTime(&c, b->ev[1], b->ev[2]));
+  CK(ctx, cudaEventElapsedTime(&a, s.ev[0], s.ev[1]));
+  CK(ctx, cudaEventElapsedTime(&c, s.ev[1], s.ev[2]));
   if (build_ms) *build_ms = a;
   if (track_ms) *track_ms = c;
   return LSDG_OK;
 }
 
 lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* b, int64_t* passes, double* pass_bytes, double* unique_bytes) {
-  if (!ctx || !b || !b->ran) return ctx_fail(ctx, LSDG_INVALID_ARG, "no run to account");
+  if (!ctx || !b || !b->slot[b->last].ran) return ctx_fail(ctx, LSDG_INVALID_ARG, "no run to account");
+  BatchSlot& s = b->slot[b->last];
   const int L = ctx->params.levels;
+  std::vector<lsdg_track_stats> stats(b->n);
   for (int i = 0; i < b->n; ++i)
-    CK(ctx, cudaMemcpyAsync(b->h_counts + kMaxLevels * i, b->fs.h_frames[i].pcount, sizeof(int) * kMaxLevels,
+    CK(ctx, cudaMemcpyAsync(b->h_counts + kMaxLevels * i, s.fs.h_frames[i].pcount, sizeof(int) * kMaxLevels,
                             cudaMemcpyDeviceToHost, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(b->h_stats, b->d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(stats.data(), s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   int64_t np = 0;
   double pb = 0, ub = 0;
   for (int i = 0; i < b->n; ++i) {
     for (int l = 0; l < L; ++l) {
       const double pts = b->h_counts[kMaxLevels * i + l];
-      const double pix = (double)(b->fs.w[i] >> l) * (b->fs.h[i] >> l);
-      const int ps = b->h_stats[i].passes[l];
+      const double pix = (double)(b->w[i] >> l) * (b->h[i] >> l);
+      const int ps = stats[i].passes[l];
       np += ps;
       // per pass: each point's float4 + its frozen variance (psig; the first pass reads pvar and
       // writes psig instead), the frame level's intensity plane, the sums.  Sim3 adds the point's

@@ -79,6 +79,9 @@ def lib():
     _sig(L, "lsdg_batch_run", st, [_vp, _vp])
     _sig(L, "lsdg_batch_read", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_track_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
+    _sig(L, "lsdg_batch_submit_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p])
+    _sig(L, "lsdg_batch_submit_sim3", st, [_vp, _vp] + [_vp] * 6 + [_f64p])
+    _sig(L, "lsdg_batch_collect", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
@@ -357,6 +360,32 @@ class Batch:
         self._keep = arrs
         self.ctx.check(lib().lsdg_batch_load_sim3(self.ctx.handle, self._h, *[self._ptr(a) for a in arrs],
                                                   np.ascontiguousarray(init, np.float64).reshape(-1)))
+
+    def submit(self, ref_images, ref_idepth, ref_var, new_images, init):
+        """Pipelined step (lsdg_batch_submit_se3): returns at once; collect() gives its results.
+        The arrays must stay untouched (and should be pinned) until then."""
+        arrs = (ref_images, ref_idepth, ref_var, new_images)
+        for a in arrs:
+            assert a.size == self.npix, (a.size, self.npix)
+        self._pending = getattr(self, "_pending", []) + [arrs]
+        self.ctx.check(lib().lsdg_batch_submit_se3(self.ctx.handle, self._h, *[self._ptr(a) for a in arrs],
+                                                   np.ascontiguousarray(init, np.float64).reshape(-1)))
+
+    def submit_sim3(self, ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var, init):
+        arrs = (ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var)
+        for a in arrs:
+            assert a.size == self.npix, (a.size, self.npix)
+        self._pending = getattr(self, "_pending", []) + [arrs]
+        self.ctx.check(lib().lsdg_batch_submit_sim3(self.ctx.handle, self._h, *[self._ptr(a) for a in arrs],
+                                                    np.ascontiguousarray(init, np.float64).reshape(-1)))
+
+    def collect(self):
+        """Results of the oldest submitted step."""
+        out = np.zeros(self.plen * self.n, np.float64)
+        stats = (T.TrackStats * self.n)()
+        self.ctx.check(lib().lsdg_batch_collect(self.ctx.handle, self._h, out, stats))
+        self._pending = self._pending[1:]
+        return (out.reshape(self.n, 13) if self.sim3 else out.reshape(self.n, 3, 4)), stats
 
     def run(self):
         self.ctx.check(lib().lsdg_batch_run(self.ctx.handle, self._h))

@@ -130,6 +130,34 @@ def test_batch_matches_oracle_per_pair(ctx):
     assert passes == sum(s.total_passes for s in stats2)
 
 
+def test_pipelined_batch_equals_synchronous(ctx):
+    """submit/collect: two input sets alternating over the two slots give, in submission order,
+    the synchronous results bit for bit; the synchronous calls refuse while steps are in flight."""
+    sets = [[synth.tracking_pair(300 + 10 * k + i, 320, 240) for i in range(4)] for k in range(2)]
+    intr = [p.intr for p in sets[0]]
+    b = lsdg.Batch(ctx, [320] * 4, [240] * 4, intr)
+    init = np.stack([np.eye(3, 4)] * 4)
+    packed = [[np.ascontiguousarray(a) for a in lsdg.pack_pairs(s)] for s in sets]
+    ref = [b.track(*packed[k], init)[0] for k in range(2)]
+    order = [0, 1, 0, 1, 1]
+    got = []
+    b.submit(*packed[order[0]], init)
+    for k in order[1:]:
+        b.submit(*packed[k], init)
+        with pytest.raises(lsdg.LsdgError):
+            b.submit(*packed[k], init)        # a third step in flight
+        with pytest.raises(lsdg.LsdgError):
+            b.run()                           # synchronous form refuses meanwhile
+        got.append(b.collect()[0])
+    got.append(b.collect()[0])
+    for k, g in zip(order, got):
+        np.testing.assert_array_equal(g, ref[k])
+    with pytest.raises(lsdg.LsdgError):
+        b.collect()                           # nothing left
+    np.testing.assert_array_equal(b.track(*packed[1], init)[0], ref[1])
+    b.close()
+
+
 def test_batch_with_lost_pair(ctx):
     pairs = [synth.tracking_pair(200, 320, 240), synth.tracking_pair(201, 320, 240)]
     pairs[1].ref_idepth = np.full_like(pairs[1].ref_idepth, -1.0)
