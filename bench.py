@@ -362,6 +362,7 @@ def run_ours(args, rank, world, local_rank):
 
     depth_res = bench_depth(ctx, stream, dseq, args)
     energy_res = bench_energy(ctx, stream, pairs[0], rprob, args)
+    input_res = bench_input(ctx, stream, pairs[0], args)
     sim3_res = bench_sim3(ctx, stream, sim3_pairs, args)
 
     result = {
@@ -395,6 +396,7 @@ def run_ours(args, rank, world, local_rank):
         "mixed_batch": mixed_res,
         "keyframe_update": depth_res,
         "energy": energy_res,
+        "input_step": input_res,
         "sim3_constraint_batch": sim3_res,
         "accuracy": {"max_gt_rot_err_rad": max_over_ranks(max(e[0] for e in errs)),
                      "max_gt_trans_err_m": max_over_ranks(max(e[1] for e in errs)),
@@ -435,14 +437,31 @@ def bench_depth(ctx, stream, seq, args):
         e1.synchronize()
         if it >= max(3, args.warmup):
             dev.append(e0.elapsed_time(e1))
-    e2e = []
+    # end to end: 8-bit reference frames (the input thread's format) from pinned memory, update,
+    # read-back of the planes publishKeyframe copies (smoothed inverse depth and variance); and the
+    # float-frame call with the whole 6-plane state read back
+    def pinned(shape, dtype):
+        t = torch.empty(int(np.prod(shape)) * np.dtype(dtype).itemsize, dtype=torch.uint8).pin_memory()
+        return t.numpy().view(dtype).reshape(shape)
+
+    refs_u8 = pinned((len(seq.ref_images), seq.h, seq.w), np.uint8)
+    refs_u8[:] = np.stack([np.clip(np.rint(r), 0, 255) for r in seq.ref_images]).astype(np.uint8)
+    pub = {k: pinned((seq.h, seq.w), np.float32) for k in ("idepth_smoothed", "var_smoothed")}
+    e2e, e2e_full = [], []
     for it in range(max(3, args.warmup) + max(10, args.steps)):
         dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
         t0 = time.perf_counter()
+        dm.updateKeyframe_u8(refs_u8, poses, regularize=True)
+        dm.get(planes=tuple(pub), out=pub)
+        t1 = time.perf_counter()
+        dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+        t2 = time.perf_counter()
         dm.updateKeyframe(seq.ref_images, poses, regularize=True)
         st = dm.get()
+        t3 = time.perf_counter()
         if it >= max(3, args.warmup):
-            e2e.append((time.perf_counter() - t0) * 1e3)
+            e2e.append((t1 - t0) * 1e3)
+            e2e_full.append((t3 - t2) * 1e3)
     prop = []
     for it in range(6):
         dm.set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
@@ -467,7 +486,10 @@ def bench_depth(ctx, stream, seq, args):
     dm.close()
     return {"workload": "updateKeyframe: 1 keyframe 640x480, 8 references on a 10 cm arc, observe + regularize",
             "ms_device": statistics.median(dev), "ms_e2e": statistics.median(e2e),
-            "e2e_api": "lsdg_depth_update + lsdg_depth_get (reference upload, update, state read-back)",
+            "e2e_api": "lsdg_depth_update_u8 (8 x 8-bit 640x480 references from pinned memory) + lsdg_depth_get "
+                       "of the two planes publishKeyframe copies",
+            "ms_e2e_float_full_state": statistics.median(e2e_full),
+            "e2e_float_full_state_api": "lsdg_depth_update (float references, pageable) + lsdg_depth_get of all 6 planes",
             "create_keyframe_ms_e2e": statistics.median(prop),
             "well_observed_pixels": int(good.sum()), "median_rel_idepth_err_vs_truth": float(np.median(rel)),
             "cloud_ms": statistics.median(cl), "cloud_vertices": int(n_vertices),
@@ -530,6 +552,35 @@ def bench_energy(ctx, stream, pair, rp, args):
             "refine_energy_before_after": [e0_, e1_],
             "refine_median_rel_idepth_err_vs_truth_before_after": [float(np.median(np.abs(rho0 / truth - 1))),
                                                                    float(np.median(np.abs(rho / truth - 1)))]}
+
+
+def bench_input(ctx, stream, pair, args):
+    """The input step: a raw 8-bit 640x480 frame of a radial-tangential ("frame" model) camera,
+    undistorted on the device into the tracking camera and built into a 5-level pyramid
+    (lsdg_frame_upload_distorted_u8, host buffer to pyramid, synchronous)."""
+    import torch
+
+    import lsdg
+    import lsdg_types as T
+
+    c = T.Calibration()
+    c.model, c.width, c.height = T.CALIB_FRAME, W, H
+    c.f, c.cx, c.cy, c.b2, c.k1, c.k2, c.p1, c.p2 = 500.0, -3.5, 2.25, -0.8, -0.12, 0.29, 3e-4, 1.8e-3
+    u = lsdg.Undistorter(ctx, c)
+    w, h, K = u.camera()
+    f = lsdg.Frame(ctx, w, h, K)
+    t = torch.empty(W * H, dtype=torch.uint8).pin_memory()
+    raw = t.numpy().reshape(H, W)
+    raw[:] = np.clip(np.rint(pair.new_image), 0, 255).astype(np.uint8)
+    ts = []
+    for it in range(max(3, args.warmup) + 20):
+        t0 = time.perf_counter()
+        u.upload(f, raw)
+        if it >= max(3, args.warmup):
+            ts.append((time.perf_counter() - t0) * 1e3)
+    u.close()
+    return {"workload": "raw 8-bit 640x480 frame -> frame-model undistortion -> 5-level pyramid",
+            "ms_e2e": statistics.median(ts), "api": "lsdg_frame_upload_distorted_u8 (pinned raw frame)"}
 
 
 def bench_sim3(ctx, stream, sps, args):

@@ -149,6 +149,26 @@ typedef struct lsdg_frame lsdg_frame;
 typedef struct lsdg_batch lsdg_batch;
 typedef struct lsdg_depthmap lsdg_depthmap;
 typedef struct lsdg_energy lsdg_energy;
+typedef struct lsdg_undistorter lsdg_undistorter;
+
+/* Input camera calibration (what libvideoio's UndistorterFactory reads from the file given with
+ * -c/--calib, tools/LSD.cpp:62,88; the sample is d2_camera.xml).  Models:
+ *   LSDG_CALIB_PINHOLE: no distortion (u = f x + w/2 + cx, v = f y + h/2 + cy);
+ *   LSDG_CALIB_FRAME ("<projection>frame</projection>"): with r^2 = x^2 + y^2,
+ *     x' = x (1 + k1 r^2 + k2 r^4 + k3 r^6 + k4 r^8) + p1 (r^2 + 2 x^2) + 2 p2 x y
+ *     y' = y (1 + k1 r^2 + k2 r^4 + k3 r^6 + k4 r^8) + p2 (r^2 + 2 y^2) + 2 p1 x y
+ *     u = w/2 + cx + x' f + x' b1 + y' b2,   v = h/2 + cy + y' f
+ *   with (u, v) measured from the image's top-left corner (pixel centres at +0.5). */
+#define LSDG_CALIB_PINHOLE 0
+#define LSDG_CALIB_FRAME 1
+typedef struct lsdg_calibration {
+  int32_t model;
+  int32_t width, height;   /* raw input size */
+  double f, cx, cy;        /* focal length; principal point offset from the image centre (pixels) */
+  double b1, b2;           /* affinity and skew */
+  double k1, k2, k3, k4;   /* radial */
+  double p1, p2;           /* tangential */
+} lsdg_calibration;
 
 /* Wire formats of the viewer path, byte-compatible with the reference's structs:
  * InputPointDense (lib/Pangolin_IOWrapper/Keyframe.h:16-21): what publishKeyframe copies per pixel,
@@ -358,6 +378,10 @@ LSDG_API lsdg_status lsdg_depth_update_loaded(lsdg_ctx* ctx, lsdg_depthmap* dm, 
 /* load_refs + update_loaded, synchronous. */
 LSDG_API lsdg_status lsdg_depth_update(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs, const float* ref_images,
                                        const double* key_to_ref, int regularize);
+/* The same with 8-bit reference frames (the InputThread's format, lib/App/InputThread.cpp:59-62):
+ * n_refs * w * h bytes, converted to intensity planes on the device. */
+LSDG_API lsdg_status lsdg_depth_update_u8(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs, const uint8_t* ref_images,
+                                          const double* key_to_ref, int regularize);
 /* regularizeDepthMap (+ hole filling and removal of unsupported hypotheses), synchronous. */
 LSDG_API lsdg_status lsdg_depth_regularize(lsdg_ctx* ctx, lsdg_depthmap* dm);
 /* DepthMap::createKeyFrame: propagateDepth of every hypothesis into the new keyframe (nearest
@@ -453,6 +477,32 @@ LSDG_API lsdg_status lsdg_energy_refine(lsdg_ctx* ctx, lsdg_energy* e, int n_fra
 /* Device time (ms) of the last forward, backward and refine kernels, from CUDA events. */
 LSDG_API lsdg_status lsdg_energy_timing(lsdg_ctx* ctx, const lsdg_energy* e, float* forward_ms, float* backward_ms,
                                         float* refine_ms);
+
+/* ------------------------------------------------------------------------------------------ */
+/* Input step: raw 8-bit frame -> undistorted frame (InputThread, lib/App/InputThread.cpp:59-71)  */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Parses a calibration file with <calibration> tags (<projection>, <width>, <height>, <f>, <cx>,
+ * <cy>, <b1>, <b2>, <k1>..<k4>, <p1>, <p2>; absent coefficients are 0).  Host only, no GPU. */
+LSDG_API lsdg_status lsdg_calibration_load_xml(const char* path, lsdg_calibration* out);
+
+/* An undistorter from `calib` to an ideal pinhole camera of out_w x out_h with intrinsics out_K
+ * (NULL: the calibration's size, fx = fy = f, principal point w/2 + cx - 0.5, h/2 + cy - 0.5 in
+ * pixel-centre coordinates).  The remap table (source position of every output pixel) is computed
+ * once on the device in FP64 and kept as float pairs. */
+LSDG_API lsdg_status lsdg_undistorter_create(lsdg_ctx* ctx, const lsdg_calibration* calib, int out_w, int out_h,
+                                             const lsdg_intrinsics* out_K, lsdg_undistorter** out);
+LSDG_API lsdg_status lsdg_undistorter_destroy(lsdg_ctx* ctx, lsdg_undistorter* u);
+/* The output camera (what undistorter->getCamera() / outputImageSize() give the SLAM system). */
+LSDG_API lsdg_status lsdg_undistorter_camera(lsdg_ctx* ctx, const lsdg_undistorter* u, int* out_w, int* out_h,
+                                             lsdg_intrinsics* out_K);
+/* Uploads a raw 8-bit frame (calib width x height), undistorts it on the device (bilinear, rounded to
+ * 8 bits like the undistorted CV_8UC1 image the input thread hands over; outside the raw image: 0)
+ * into `frame` (out_w x out_h, created with the output camera) and builds its pyramid. */
+LSDG_API lsdg_status lsdg_frame_upload_distorted_u8(lsdg_ctx* ctx, lsdg_undistorter* u, lsdg_frame* frame,
+                                                    const uint8_t* raw);
+/* The undistorted 8-bit image of the last upload (host, out_w x out_h), for the GUI's live view. */
+LSDG_API lsdg_status lsdg_undistorter_last_image(lsdg_ctx* ctx, const lsdg_undistorter* u, uint8_t* out);
 
 /* ------------------------------------------------------------------------------------------ */
 /* Keyframe point cloud (the viewer's data path, headless)                                      */

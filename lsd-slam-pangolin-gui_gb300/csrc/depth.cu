@@ -33,6 +33,7 @@ using namespace lsdg;
 namespace lsdg {
 int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, int max_h, bool with_grads,
                          cudaStream_t s);
+void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
 }
 
 #define CK(ctx, expr)                                \
@@ -458,6 +459,7 @@ struct lsdg_depthmap {
   void* arena = nullptr;   // state A, state B, references, propagation keys
   DepthPlanes cur{}, alt{};
   float* refs = nullptr;
+  uint8_t* refs_u8 = nullptr;  // staging of 8-bit reference frames (lsdg_depth_update_u8)
   unsigned long long* keys = nullptr;
   bool has_key = false;
 };
@@ -534,7 +536,7 @@ lsdg_status lsdg_depth_create(lsdg_ctx* ctx, int width, int height, const lsdg_i
     return st;
   }
   const size_t n = (size_t)width * height;
-  const size_t bytes = 2 * 6 * n * 4 + (size_t)LSDG_MAX_REFS * n * 4 + n * 8 + 1024;
+  const size_t bytes = 2 * 6 * n * 4 + (size_t)LSDG_MAX_REFS * n * 5 + n * 8 + 2048;
   cudaError_t e = cudaMalloc(&dm->arena, bytes);
   if (e != cudaSuccess) {
     depth_free(dm);
@@ -545,6 +547,9 @@ lsdg_status lsdg_depth_create(lsdg_ctx* ctx, int width, int height, const lsdg_i
   dm->alt = carve_planes(p, n);
   dm->refs = (float*)p;
   p += (size_t)LSDG_MAX_REFS * n * 4;
+  p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+  dm->refs_u8 = (uint8_t*)p;
+  p += (size_t)LSDG_MAX_REFS * n;
   p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
   dm->keys = (unsigned long long*)p;
   *out = dm;
@@ -631,6 +636,21 @@ lsdg_status lsdg_depth_update(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs, cons
   lsdg_status st = lsdg_depth_load_refs(ctx, dm, n_refs, ref_images);
   if (st != LSDG_OK) return st;
   st = lsdg_depth_update_loaded(ctx, dm, n_refs, key_to_ref, regularize);
+  if (st != LSDG_OK) return st;
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_depth_update_u8(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_refs, const uint8_t* ref_images,
+                                 const double* key_to_ref, int regularize) {
+  if (!ctx || !dm || !ref_images) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (n_refs < 1 || n_refs > LSDG_MAX_REFS) return ctx_fail(ctx, LSDG_INVALID_ARG, "n_refs must be in 1..%d", LSDG_MAX_REFS);
+  const size_t n = (size_t)dm->w * dm->h * n_refs;
+  CK(ctx, cudaMemcpyAsync(dm->refs_u8, ref_images, n, cudaMemcpyHostToDevice, ctx->stream));
+  launch_u8_to_plane(dm->refs_u8, dm->refs, (int)n, ctx->stream);
+  ctx->launches += 1;
+  CK(ctx, cudaGetLastError());
+  lsdg_status st = lsdg_depth_update_loaded(ctx, dm, n_refs, key_to_ref, regularize);
   if (st != LSDG_OK) return st;
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   return LSDG_OK;

@@ -91,6 +91,7 @@ def lib():
     _sig(L, "lsdg_depth_load_refs", st, [_vp, _vp, C.c_int, _f32p])
     _sig(L, "lsdg_depth_update_loaded", st, [_vp, _vp, C.c_int, _f64p, C.c_int])
     _sig(L, "lsdg_depth_update", st, [_vp, _vp, C.c_int, _f32p, _f64p, C.c_int])
+    _sig(L, "lsdg_depth_update_u8", st, [_vp, _vp, C.c_int, _vp, _f64p, C.c_int])
     _sig(L, "lsdg_depth_regularize", st, [_vp, _vp])
     _sig(L, "lsdg_depth_create_keyframe", st, [_vp, _vp, _f32p, _f64p, C.c_int])
     _sig(L, "lsdg_depth_get", st, [_vp, _vp] + [C.c_void_p] * 6)
@@ -111,6 +112,13 @@ def lib():
     _sig(L, "lsdg_cloud_build", st, [_vp, C.c_int, C.c_int] + [C.c_float] * 5 + [C.POINTER(T.CloudParams), _vp, _vp,
                                                                                  C.POINTER(C.c_int)])
     _sig(L, "lsdg_cloud_from_depthmap", st, [_vp, _vp, C.c_float, C.POINTER(T.CloudParams), _vp, C.POINTER(C.c_int)])
+    _sig(L, "lsdg_calibration_load_xml", st, [C.c_char_p, C.POINTER(T.Calibration)])
+    _sig(L, "lsdg_undistorter_create", st, [_vp, C.POINTER(T.Calibration), C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                            C.POINTER(_vp)])
+    _sig(L, "lsdg_undistorter_destroy", st, [_vp, _vp])
+    _sig(L, "lsdg_undistorter_camera", st, [_vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(T.Intrinsics)])
+    _sig(L, "lsdg_frame_upload_distorted_u8", st, [_vp, _vp, _vp, _u8p])
+    _sig(L, "lsdg_undistorter_last_image", st, [_vp, _vp, _u8p])
     _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
     _lib = L
     return L
@@ -462,6 +470,14 @@ class DepthMap:
         imgs, poses = self._refs(ref_images, key_to_ref)
         self.ctx.check(lib().lsdg_depth_update(self.ctx.handle, self._h, len(ref_images), imgs, poses, int(regularize)))
 
+    def updateKeyframe_u8(self, ref_images_u8, key_to_ref, regularize=True):
+        """8-bit reference frames: one (n, h, w) uint8 array (pinned for speed) or a list of (h, w)."""
+        a = ref_images_u8 if isinstance(ref_images_u8, np.ndarray) else np.stack(ref_images_u8)
+        assert a.dtype == np.uint8 and a.flags["C_CONTIGUOUS"] and a.size % (self.w * self.h) == 0
+        n = a.size // (self.w * self.h)
+        poses = np.ascontiguousarray(np.concatenate([np.asarray(p, np.float64).reshape(-1) for p in key_to_ref]))
+        self.ctx.check(lib().lsdg_depth_update_u8(self.ctx.handle, self._h, n, a.ctypes.data, poses, int(regularize)))
+
     def load_refs(self, ref_images):
         imgs = np.ascontiguousarray(np.concatenate([np.asarray(r, np.float32).ravel() for r in ref_images]), np.float32)
         self._keep = imgs
@@ -493,12 +509,16 @@ class DepthMap:
         self.ctx.check(lib().lsdg_depth_create_keyframe(self.ctx.handle, self._h, np.ascontiguousarray(new_image, np.float32),
                                                         _pose12(key_to_new), int(regularize)))
 
-    def get(self):
-        out = {}
-        for name in self.PLANES:
-            dt = np.int32 if name in ("validity", "blacklist") else np.float32
-            out[name] = np.zeros((self.h, self.w), dt)
-        self.ctx.check(lib().lsdg_depth_get(self.ctx.handle, self._h, *[out[n].ctypes.data for n in self.PLANES]))
+    def get(self, planes=None, out=None):
+        """The state planes (all by default); `out` may hold preallocated (e.g. pinned) arrays."""
+        planes = self.PLANES if planes is None else planes
+        out = {} if out is None else out
+        for name in planes:
+            if name not in out:
+                dt = np.int32 if name in ("validity", "blacklist") else np.float32
+                out[name] = np.zeros((self.h, self.w), dt)
+        ptrs = [out[n].ctypes.data if n in planes else None for n in self.PLANES]
+        self.ctx.check(lib().lsdg_depth_get(self.ctx.handle, self._h, *ptrs))
         return out
 
     def close(self):
@@ -581,6 +601,57 @@ class PhotometricEnergy:
     def close(self):
         if self._h and self.ctx.handle:
             lib().lsdg_energy_destroy(self.ctx.handle, self._h)
+        self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def calibration_load_xml(path: str) -> T.Calibration:
+    """Parse a calibration file (d2_camera.xml format) with the library's reader (host only)."""
+    c = T.Calibration()
+    rc = lib().lsdg_calibration_load_xml(path.encode(), C.byref(c))
+    if rc != T.OK:
+        raise LsdgError(rc, "cannot read calibration %s" % path)
+    return c
+
+
+class Undistorter:
+    """The input thread's undistorter: raw 8-bit frames of the calibrated camera -> frames of the
+    ideal pinhole output camera (camera())."""
+
+    def __init__(self, ctx: Context, calib: T.Calibration, out_w: int = None, out_h: int = None, out_K=None):
+        self.ctx = ctx
+        self.calib = calib
+        self._h = _vp()
+        ow = calib.width if out_w is None else out_w
+        oh = calib.height if out_h is None else out_h
+        k = None if out_K is None else C.byref(intrinsics(out_K))
+        ctx.check(lib().lsdg_undistorter_create(ctx.handle, C.byref(calib), ow, oh, k, C.byref(self._h)))
+
+    def camera(self):
+        w, h, k = C.c_int(), C.c_int(), T.Intrinsics()
+        self.ctx.check(lib().lsdg_undistorter_camera(self.ctx.handle, self._h, C.byref(w), C.byref(h), C.byref(k)))
+        return w.value, h.value, k
+
+    def upload(self, frame: "Frame", raw: np.ndarray):
+        raw = np.ascontiguousarray(raw, np.uint8)
+        assert raw.shape == (self.calib.height, self.calib.width)
+        self.ctx.check(lib().lsdg_frame_upload_distorted_u8(self.ctx.handle, self._h, frame.handle, raw.reshape(-1)))
+        return frame
+
+    def last_image(self):
+        w, h, _ = self.camera()
+        out = np.zeros(w * h, np.uint8)
+        self.ctx.check(lib().lsdg_undistorter_last_image(self.ctx.handle, self._h, out))
+        return out.reshape(h, w)
+
+    def close(self):
+        if self._h and self.ctx.handle:
+            lib().lsdg_undistorter_destroy(self.ctx.handle, self._h)
         self._h = _vp()
 
     def __del__(self):

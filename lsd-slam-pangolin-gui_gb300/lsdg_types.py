@@ -110,3 +110,15 @@ class CloudParams(C.Structure):
     """lsdg_cloud_params (include/lsdg.h)."""
     _fields_ = [("scaled_th", C.c_float), ("abs_th", C.c_float), ("min_near_support", C.c_int32),
                 ("reserved", C.c_int32)]
+
+
+CALIB_PINHOLE = 0
+CALIB_FRAME = 1
+
+
+class Calibration(C.Structure):
+    """lsdg_calibration (include/lsdg.h)."""
+    _fields_ = [("model", C.c_int32), ("width", C.c_int32), ("height", C.c_int32),
+                ("f", C.c_double), ("cx", C.c_double), ("cy", C.c_double), ("b1", C.c_double), ("b2", C.c_double),
+                ("k1", C.c_double), ("k2", C.c_double), ("k3", C.c_double), ("k4", C.c_double),
+                ("p1", C.c_double), ("p2", C.c_double)]

@@ -14,7 +14,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["lsdo_params.cpp", "lsdo_track.cpp", "lsdo_depth.cpp", "lsdo_sim3.cpp", "lsdo_energy.cpp", "lsdo_cloud.cpp"]
+SOURCES = ["lsdo_params.cpp", "lsdo_track.cpp", "lsdo_depth.cpp", "lsdo_sim3.cpp", "lsdo_energy.cpp", "lsdo_cloud.cpp", "lsdo_input.cpp"]
 LIB = os.path.join(HERE, "liblsdo.so")
 
 

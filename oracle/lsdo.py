@@ -82,6 +82,8 @@ def lib():
         L.lsdo_cloud_build.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                        _vp, _vp, _vp]
         L.lsdo_cloud_build.restype = C.c_int
+        L.lsdo_undistort_map.argtypes = [C.POINTER(T.Calibration), C.c_int, C.c_int, C.POINTER(T.Intrinsics), _f32p]
+        L.lsdo_undistort.argtypes = [_vp, C.c_int, C.c_int, _f32p, C.c_int, _vp]
         L.lsdo_hardware_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -380,3 +382,22 @@ def cloud_build(points, w, h, fx, fy, cx, cy, scale=1.0, scaled_th=1e-3, abs_th=
     p = T.CloudParams(scaled_th, abs_th, min_near_support, 0)
     n = lib().lsdo_cloud_build(w, h, fx, fy, cx, cy, scale, C.addressof(p), pts.ctypes.data, out.ctypes.data)
     return out[:n].copy()
+
+
+# ------------------------------------------------------------------------------------------
+# Input step: undistortion
+# ------------------------------------------------------------------------------------------
+def undistort_map(calib, out_w, out_h, K):
+    """(out_h, out_w, 2) float32 source positions of the output pixels."""
+    m = np.zeros((out_h, out_w, 2), np.float32)
+    lib().lsdo_undistort_map(C.byref(calib), out_w, out_h, C.byref(_intr(K)), m.reshape(-1))
+    return m
+
+
+def undistort(raw, map_):
+    raw = np.ascontiguousarray(raw, np.uint8)
+    h, w = raw.shape
+    out = np.zeros(map_.shape[:2], np.uint8)
+    m = np.ascontiguousarray(map_, np.float32)
+    lib().lsdo_undistort(raw.ctypes.data, w, h, m.reshape(-1), out.size, out.ctypes.data)
+    return out

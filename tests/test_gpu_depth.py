@@ -84,3 +84,25 @@ def test_depth_argument_errors(ctx, seq320):
     with pytest.raises(lsdg.LsdgError):
         dm.updateKeyframe(seq320.ref_images[:1] * 17, [np.eye(3, 4)] * 17)
     dm.close()
+
+
+def test_u8_reference_frames_equal_float_path(ctx):
+    """lsdg_depth_update_u8 (8-bit frames, converted on the device) gives the state of the float path
+    on the same (quantised) frames, bit for bit."""
+    import lsdg
+    import synth
+    seq = synth.depth_sequence(11, 320, 240, n_refs=4)
+    q = [np.clip(np.rint(r), 0, 255).astype(np.uint8) for r in seq.ref_images]
+    poses = [synth.pose_inv(T) for T in seq.ref_frame_to_key]
+    a = lsdg.DepthMap(ctx, seq.w, seq.h, seq.intr).set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+    a.updateKeyframe([x.astype(np.float32) for x in q], poses)
+    b = lsdg.DepthMap(ctx, seq.w, seq.h, seq.intr).set_keyframe(seq.key_image, seq.init_idepth, seq.init_var)
+    b.updateKeyframe_u8(np.ascontiguousarray(np.stack(q)), poses)
+    sa, sb = a.get(), b.get()
+    for k in sa:
+        np.testing.assert_array_equal(sa[k], sb[k], err_msg=k)
+    part = b.get(planes=("idepth_smoothed", "var_smoothed"))
+    assert set(part) == {"idepth_smoothed", "var_smoothed"}
+    np.testing.assert_array_equal(part["idepth_smoothed"], sa["idepth_smoothed"])
+    a.close()
+    b.close()
