@@ -534,6 +534,28 @@ LSDG_API lsdg_status lsdg_cloud_from_depthmap(lsdg_ctx* ctx, lsdg_depthmap* dm, 
                                               int* count);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Pose wire formats (host only, no GPU)                                                        */
+/* ------------------------------------------------------------------------------------------ */
+
+/* GraphFramePose (lib/Pangolin_IOWrapper/Keyframe.h:23-27): a keyframe id and the 7 floats that
+ * publishKeyframeGraph memcpys out of Sophus::Sim3f::data() (PangolinOutputIOWrapper.cpp:161):
+ * the RxSO3 quaternion (x, y, z, w), whose squared norm is the scale, then the translation. */
+typedef struct lsdg_graph_frame_pose {
+  int32_t id;
+  float cam_to_world[7];
+} lsdg_graph_frame_pose;
+
+/* 13-double Sim3 {R, t, s} <-> the 7-float Sophus layout above. */
+LSDG_API void lsdg_sim3_to_sophus7(const double pose13[13], float out7[7]);
+LSDG_API void lsdg_sophus7_to_sim3(const float in7[7], double pose13[13]);
+/* One line of TextOutputIOWrapper's pose file (lib/Pangolin_IOWrapper/TextOutputIOWrapper.cpp:104-117):
+ * "id,x,y,z,px,py,pz\n" with the camera-to-world translation and the translation of the frame's
+ * pose relative to its parent, each value as a default C++ stream prints it (6 significant digits).
+ * Returns the number of characters written (excluding the terminating 0), or -1 if `len` is short. */
+LSDG_API int lsdg_format_pose_row(int id, const double cam_to_world13[13], const double this_to_parent13[13],
+                                  char* buf, int len);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                   */
 /* ------------------------------------------------------------------------------------------ */
 

@@ -119,6 +119,9 @@ def lib():
     _sig(L, "lsdg_undistorter_camera", st, [_vp, _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(T.Intrinsics)])
     _sig(L, "lsdg_frame_upload_distorted_u8", st, [_vp, _vp, _vp, _u8p])
     _sig(L, "lsdg_undistorter_last_image", st, [_vp, _vp, _u8p])
+    _sig(L, "lsdg_sim3_to_sophus7", None, [_f64p, _f32p])
+    _sig(L, "lsdg_sophus7_to_sim3", None, [_f32p, _f64p])
+    _sig(L, "lsdg_format_pose_row", C.c_int, [C.c_int, _f64p, _f64p, C.c_char_p, C.c_int])
     _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
     _lib = L
     return L
@@ -608,6 +611,27 @@ class PhotometricEnergy:
             self.close()
         except Exception:
             pass
+
+
+def sim3_to_sophus7(pose13) -> np.ndarray:
+    """13-double {R, t, s} -> the 7 floats of Sophus::Sim3f::data() (quaternion x y z w with
+    squared norm = scale, translation) that GraphFramePose carries."""
+    out = np.zeros(7, np.float32)
+    lib().lsdg_sim3_to_sophus7(_pose13(pose13), out)
+    return out
+
+
+def sophus7_to_sim3(p7) -> np.ndarray:
+    out = np.zeros(13, np.float64)
+    lib().lsdg_sophus7_to_sim3(np.ascontiguousarray(p7, np.float32), out)
+    return out
+
+
+def format_pose_row(frame_id: int, cam_to_world13, this_to_parent13) -> str:
+    buf = C.create_string_buffer(256)
+    n = lib().lsdg_format_pose_row(frame_id, _pose13(cam_to_world13), _pose13(this_to_parent13), buf, 256)
+    assert n > 0
+    return buf.value.decode()
 
 
 def calibration_load_xml(path: str) -> T.Calibration:
