@@ -322,6 +322,12 @@ LSDG_API lsdg_status lsdg_batch_submit_sim3(lsdg_ctx* ctx, lsdg_batch* batch, co
                                             const float* new_idepth_var, const double* frame_to_ref_init);
 LSDG_API lsdg_status lsdg_batch_collect(lsdg_ctx* ctx, lsdg_batch* batch, double* frame_to_ref_out,
                                         lsdg_track_stats* stats);
+/* Fill the batch from frames already on the device (device-to-device copies of their level-0
+ * planes): pair i tracks frames[i] against refs[i] (refs need depth; frames too for a Sim3 batch),
+ * sizes as the batch was created with.  The constraint search's candidates are resident keyframes,
+ * so nothing crosses the host bus but the initial poses.  Then lsdg_batch_run / lsdg_batch_read. */
+LSDG_API lsdg_status lsdg_batch_load_frames(lsdg_ctx* ctx, lsdg_batch* batch, const lsdg_frame* const* refs,
+                                            const lsdg_frame* const* frames, const double* frame_to_ref_init);
 /* A batch of Sim3 constraint trackings (a new keyframe against its candidates): both keyframes of
  * every pair carry depth; poses are 13 doubles.  lsdg_batch_run and lsdg_batch_read work on it as on
  * an SE3 batch. */

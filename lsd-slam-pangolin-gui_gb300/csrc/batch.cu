@@ -376,6 +376,42 @@ lsdg_status lsdg_batch_load_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_
                      new_var, init);
 }
 
+lsdg_status lsdg_batch_load_frames(lsdg_ctx* ctx, lsdg_batch* b, const lsdg_frame* const* refs,
+                                   const lsdg_frame* const* frames, const double* init) {
+  if (!ctx || !b || !refs || !frames || !init) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  lsdg_status st = no_pipeline(ctx, b);
+  if (st == LSDG_OK && b->sim3) st = check_sim3_init(ctx, b, init);
+  if (st != LSDG_OK) return st;
+  BatchSlot& s = b->slot[0];
+  for (int i = 0; i < b->n; ++i) {
+    if (!refs[i] || !frames[i]) return ctx_fail(ctx, LSDG_INVALID_ARG, "pair %d: null frame", i);
+    const FrameDev& R = refs[i]->fs.h_frames[0];
+    const FrameDev& F = frames[i]->fs.h_frames[0];
+    if (R.w != b->w[i] || R.h != b->h[i] || F.w != b->w[i] || F.h != b->h[i])
+      return ctx_fail(ctx, LSDG_INVALID_ARG, "pair %d: frame size differs from the batch's", i);
+    if (!refs[i]->has_image || !frames[i]->has_image || !R.has_depth || (b->sim3 && !F.has_depth))
+      return ctx_fail(ctx, LSDG_INVALID_ARG, "pair %d: image or depth missing", i);
+  }
+  for (int i = 0; i < b->n; ++i) {
+    const FrameDev& R = refs[i]->fs.h_frames[0];
+    const FrameDev& F = frames[i]->fs.h_frames[0];
+    const FrameDev& Ki = s.fs.h_frames[i];
+    const FrameDev& Kj = s.fs.h_frames[b->n + i];
+    const size_t bytes = (size_t)b->w[i] * b->h[i] * 4;
+    const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    CK(ctx, cudaMemcpyAsync(Ki.plane[0], R.plane[0], bytes, d2d, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(Ki.idepth[0], R.idepth[0], bytes, d2d, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(Ki.ivar[0], R.ivar[0], bytes, d2d, ctx->stream));
+    CK(ctx, cudaMemcpyAsync(Kj.plane[0], F.plane[0], bytes, d2d, ctx->stream));
+    if (b->sim3) {
+      CK(ctx, cudaMemcpyAsync(Kj.idepth[0], F.idepth[0], bytes, d2d, ctx->stream));
+      CK(ctx, cudaMemcpyAsync(Kj.ivar[0], F.ivar[0], bytes, d2d, ctx->stream));
+    }
+  }
+  CK(ctx, cudaMemcpyAsync(s.d_init, init, sizeof(double) * b->pose_len * b->n, cudaMemcpyHostToDevice, ctx->stream));
+  return LSDG_OK;
+}
+
 lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* b) {
   if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   lsdg_status st = no_pipeline(ctx, b);

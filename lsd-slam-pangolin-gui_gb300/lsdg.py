@@ -81,6 +81,7 @@ def lib():
     _sig(L, "lsdg_batch_track_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_submit_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p])
     _sig(L, "lsdg_batch_submit_sim3", st, [_vp, _vp] + [_vp] * 6 + [_f64p])
+    _sig(L, "lsdg_batch_load_frames", st, [_vp, _vp, _vp, _vp, _f64p])
     _sig(L, "lsdg_batch_collect", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
@@ -397,6 +398,14 @@ class Batch:
         self.ctx.check(lib().lsdg_batch_collect(self.ctx.handle, self._h, out, stats))
         self._pending = self._pending[1:]
         return (out.reshape(self.n, 13) if self.sim3 else out.reshape(self.n, 3, 4)), stats
+
+    def load_frames(self, refs, frames, init):
+        """Fill the batch from resident Frames (device-to-device); init (n, 12) or (n, 13)."""
+        assert len(refs) == len(frames) == self.n
+        ra = (_vp * self.n)(*[f.handle for f in refs])
+        fa = (_vp * self.n)(*[f.handle for f in frames])
+        self.ctx.check(lib().lsdg_batch_load_frames(self.ctx.handle, self._h, ra, fa,
+                                                    np.ascontiguousarray(init, np.float64).reshape(-1)))
 
     def run(self):
         self.ctx.check(lib().lsdg_batch_run(self.ctx.handle, self._h))

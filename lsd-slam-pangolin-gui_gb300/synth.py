@@ -111,11 +111,19 @@ def _hash01(ix: np.ndarray, iy: np.ndarray, seed: int) -> np.ndarray:
     return h.astype(np.float64) * (1.0 / 4294967296.0)
 
 
-def value_noise(u: np.ndarray, v: np.ndarray, seed: int, octaves: int = 4, base_freq: float = 1.0) -> np.ndarray:
-    """Sum of ``octaves`` octaves of lattice value noise, normalised to [0, 1]."""
+def value_noise(u: np.ndarray, v: np.ndarray, seed: int, octaves: int = 4, base_freq: float = 1.0,
+                footprint: np.ndarray = None) -> np.ndarray:
+    """Sum of ``octaves`` octaves of lattice value noise, normalised to [0, 1].  ``footprint``
+    (optional, per sample, in texture units): octaves with more than 1/4 cycle per footprint fade
+    out linearly, gone at 1/2 (band-limited texture, so a point-sampled render does not alias)."""
     total = np.zeros_like(u)
     amp, norm, f = 1.0, 0.0, base_freq
     for o in range(octaves):
+        if footprint is not None:
+            c = f * footprint
+            fade = np.clip(2.0 - 4.0 * c, 0.0, 1.0)
+        else:
+            fade = 1.0
         x = u * f
         y = v * f
         ix = np.floor(x)
@@ -131,7 +139,7 @@ def value_noise(u: np.ndarray, v: np.ndarray, seed: int, octaves: int = 4, base_
         h11 = _hash01(ix + 1, iy + 1, s)
         a = h00 + (h10 - h00) * sx
         b = h01 + (h11 - h01) * sx
-        total += amp * (a + (b - a) * sy)
+        total += (amp * fade) * (a + (b - a) * sy) + (amp * (1.0 - fade)) * 0.5
         norm += amp
         amp *= 0.5
         f *= 2.0
@@ -197,9 +205,10 @@ def make_scene(rng: np.random.Generator, n_planes: int = 6, depth_range=(1.0, 5.
     return patches
 
 
-def render(patches, intr: Intrinsics, w: int, h: int, cam_to_ref: np.ndarray):
+def render(patches, intr: Intrinsics, w: int, h: int, cam_to_ref: np.ndarray, antialias: bool = False):
     """Ray-cast the patches.  ``cam_to_ref`` (3x4) is the rendering camera's pose in the scene
-    (keyframe) frame.  Returns (image float64 [h,w] before noise, depth z in this camera [h,w])."""
+    (keyframe) frame.  Returns (image float64 [h,w] before noise, depth z in this camera [h,w]).
+    ``antialias``: band-limit the texture to each pixel's footprint on the surface."""
     R = cam_to_ref[:, :3]
     o = cam_to_ref[:, 3]
     xs = (np.arange(w, dtype=np.float64) - intr.cx) / intr.fx
@@ -225,7 +234,12 @@ def render(patches, intr: Intrinsics, w: int, h: int, cam_to_ref: np.ndarray):
             hit &= (np.abs(a) <= p.half[0]) & (np.abs(b) <= p.half[1])
         if not np.any(hit):
             continue
-        tex = value_noise(a[hit], b[hit], p.tex_seed, 4, p.tex_freq)
+        fp = None
+        if antialias:
+            # footprint of one pixel on the plane: ray length / focal length / |cos incidence|
+            dn = np.abs(denom[hit]) / np.linalg.norm(dirs[hit], axis=-1)
+            fp = (t[hit] * np.linalg.norm(dirs[hit], axis=-1)) / (intr.fx * np.maximum(dn, 0.05))
+        tex = value_noise(a[hit], b[hit], p.tex_seed, 4, p.tex_freq, fp)
         tex = np.clip(0.5 + (tex - 0.5) * 2.2 * p.contrast, 0.0, 1.0) * 255.0
         img[hit] = tex
         best_t[hit] = t[hit]
@@ -416,3 +430,125 @@ def refine_problem(seed: int = 0, w: int = BASE_W, h: int = BASE_H, n_frames: in
     var = np.where(sel, (rel_noise * s.key_true_idepth) ** 2, -1.0)
     return RefineProblem(w, h, s.intr, s.key_image, idepth.astype(np.float32), var.astype(np.float32),
                          s.key_true_idepth, list(s.ref_images), [pose_inv(T) for T in s.ref_frame_to_key])
+
+
+# ----------------------------------------------------------------------------------------------
+# A room sequence: 20 textured planes, a closed cubic-spline camera path (full SLAM runs)
+# ----------------------------------------------------------------------------------------------
+
+@dataclasses.dataclass
+class RoomSequence:
+    """Frames of a camera moving through a room; world frame: x right, y down, z forward of the
+    room, origin at the room centre (the camera convention, so the first pose is near identity)."""
+    w: int
+    h: int
+    intr: Intrinsics
+    fps: float
+    patches: list
+    cam_to_world: np.ndarray   # (n, 3, 4) ground-truth camera poses
+    first_depth: np.ndarray    # float64 [h, w]: z-depth of frame 0 (bootstraps the first keyframe)
+    depths: np.ndarray = None  # float32 (n, h, w) z-depth of every frame (keep_depths=True)
+
+    @property
+    def n(self) -> int:
+        return len(self.cam_to_world)
+
+
+def make_room(rng: np.random.Generator, size=(8.0, 3.0, 6.0), n_panels: int = 14):
+    """6 walls of a box room plus ``n_panels`` vertical panels standing in front of the walls,
+    all textured with value noise: 20 planes for the default panel count."""
+    sx, sy, sz = size[0] / 2, size[1] / 2, size[2] / 2
+    patches = []
+
+    def add(centre, normal, e1, half, freq):
+        n = np.asarray(normal, np.float64)
+        patches.append(Patch(np.asarray(centre, np.float64), n / np.linalg.norm(n), np.asarray(e1, np.float64),
+                             np.cross(n / np.linalg.norm(n), np.asarray(e1, np.float64)), half,
+                             int(rng.integers(1 << 30)), freq, float(rng.uniform(0.75, 0.85)), 0.0))
+
+    ex, ey, ez = np.eye(3)
+    add([sx, 0, 0], -ex, ez, (sz, sy), float(rng.uniform(3.0, 3.6)))    # walls (normals point inward)
+    add([-sx, 0, 0], ex, ez, (sz, sy), float(rng.uniform(3.0, 3.6)))
+    add([0, 0, sz], -ez, ex, (sx, sy), float(rng.uniform(3.0, 3.6)))
+    add([0, 0, -sz], ez, ex, (sx, sy), float(rng.uniform(3.0, 3.6)))
+    add([0, sy, 0], -ey, ex, (sx, sz), float(rng.uniform(3.0, 3.6)))    # floor (y down)
+    add([0, -sy, 0], ey, ex, (sx, sz), float(rng.uniform(3.0, 3.6)))    # ceiling
+    for _ in range(n_panels):
+        ang = rng.uniform(0, 2 * math.pi)
+        # a point on an ellipse between the path (radius <= 1.5 m) and the walls, so that every
+        # surface stays >= ~1.3 m from the camera (inside the depth filter's default idepth range)
+        r = rng.uniform(0.78, 0.92)
+        c = np.array([math.cos(ang) * sx * r, rng.uniform(-0.6, 0.6), math.sin(ang) * sz * r])
+        yaw = ang + math.pi + rng.uniform(-0.5, 0.5)                      # roughly facing the centre
+        n = np.array([math.cos(yaw), 0.0, math.sin(yaw)])
+        e1 = np.cross(ey, n)
+        add(c, n, e1 / np.linalg.norm(e1), (float(rng.uniform(0.3, 0.7)), float(rng.uniform(0.3, 0.8))),
+            float(rng.uniform(3.6, 4.4)))
+    return patches
+
+
+def room_path(rng: np.random.Generator, n_frames: int, fps: float = 30.0, speed: float = 0.5,
+              radius=(1.5, 0.9), look_yaw_deg: float = 35.0):
+    """Camera poses along a closed periodic cubic spline through 8 jittered points of an ellipse
+    around the room centre, traversed at constant speed; the camera looks outwards, turned
+    `look_yaw_deg` towards the direction of travel, with a small pitch."""
+    from scipy.interpolate import CubicSpline
+
+    k = 8
+    phis = np.arange(k) * 2 * math.pi / k + rng.uniform(-0.15, 0.15, k)
+    pts = np.stack([radius[0] * np.cos(phis) * rng.uniform(0.9, 1.1, k), rng.uniform(-0.15, 0.15, k),
+                    radius[1] * np.sin(phis) * rng.uniform(0.9, 1.1, k)], 1)
+    pts = np.vstack([pts, pts[:1]])
+    s = np.concatenate([[0.0], np.cumsum(np.linalg.norm(np.diff(pts, axis=0), axis=1))])
+    spline = CubicSpline(s, pts, bc_type="periodic")
+    # arc-length table for constant speed
+    ss = np.linspace(0, s[-1], 20001)
+    d = np.concatenate([[0.0], np.cumsum(np.linalg.norm(np.diff(spline(ss), axis=0), axis=1))])
+    dist = (np.arange(n_frames) * speed / fps) % d[-1]
+    u = np.interp(dist, d, ss)
+    P = spline(u)
+    V = spline(u, 1)
+    out = np.zeros((n_frames, 3, 4))
+    ey = np.array([0.0, 1.0, 0.0])
+    for i in range(n_frames):
+        outward = np.array([P[i, 0], 0.0, P[i, 2]])
+        outward /= np.linalg.norm(outward)
+        vel = np.array([V[i, 0], 0.0, V[i, 2]])
+        vel /= np.linalg.norm(vel)
+        a = math.radians(look_yaw_deg)
+        fwd = math.cos(a) * outward + math.sin(a) * vel
+        fwd[1] = 0.08 * math.sin(2 * math.pi * i / 400.0)
+        z = fwd / np.linalg.norm(fwd)
+        x = np.cross(ey, z)
+        x /= np.linalg.norm(x)
+        y = np.cross(z, x)
+        out[i, :, :3] = np.stack([x, y, z], 1)   # columns: camera axes in the world
+        out[i, :, 3] = P[i]
+    return out
+
+
+def _render_u8(args):
+    patches, intr, w, h, T, seed, noise_sigma = args
+    img, depth = render(patches, intr, w, h, T, antialias=True)
+    rng = np.random.default_rng(seed)
+    return np.clip(np.rint(img + rng.normal(0.0, noise_sigma, img.shape)), 0, 255).astype(np.uint8), depth
+
+
+def room_sequence(seed: int = 0, n_frames: int = 1000, w: int = BASE_W, h: int = BASE_H, fps: float = 30.0,
+                  speed: float = 0.5, noise_sigma: float = 2.0, workers: int = 1, keep_depths: bool = False):
+    """(RoomSequence, frames uint8 (n, h, w)).  Rendering takes a while at 640x480: pass
+    `workers` > 1 to render in a process pool (created with the spawn method)."""
+    rng = np.random.default_rng(seed)
+    intr = Intrinsics.for_size(w, h)
+    patches = make_room(rng)
+    poses = room_path(rng, n_frames, fps, speed)
+    jobs = [(patches, intr, w, h, poses[i], seed * 100003 + i, noise_sigma) for i in range(n_frames)]
+    if workers > 1:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.map(_render_u8, jobs, chunksize=4)
+    else:
+        res = [_render_u8(j) for j in jobs]
+    frames = np.stack([r[0] for r in res])
+    depths = np.stack([r[1].astype(np.float32) for r in res]) if keep_depths else None
+    return RoomSequence(w, h, intr, fps, patches, poses, res[0][1], depths), frames

@@ -141,3 +141,26 @@ def test_sim3_argument_checks(ctx):
     with pytest.raises(lsdg.LsdgError):
         b.load_sim3(*lsdg.pack_sim3_pairs([sp]), np.zeros((1, 13)))
     b.close()
+
+
+def test_sim3_batch_from_resident_frames_equals_host_load(ctx):
+    """lsdg_batch_load_frames (device-to-device from resident keyframes) gives the results of the
+    host upload bit for bit."""
+    import lsdg
+    sps = [spair(s, 320, 240) for s in range(3)]
+    init = np.tile(np.concatenate([np.eye(3).ravel(), np.zeros(3), [1.0]]), (3, 1))
+    b = lsdg.Batch(ctx, [320] * 3, [240] * 3, [q.intr for q in sps], sim3=True)
+    try:
+        b.load_sim3(*lsdg.pack_sim3_pairs(sps), init)
+        b.run()
+        ref, _ = b.read()
+        pairs = [frames(ctx, q) for q in sps]
+        b.load_frames([p[0] for p in pairs], [p[1] for p in pairs], init)
+        b.run()
+        got, stats = b.read()
+        np.testing.assert_array_equal(got, ref)
+        with pytest.raises(lsdg.LsdgError):
+            b.load_frames([pairs[0][0]] * 3, [lsdg.Frame(ctx, 320, 240, sps[0].intr).upload(sps[0].new_image)] * 3,
+                          init)   # Sim3 frames need depth
+    finally:
+        b.close()
