@@ -354,6 +354,11 @@ LSDG_API lsdg_status lsdg_batch_timing(lsdg_ctx* ctx, lsdg_batch* batch, float* 
  * in the persistent grid) and the kernel launches one lsdg_batch_run issues. */
 LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* threads, int* minblocks, int* cluster,
                                       int* clusters, int* launches_per_run);
+/* The coarse phase of the batch's plan: levels [top, split] run first with each pair on a cluster of
+ * `cluster` CTAs of `threads`, then the finer levels with the shape lsdg_batch_shape reports
+ * (split = -1: a single launch over all levels). */
+LSDG_API lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* batch, int* split, int* threads, int* minblocks,
+                                      int* cluster);
 /* Residual passes the last lsdg_batch_run executed, summed over pairs and levels, and the
  * algorithmic bytes those passes read (points + frame levels + sums). */
 LSDG_API lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* batch, int64_t* passes,

@@ -339,11 +339,87 @@ TrackArgs make_track_args(const lsdg_params& p) {
 // cluster (the cluster owns one pair).
 static const int kCandCluster[] = {2, 4, 8, 16};
 
-lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc, bool sim3) {
-  int n_clusters = std::min(a.n_pairs, std::max(1, tc.max_clusters));
+static lsdg_status launch_phase(lsdg_ctx* ctx, const TrackArgs& a, int threads, int minblocks, int cluster,
+                                int max_clusters, bool sim3) {
+  const int n_clusters = std::min(a.n_pairs, std::max(1, max_clusters));
   CK(ctx, cudaMemsetAsync(a.work_counter, 0, sizeof(int), ctx->stream));
-  CK(ctx, launch_track(a, tc.threads, tc.minblocks, tc.cluster, n_clusters, ctx->stream, sim3));
+  CK(ctx, launch_track(a, threads, minblocks, cluster, n_clusters, ctx->stream, sim3));
   ctx->launches += 1;
+  return LSDG_OK;
+}
+
+static bool use_split(const TrackArgs& a, const TuneChoice& tc, const double* mid) {
+  return tc.split >= 1 && mid && a.top_level >= tc.split && a.bottom_level < tc.split;
+}
+
+// The two phases of a split run: coarse levels [top, split] (out_pose -> mid), then the finer
+// levels from those poses, continuing each pair's pass counts.
+static void split_args(const TrackArgs& a, int split, double* mid, TrackArgs* a1, TrackArgs* a2) {
+  *a1 = a;
+  a1->bottom_level = split;
+  a1->out_pose = mid;
+  a1->out_sums = nullptr;
+  a1->accumulate_stats = 0;
+  *a2 = a;
+  a2->top_level = split - 1;
+  a2->init = mid;
+  a2->init_is_ref_to_frame = 0;
+  a2->accumulate_stats = 1;
+}
+
+lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc, bool sim3, double* mid) {
+  if (use_split(a, tc, mid)) {
+    TrackArgs a1, a2;
+    split_args(a, tc.split, mid, &a1, &a2);
+    lsdg_status st = launch_phase(ctx, a1, tc.c_threads, tc.c_minblocks, tc.c_cluster, tc.c_max_clusters, sim3);
+    if (st != LSDG_OK) return st;
+    return launch_phase(ctx, a2, tc.threads, tc.minblocks, tc.cluster, tc.max_clusters, sim3);
+  }
+  return launch_phase(ctx, a, tc.threads, tc.minblocks, tc.cluster, tc.max_clusters, sim3);
+}
+
+// Times one launch shape on `a` (best of two runs).
+static lsdg_status time_phase(lsdg_ctx* ctx, const TrackArgs& a, int nt, int mb, int c, int mc, bool sim3,
+                              cudaEvent_t e0, cudaEvent_t e1, float* ms_out) {
+  float t_best = 1e30f;
+  for (int rep = 0; rep < 2; ++rep) {
+    CK(ctx, cudaEventRecord(e0, ctx->stream));
+    lsdg_status st = launch_phase(ctx, a, nt, mb, c, mc, sim3);
+    if (st != LSDG_OK) return st;
+    CK(ctx, cudaEventRecord(e1, ctx->stream));
+    CK(ctx, cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(ctx, cudaEventElapsedTime(&ms, e0, e1));
+    t_best = std::min(t_best, ms);
+  }
+  *ms_out = t_best;
+  return LSDG_OK;
+}
+
+// Best shape over the candidates for one phase; clusters: the cluster sizes to try.
+static lsdg_status best_phase(lsdg_ctx* ctx, const TrackArgs& a, const int* clusters, int n_clusters, bool sim3,
+                              cudaEvent_t e0, cudaEvent_t e1, int* nt_o, int* mb_o, int* c_o, int* mc_o,
+                              float* ms_o) {
+  *ms_o = 1e30f;
+  *nt_o = 0;
+  for (int si = 0; si < track_shape_count(); ++si)
+    for (int k = 0; k < n_clusters; ++k) {
+      int nt = 0, mb = 0;
+      track_shape(si, &nt, &mb);
+      const int c = clusters[k];
+      const int mc = track_max_clusters(nt, mb, c, sim3);
+      if (mc <= 0) continue;
+      float ms = 0;
+      lsdg_status st = time_phase(ctx, a, nt, mb, c, mc, sim3, e0, e1, &ms);
+      if (st != LSDG_OK) return st;
+      if (ms < *ms_o) {
+        *ms_o = ms;
+        *nt_o = nt;
+        *mb_o = mb;
+        *c_o = c;
+        *mc_o = mc;
+      }
+    }
   return LSDG_OK;
 }
 
@@ -351,7 +427,14 @@ lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc,
 // caller's own data (two runs each, best kept).  The choice is cached per context.
 // The environment variable LSDG_TRACK_SHAPE="threads,cluster" pins the shape instead (used to
 // profile one known configuration); it is ignored when that shape does not fit the device.
-lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, TuneChoice* out, bool sim3) {
+// Picks the tracker's launch plan for a workload signature by timing candidates on the caller's
+// own data (two runs each, best kept): the best single launch over all levels, and, when the caller
+// provides pose scratch, split runs (coarse levels first with each pair on a cluster of 1 or 2 CTAs,
+// then the finer levels with their own best shape).  The fastest plan is cached per context.
+// LSDG_TRACK_SHAPE="threads,cluster[,minblocks]" pins a single-launch shape;
+// LSDG_TRACK_SPLIT="split,threads,cluster[,minblocks]" adds a pinned coarse phase to it.
+lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, TuneChoice* out, bool sim3,
+                     double* mid) {
   auto it = ctx->tune_cache.find(key);
   if (it != ctx->tune_cache.end()) {
     *out = it->second;
@@ -362,7 +445,23 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
     if (std::sscanf(env, "%d,%d,%d", &nt, &c, &mb) >= 2) {
       int mc = track_max_clusters(nt, mb, c, sim3);
       if (mc > 0) {
-        TuneChoice tc{nt, mb, c, mc, 0.f};
+        TuneChoice tc;
+        tc.threads = nt;
+        tc.minblocks = mb;
+        tc.cluster = c;
+        tc.max_clusters = mc;
+        const char* sp = std::getenv("LSDG_TRACK_SPLIT");
+        int s = -1, cnt = 0, cc = 0, cmb = 1;
+        if (sp && mid && std::sscanf(sp, "%d,%d,%d,%d", &s, &cnt, &cc, &cmb) >= 3) {
+          const int cmc = track_max_clusters(cnt, cmb, cc, sim3);
+          if (cmc > 0 && s >= 1) {
+            tc.split = s;
+            tc.c_threads = cnt;
+            tc.c_minblocks = cmb;
+            tc.c_cluster = cc;
+            tc.c_max_clusters = cmc;
+          }
+        }
         ctx->tune_cache[key] = tc;
         *out = tc;
         return LSDG_OK;
@@ -373,34 +472,45 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
   CK(ctx, cudaEventCreate(&e0));
   CK(ctx, cudaEventCreate(&e1));
   TuneChoice best;
-  best.threads = 0;
-  float best_ms = 1e30f;
-  for (int si = 0; si < track_shape_count(); ++si)
-    for (int c : kCandCluster) {
-      int nt = 0, mb = 0;
-      track_shape(si, &nt, &mb);
-      int mc = track_max_clusters(nt, mb, c, sim3);
-      if (mc <= 0) continue;
-      TuneChoice tc{nt, mb, c, mc, 0.f};
-      float t_best = 1e30f;
-      for (int rep = 0; rep < 2; ++rep) {
-        CK(ctx, cudaEventRecord(e0, ctx->stream));
-        lsdg_status st = run_tracker(ctx, a, tc, sim3);
-        if (st != LSDG_OK) return st;
-        CK(ctx, cudaEventRecord(e1, ctx->stream));
-        CK(ctx, cudaEventSynchronize(e1));
-        float ms = 0;
-        CK(ctx, cudaEventElapsedTime(&ms, e0, e1));
-        t_best = std::min(t_best, ms);
-      }
-      if (t_best < best_ms) {
-        best_ms = t_best;
-        best = tc;
-      }
+  int nt = 0, mb = 0, c = 0, mc = 0;
+  float best_ms = 0;
+  lsdg_status st = best_phase(ctx, a, kCandCluster, 4, sim3, e0, e1, &nt, &mb, &c, &mc, &best_ms);
+  if (st == LSDG_OK && nt == 0) st = ctx_fail(ctx, LSDG_NOT_SUPPORTED, "no cluster launch shape fits this device");
+  if (st == LSDG_OK) {
+    best.threads = nt;
+    best.minblocks = mb;
+    best.cluster = c;
+    best.max_clusters = mc;
+    best.split = -1;
+  }
+  static const int kCoarseCluster[] = {1, 2};
+  for (int split = 2; st == LSDG_OK && mid && split >= 1; --split) {
+    if (!(a.top_level >= split && a.bottom_level < split)) continue;
+    TrackArgs a1, a2;
+    split_args(a, split, mid, &a1, &a2);
+    int cnt = 0, cmb = 0, cc = 0, cmc = 0, fnt = 0, fmb = 0, fc = 0, fmc = 0;
+    float cms = 0, fms = 0;
+    st = best_phase(ctx, a1, kCoarseCluster, 2, sim3, e0, e1, &cnt, &cmb, &cc, &cmc, &cms);
+    if (st != LSDG_OK || cnt == 0) break;
+    st = launch_phase(ctx, a1, cnt, cmb, cc, cmc, sim3);  // the coarse poses the fine phase starts from
+    if (st == LSDG_OK) st = best_phase(ctx, a2, kCandCluster, 4, sim3, e0, e1, &fnt, &fmb, &fc, &fmc, &fms);
+    if (st != LSDG_OK || fnt == 0) break;
+    if (cms + fms < best_ms) {
+      best_ms = cms + fms;
+      best.threads = fnt;
+      best.minblocks = fmb;
+      best.cluster = fc;
+      best.max_clusters = fmc;
+      best.split = split;
+      best.c_threads = cnt;
+      best.c_minblocks = cmb;
+      best.c_cluster = cc;
+      best.c_max_clusters = cmc;
     }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (best.threads == 0) return ctx_fail(ctx, LSDG_NOT_SUPPORTED, "no cluster launch shape fits this device");
+  if (st != LSDG_OK) return st;
   best.tuned_ms = best_ms;
   ctx->tune_cache[key] = best;
   *out = best;

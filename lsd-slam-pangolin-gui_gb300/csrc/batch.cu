@@ -47,6 +47,7 @@ struct BatchSlot {
   double* d_out = nullptr;
   lsdg_track_stats* d_stats = nullptr;
   int* d_work = nullptr;
+  double* d_mid = nullptr;            // coarse-phase poses of a split run
   double* h_out = nullptr;            // pinned staging of the results
   lsdg_track_stats* h_stats = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -87,6 +88,7 @@ static void slot_free(BatchSlot& s) {
   if (s.d_out) cudaFree(s.d_out);
   if (s.d_stats) cudaFree(s.d_stats);
   if (s.d_work) cudaFree(s.d_work);
+  if (s.d_mid) cudaFree(s.d_mid);
   if (s.h_out) cudaFreeHost(s.h_out);
   if (s.h_stats) cudaFreeHost(s.h_stats);
   for (auto& e : s.ev)
@@ -128,6 +130,7 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   if (e == cudaSuccess) e = cudaMalloc(&s.d_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_stats, sizeof(lsdg_track_stats) * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_work, sizeof(int) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_mid, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_stats, sizeof(lsdg_track_stats) * n);
   for (auto& ev : s.ev)
@@ -183,7 +186,7 @@ static lsdg_status slot_run(lsdg_ctx* ctx, lsdg_batch* b, int si) {
       lsdg_status st = enqueue_build(ctx, b, s, &k);
       if (st != LSDG_OK) return st;
       ctx->launches += k;
-      st = autotune(ctx, b->key, a, &b->tc, b->sim3);
+      st = autotune(ctx, b->key, a, &b->tc, b->sim3, s.d_mid);
       if (st != LSDG_OK) return st;
       b->tune_epoch = ctx->params_epoch;
     }
@@ -195,7 +198,7 @@ static lsdg_status slot_run(lsdg_ctx* ctx, lsdg_batch* b, int si) {
     lsdg_status st = enqueue_build(ctx, b, s, &nl);
     cudaEventRecordWithFlags(s.ev[1], ctx->stream, cudaEventRecordExternal);
     int64_t before = ctx->launches;
-    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc, b->sim3);
+    if (st == LSDG_OK) st = run_tracker(ctx, a, b->tc, b->sim3, s.d_mid);
     nl += (int)(ctx->launches - before);
     ctx->launches = before;
     cudaEventRecordWithFlags(s.ev[2], ctx->stream, cudaEventRecordExternal);
@@ -529,6 +532,16 @@ lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* b, int64_t* passes, doubl
   if (passes) *passes = np;
   if (pass_bytes) *pass_bytes = pb;
   if (unique_bytes) *unique_bytes = ub;
+  return LSDG_OK;
+}
+
+// The coarse phase of the autotuner's plan for this batch (split = -1: one launch).
+lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* b, int* split, int* threads, int* minblocks, int* cluster) {
+  if (!ctx || !b) return LSDG_INVALID_ARG;
+  if (split) *split = b->tc.split;
+  if (threads) *threads = b->tc.c_threads;
+  if (minblocks) *minblocks = b->tc.c_minblocks;
+  if (cluster) *cluster = b->tc.c_cluster;
   return LSDG_OK;
 }
 

@@ -17,6 +17,10 @@ struct TuneChoice {
   int cluster = 8;
   int max_clusters = 1;
   float tuned_ms = 0.f;
+  // split run: levels [top, split] first, each pair on a small cluster (c_*), then the finer levels
+  // with the shape above starting from the coarse poses; split = -1: one launch over all levels
+  int split = -1;
+  int c_threads = 256, c_minblocks = 2, c_cluster = 1, c_max_clusters = 1;
 };
 
 struct lsdg_ctx {
@@ -64,5 +68,8 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
                            const bool* depth, int levels, bool grads);
 void frameset_free(FrameSet& fs);
 lsdg::TrackArgs make_track_args(const lsdg_params& p);
-lsdg_status run_tracker(lsdg_ctx* ctx, const lsdg::TrackArgs& a, const TuneChoice& tc, bool sim3);
-lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const lsdg::TrackArgs& a, TuneChoice* out, bool sim3);
+// mid: device scratch of one pose per pair (12 or 13 doubles) for a split run; nullptr = one launch
+lsdg_status run_tracker(lsdg_ctx* ctx, const lsdg::TrackArgs& a, const TuneChoice& tc, bool sim3,
+                        double* mid = nullptr);
+lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const lsdg::TrackArgs& a, TuneChoice* out, bool sim3,
+                     double* mid = nullptr);

@@ -66,6 +66,7 @@ struct TrackArgs {
   float photometric_variance, huber_delta, min_z, border_margin, sim3_depth_variance, sim3_depth_weight;
   double lambda0, lambda_up, lambda_down, step_eps, stall_eps;
   float min_good_ratio, min_usage;
+  int accumulate_stats;      // continue the pass counts already in out_stats (second phase of a split run)
 };
 
 // Kahan-compensated float sum (value = s - c) and the merge of two of them (an exact TwoSum of the

@@ -441,8 +441,12 @@ __device__ __noinline__ void fetch_pair(const TrackArgs& a, LMState& lm, Ctl& ct
     lm.E = 0;
     lm.lambda = a.lambda0;
     for (int i = 0; i < kMaxRec; ++i) lm.S[i] = 0;
-    char* sp = reinterpret_cast<char*>(&lm.st);
-    for (int i = 0; i < (int)sizeof(lsdg_track_stats); ++i) sp[i] = 0;
+    if (a.accumulate_stats) {
+      lm.st = a.out_stats[p];  // the coarse levels' pass counts, from the first phase
+    } else {
+      char* sp = reinterpret_cast<char*>(&lm.st);
+      for (int i = 0; i < (int)sizeof(lsdg_track_stats); ++i) sp[i] = 0;
+    }
     const double* in = a.init + (size_t)Md::POSE * p;
     double Tin[12];
     if (SIM3) {  // {R, t, s} -> [sR | t]

@@ -85,6 +85,7 @@ def lib():
     _sig(L, "lsdg_batch_collect", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
+    _sig(L, "lsdg_batch_split", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 4)
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
     _sig(L, "lsdg_depth_create", st, [_vp, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
     _sig(L, "lsdg_depth_destroy", st, [_vp, _vp])
@@ -435,8 +436,15 @@ class Batch:
         t, mb, c, n, k = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_int()
         self.ctx.check(lib().lsdg_batch_shape(self.ctx.handle, self._h, C.byref(t), C.byref(mb), C.byref(c), C.byref(n),
                                               C.byref(k)))
-        return {"threads": t.value, "minblocks": mb.value, "cluster": c.value, "clusters": n.value,
-                "launches_per_run": k.value}
+        sp, ct, cm, cc = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self.ctx.check(lib().lsdg_batch_split(self.ctx.handle, self._h, C.byref(sp), C.byref(ct), C.byref(cm),
+                                              C.byref(cc)))
+        out = {"threads": t.value, "minblocks": mb.value, "cluster": c.value, "clusters": n.value,
+               "launches_per_run": k.value}
+        if sp.value >= 0:
+            out["coarse_phase"] = {"levels_from": sp.value, "threads": ct.value, "minblocks": cm.value,
+                                   "cluster": cc.value}
+        return out
 
     def work(self):
         p, b, u = C.c_int64(), C.c_double(), C.c_double()
