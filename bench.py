@@ -165,7 +165,9 @@ def run_profile(args):
         batch.run()
     out, stats = batch.read()
     b_ms, t_ms = batch.timing()
+    per_level = [float(np.mean([s.passes[l] for s in stats])) for l in range(5)]
     print(json.dumps({"profile_pairs": len(pairs), "shape": batch.shape(), "passes": batch.work()[0],
+                      "mean_passes_per_level": per_level, "mean_points_level0": float(np.mean([s.n_points for s in stats])),
                       "build_ms": b_ms, "track_ms": t_ms, "tune": ctx.tune_table()}))
     batch.close()
     ctx.close()

@@ -689,6 +689,99 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
     for (int i = 0; i < D; ++i) { gs[i] = 0.f; gc[i] = 0.f; }
     int good = 0, bad = 0, oob = 0;
 
+    if (!SIM3) {
+      // SE3: two points per iteration, each evaluated without branches (a point that sits out gathers
+      // a clamped in-frame cell and gets zero weight), so both points' 32 gathers are in flight
+      // together and one add per sum takes both products.  The level's first pass freezes 1/sigma^2
+      // in psig, so later passes divide nothing; inliers take no square root.  A thread sums a few
+      // dozen points per pass: the 21 Hessian sums (all terms of one sign on the diagonal, and only
+      // the curvature of the step) are plain float sums there, the gradient and the energy (whose
+      // terms cancel, and whose differences decide LM steps) stay compensated; every merge across
+      // threads, warps and CTAs is compensated.
+      const int stride = (int)C * NT;
+      const float d2 = delta * delta;
+      auto eval = [&](int k, float (&J)[D], float& wgt, float& res, float& rho) {
+        const bool in = k < n;
+        const int kk = in ? k : 0;
+        const float sig = first ? 1.f : psig[kk];
+        const bool act = in && sig > 0.f;
+        const float4 p = __ldg(&pts[kk]);
+        const float X = p.x, Y = p.y, Z = p.z, Ik = p.w;
+        const float Rpx = (R00 * X + R01 * Y) + R02 * Z;
+        const float Rpy = (R10 * X + R11 * Y) + R12 * Z;
+        const float Rpz = (R20 * X + R21 * Y) + R22 * Z;
+        const float Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
+        const bool zok = Zp > minz;
+        const float iz = 1.0f / (zok ? Zp : 1.f);
+        const float u = fx * (Xp * iz) + cx;
+        const float v = fy * (Yp * iz) + cy;
+        const bool bok = first ? (u >= ulo && v >= vlo && u < uhi && v < vhi)
+                               : (u >= 1.f && v >= 1.f && u < umax && v < vmax);
+        const bool ok = act && zok && bok;
+        if (act && !ok) {
+          ++oob;
+          if (first) psig[k] = 0.f;
+        }
+        const float uc = ok ? u : 1.f, vc = ok ? v : 1.f;
+        const int ix = (int)uc, iy = (int)vc;
+        const float ax = uc - (float)ix, ay = vc - (float)iy;
+        float wx[4], dxw[4], wy[4], dyw[4];
+        catmull_rom(ax, wx, dxw);
+        catmull_rom(ay, wy, dyw);
+        float rI[4], rD[4];
+        const float* q = img + (size_t)(iy - 1) * w + (ix - 1);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float i0 = __ldg(q), i1 = __ldg(q + 1), i2 = __ldg(q + 2), i3 = __ldg(q + 3);
+          rI[j] = ((wx[0] * i0 + wx[1] * i1) + wx[2] * i2) + wx[3] * i3;
+          rD[j] = ((dxw[0] * i0 + dxw[1] * i1) + dxw[2] * i2) + dxw[3] * i3;
+          q += w;
+        }
+        const float In = ((wy[0] * rI[0] + wy[1] * rI[1]) + wy[2] * rI[2]) + wy[3] * rI[3];
+        const float Gx = ((wy[0] * rD[0] + wy[1] * rD[1]) + wy[2] * rD[2]) + wy[3] * rD[3];
+        const float Gy = ((dyw[0] * rI[0] + dyw[1] * rI[1]) + dyw[2] * rI[2]) + dyw[3] * rI[3];
+        const float r = In - Ik;
+        const float a0 = (Gx * fx) * iz, a1 = (Gy * fy) * iz;
+        const float a2 = -((a0 * Xp + a1 * Yp) * iz);
+        float isig = sig;
+        if (first) {
+          const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
+          isig = 1.0f / (pvr + (drd * drd) * __ldg(&pvar[kk]));
+          if (ok) psig[k] = isig;
+        }
+        const float e2 = (r * r) * isig;
+        const bool inl = e2 <= d2;
+        const float ir = rsqrtf(e2);
+        good += (ok && inl) ? 1 : 0;
+        bad += (ok && !inl) ? 1 : 0;
+        wgt = ok ? (inl ? isig : (delta * ir) * isig) : 0.f;
+        rho = ok ? (inl ? e2 : delta * (2.f * (e2 * ir) - delta)) : 0.f;
+        res = ok ? r : 0.f;
+        J[0] = ok ? a0 : 0.f;
+        J[1] = ok ? a1 : 0.f;
+        J[2] = ok ? a2 : 0.f;
+        J[3] = ok ? Yp * a2 - Zp * a1 : 0.f;
+        J[4] = ok ? Zp * a0 - Xp * a2 : 0.f;
+        J[5] = ok ? Xp * a1 - Yp * a0 : 0.f;
+      };
+      for (int k = (int)rank * NT + tid; k < n; k += 2 * stride) {
+        float Ja[D], Jb[D], wa, wb, ra, rb, ea, eb;
+        eval(k, Ja, wa, ra, ea);
+        eval(k + stride, Jb, wb, rb, eb);
+        float wJa[D], wJb[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) { wJa[i] = wa * Ja[i]; wJb[i] = wb * Jb[i]; }
+        int q2 = 0;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = i; j < D; ++j) { hs[q2] += wJa[i] * Ja[j] + wJb[i] * Jb[j]; ++q2; }
+#pragma unroll
+        for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJa[i] * ra + wJb[i] * rb);
+        kadd(es, ec, ea + eb);
+      }
+    }
+    if (SIM3)
     for (int k = (int)rank * NT + tid; k < n; k += (int)C * NT) {
       float s2 = 0.f;
       if (!first) {
@@ -766,16 +859,7 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
       float wJ[D];
 #pragma unroll
       for (int i = 0; i < D; ++i) wJ[i] = wgt * J[i];
-      if (!SIM3) {
-        int q2 = 0;
-#pragma unroll
-        for (int i = 0; i < D; ++i)
-#pragma unroll
-          for (int j = i; j < D; ++j) { kadd(hs[q2], hc[q2], wJ[i] * J[j]); ++q2; }
-#pragma unroll
-        for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJ[i] * r);
-        kadd(es, ec, rho);
-      } else {
+      {
         // inverse-depth residual against the other keyframe's depth map (4 valid bilinear corners)
         float Jd[D], rd = 0.f, wgd = 0.f, rhod = 0.f;
 #pragma unroll

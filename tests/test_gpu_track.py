@@ -1,9 +1,10 @@
 """GPU parity of the direct-alignment path (through the C-ABI) against the CPU oracle.
 
 Bars: pyramids, depth pyramids and reference points bit-exact (integer-like float work with the
-same operation order); normal-equation sums within 1e-5 relative (only the summation order
-differs, both sides Kahan-compensated); final poses within 1e-4 rad / 1e-4 m of the FP64 oracle
-and 1e-5 of the float oracle."""
+same operation order); normal-equation sums within 1e-4 relative (the summation order differs;
+the oracle compensates every sum, the kernel its merges and the per-thread gradient and energy
+sums, its per-thread Hessian sums run over a few dozen points); final poses within 1e-4 rad /
+1e-4 m of the FP64 oracle and 1e-5 of the float oracle."""
 import numpy as np
 import pytest
 
