@@ -429,7 +429,7 @@ static lsdg_status best_phase(lsdg_ctx* ctx, const TrackArgs& a, const int* clus
 // profile one known configuration); it is ignored when that shape does not fit the device.
 // Picks the tracker's launch plan for a workload signature by timing candidates on the caller's
 // own data (two runs each, best kept): the best single launch over all levels, and, when the caller
-// provides pose scratch, split runs (coarse levels first with each pair on a cluster of 1 or 2 CTAs,
+// provides pose scratch, split runs (coarse levels first with each pair on a cluster of 1, 2 or 4 CTAs,
 // then the finer levels with their own best shape).  The fastest plan is cached per context.
 // LSDG_TRACK_SHAPE="threads,cluster[,minblocks]" pins a single-launch shape;
 // LSDG_TRACK_SPLIT="split,threads,cluster[,minblocks]" adds a pinned coarse phase to it.
@@ -483,14 +483,14 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
     best.max_clusters = mc;
     best.split = -1;
   }
-  static const int kCoarseCluster[] = {1, 2};
+  static const int kCoarseCluster[] = {1, 2, 4};
   for (int split = 2; st == LSDG_OK && mid && split >= 1; --split) {
     if (!(a.top_level >= split && a.bottom_level < split)) continue;
     TrackArgs a1, a2;
     split_args(a, split, mid, &a1, &a2);
     int cnt = 0, cmb = 0, cc = 0, cmc = 0, fnt = 0, fmb = 0, fc = 0, fmc = 0;
     float cms = 0, fms = 0;
-    st = best_phase(ctx, a1, kCoarseCluster, 2, sim3, e0, e1, &cnt, &cmb, &cc, &cmc, &cms);
+    st = best_phase(ctx, a1, kCoarseCluster, 3, sim3, e0, e1, &cnt, &cmb, &cc, &cmc, &cms);
     if (st != LSDG_OK || cnt == 0) break;
     st = launch_phase(ctx, a1, cnt, cmb, cc, cmc, sim3);  // the coarse poses the fine phase starts from
     if (st == LSDG_OK) st = best_phase(ctx, a2, kCandCluster, 4, sim3, e0, e1, &fnt, &fmb, &fc, &fmc, &fms);

@@ -64,7 +64,7 @@ struct TrackArgs {
   int bottom_level;          // last level to run
   int max_iter[kMaxLevels];
   float photometric_variance, huber_delta, min_z, border_margin, sim3_depth_variance, sim3_depth_weight;
-  double lambda0, lambda_up, lambda_down, step_eps, stall_eps;
+  float lambda0, lambda_up, lambda_down, step_eps, stall_eps;  // the LM schedule runs in float
   float min_good_ratio, min_usage;
   int accumulate_stats;      // continue the pass counts already in out_stats (second phase of a split run)
 };

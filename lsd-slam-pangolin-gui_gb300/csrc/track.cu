@@ -78,15 +78,20 @@ struct CtaPart {
 
 enum { PH_INIT = 0, PH_TRY = 1 };
 
+// The pose and the energy comparison are FP64; the linear algebra and the schedule are float.
+// On GB300 an FP64 warp instruction costs ~64 issue cycles, and the solves work on float sums:
+// their systems are Jacobi-scaled to a unit diagonal so float pivots keep the accuracy the sums have.
 struct LMState {
   double T[12];     // ref_to_frame [M | t] (M = R, or sR for Sim3), accepted
   double Ttry[12];  // ref_to_frame being evaluated
   double S[kMaxRec];  // record of the last accepted pass
-  double E, lambda, gnmax;
+  float Sf[kMaxSums];  // its sums rounded to float (the kept linearisation the solves read)
+  double E_num, E_den;  // mean energy of the last accepted pass, E_num / E_den (compared by cross-multiplying)
+  float lambda, gnmax;
   int it, phase, level, pair, have_final, fresh;
   int s_src;  // 0: lm.S holds the sums of the pass just merged, 1: of an earlier pass
   int need_exp;  // try_step chose dx: the warp applies exp(dx) * T and publishes the trial pose
-  double dx[7];
+  float dx[7];
   lsdg_track_stats st;
 };
 
@@ -123,6 +128,55 @@ __device__ __forceinline__ void se3_coeffs(double th2, double& A, double& B, dou
     B = (1.0 - cs) / th2;
     C = (th - sn) / (th2 * th);
   }
+}
+
+// Float twin of se3_coeffs for the SE3 tracker's increments (same rule: Taylor series below t = 0.05).
+__device__ __forceinline__ void se3_coeffs_f(float th2, float& A, float& B, float& C) {
+  if (th2 < 0.0025f) {
+    A = 1.0f + th2 * (-1.0f / 6.0f + th2 * (1.0f / 120.0f + th2 * (-1.0f / 5040.0f + th2 * (1.0f / 362880.0f))));
+    B = 0.5f + th2 * (-1.0f / 24.0f + th2 * (1.0f / 720.0f + th2 * (-1.0f / 40320.0f + th2 * (1.0f / 3628800.0f))));
+    C = 1.0f / 6.0f + th2 * (-1.0f / 120.0f + th2 * (1.0f / 5040.0f + th2 * (-1.0f / 362880.0f + th2 * (1.0f / 39916800.0f))));
+  } else {
+    const float th = sqrtf(th2);
+    float sn, cs;
+    sincosf(th, &sn, &cs);
+    A = sn / th;
+    B = (1.0f - cs) / th2;
+    C = (th - sn) / (th2 * th);
+  }
+}
+
+// Tout = exp(xi) * Tin for an se(3) increment xi (float): the increment's rotation and V are built
+// in float (lane e < 9 one element each, lanes 0..2 the translation), the product with the FP64
+// pose in FP64 (lane o < 12 one element).  Every lane must call.
+__device__ __forceinline__ void warp_exp_mul_se3f(const float* xi, const double* Tin, double* Tout, int lane) {
+  const float v0 = xi[0], v1 = xi[1], v2 = xi[2], w0 = xi[3], w1 = xi[4], w2 = xi[5];
+  const float th2 = (w0 * w0 + w1 * w1) + w2 * w2;
+  float A, B, Cc;
+  se3_coeffs_f(th2, A, B, Cc);
+  const int e = lane < 9 ? lane : 0;
+  const int i = e / 3, j = e % 3;
+  const float wi = i == 0 ? w0 : i == 1 ? w1 : w2;
+  const float wj = j == 0 ? w0 : j == 1 ? w1 : w2;
+  const float K = e == 1 ? -w2 : e == 2 ? w1 : e == 3 ? w2 : e == 5 ? -w0 : e == 6 ? -w1 : e == 7 ? w0 : 0.0f;
+  const float I = (i == j) ? 1.0f : 0.0f;
+  const float K2 = wi * wj - ((i == j) ? th2 : 0.0f);
+  const float R = (I + A * K) + B * K2;
+  const float V = (I + B * K) + Cc * K2;
+  const int tr = lane < 3 ? lane : 0;
+  const float V0 = __shfl_sync(0xffffffffu, V, 3 * tr + 0);
+  const float V1 = __shfl_sync(0xffffffffu, V, 3 * tr + 1);
+  const float V2 = __shfl_sync(0xffffffffu, V, 3 * tr + 2);
+  const float t = (V0 * v0 + V1 * v1) + V2 * v2;
+  const int o = lane < 12 ? lane : 0;
+  const int r = o / 4, c = o % 4;
+  const float E0 = __shfl_sync(0xffffffffu, R, 3 * r + 0);
+  const float E1 = __shfl_sync(0xffffffffu, R, 3 * r + 1);
+  const float E2 = __shfl_sync(0xffffffffu, R, 3 * r + 2);
+  const float Et = __shfl_sync(0xffffffffu, t, r);
+  double out = ((double)E0 * Tin[c] + (double)E1 * Tin[4 + c]) + (double)E2 * Tin[8 + c];
+  if (c == 3) out = out + (double)Et;
+  if (lane < 12) Tout[o] = out;
 }
 
 // Coefficients a0, a1, a2 of V = a0 I + a1 K + a2 K^2 in the sim(3) exp (integrals of e^{sigma tau}
@@ -189,16 +243,16 @@ __device__ __forceinline__ void sim3_coeffs_warp(double th2, double sg, int lane
 // Tout = exp(xi) * Tin (3x4 row-major), computed by a whole warp: lane e < 9 builds element e of
 // the rotation (times e^sigma for Sim3) and of V, lanes 0..2 the translation, lane o < 12 one element
 // of the product.  xi (6 or 7 doubles), Tin, Tout are in shared memory; every lane must call.
-template <bool SIM3>
-__device__ __forceinline__ void warp_exp_mul(const double* xi, const double* Tin, double* Tout, int lane) {
+template <bool SIM3, typename X>
+__device__ __forceinline__ void warp_exp_mul(const X* xi, const double* Tin, double* Tout, int lane) {
   const double v0 = xi[0], v1 = xi[1], v2 = xi[2], w0 = xi[3], w1 = xi[4], w2 = xi[5];
   const double th2 = (w0 * w0 + w1 * w1) + w2 * w2;
   double A, B, Cc;
   se3_coeffs(th2, A, B, Cc);
   double sc = 1.0, a0 = 1.0, a1 = B, a2 = Cc;  // SE3: V = I + B K + C K^2
   if (SIM3) {
-    sim3_coeffs_warp(th2, xi[6], lane, a0, a1, a2);
-    sc = exp(xi[6]);
+    sim3_coeffs_warp(th2, (double)xi[6], lane, a0, a1, a2);
+    sc = exp((double)xi[6]);
   }
   const int e = lane < 9 ? lane : 0;
   const int i = e / 3, j = e % 3;
@@ -230,31 +284,37 @@ __device__ __forceinline__ void warp_exp_mul(const double* xi, const double* Tin
 }
 
 // (H + lambda diag H) x = -g for N x N symmetric H given as its upper triangle (row-major), by an
-// LDL^T factorisation held entirely in registers (every loop has compile-time bounds).  Returns
-// false when a pivot is not positive.
+// LDL^T factorisation of the Jacobi-scaled system (row and column j times 1/sqrt(H_jj), so the
+// factorised matrix has the diagonal 1 + lambda) held in float registers.  Returns false when a
+// pivot is not positive.  The warp's four-system solve (warp_solve) computes the same thing.
 template <int N>
-__device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, const double* __restrict__ g,
-                                               double lambda, double* x) {
-  double L[N * (N + 1) / 2];
-  double d[N], id[N], y[N];
+__device__ __forceinline__ bool ldlt_solve_reg(const float* __restrict__ hu, const float* __restrict__ g,
+                                               float lambda, float* x) {
+  float L[N * (N + 1) / 2];
+  float d[N], id[N], y[N], sc[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    const float h = hu[j * N - (j * (j - 1)) / 2];
+    sc[j] = h > 0.f ? rsqrtf(h) : 1.f;
+  }
 #pragma unroll
   for (int i = 0; i < N; ++i)
 #pragma unroll
-    for (int j = 0; j <= i; ++j) L[i * (i + 1) / 2 + j] = hu[j * N - (j * (j - 1)) / 2 + (i - j)];
+    for (int j = 0; j <= i; ++j) L[i * (i + 1) / 2 + j] = (hu[j * N - (j * (j - 1)) / 2 + (i - j)] * sc[i]) * sc[j];
 #pragma unroll
-  for (int i = 0; i < N; ++i) L[i * (i + 1) / 2 + i] *= (1.0 + lambda);
+  for (int i = 0; i < N; ++i) L[i * (i + 1) / 2 + i] *= (1.0f + lambda);
   bool ok = true;
 #pragma unroll
   for (int j = 0; j < N; ++j) {
-    double sj = L[j * (j + 1) / 2 + j];
+    float sj = L[j * (j + 1) / 2 + j];
 #pragma unroll
     for (int k = 0; k < j; ++k) sj -= (L[j * (j + 1) / 2 + k] * L[j * (j + 1) / 2 + k]) * d[k];
-    ok = ok && (sj > 1e-30);
+    ok = ok && (sj > 1e-20f);
     d[j] = sj;
-    id[j] = 1.0 / sj;
+    id[j] = 1.0f / sj;
 #pragma unroll
     for (int i = j + 1; i < N; ++i) {
-      double t = L[i * (i + 1) / 2 + j];
+      float t = L[i * (i + 1) / 2 + j];
 #pragma unroll
       for (int k = 0; k < j; ++k) t -= (L[i * (i + 1) / 2 + k] * L[j * (j + 1) / 2 + k]) * d[k];
       L[i * (i + 1) / 2 + j] = t * id[j];
@@ -262,7 +322,7 @@ __device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, co
   }
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    double si = -g[i];
+    float si = -(g[i] * sc[i]);
 #pragma unroll
     for (int k = 0; k < i; ++k) si -= L[i * (i + 1) / 2 + k] * y[k];
     y[i] = si;
@@ -271,11 +331,13 @@ __device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, co
   for (int i = 0; i < N; ++i) y[i] *= id[i];
 #pragma unroll
   for (int i = N - 1; i >= 0; --i) {
-    double si = y[i];
+    float si = y[i];
 #pragma unroll
     for (int k = i + 1; k < N; ++k) si -= L[k * (k + 1) / 2 + i] * x[k];
     x[i] = si;
   }
+#pragma unroll
+  for (int i = 0; i < N; ++i) x[i] *= sc[i];
   return ok;
 }
 
@@ -284,56 +346,66 @@ __device__ __forceinline__ bool ldlt_solve_reg(const double* __restrict__ hu, co
 // accepted (or is a level's first pass), [2] and [3] damped steps on the kept linearisation after
 // one or two rejections.  The decision logic takes an entry only when source and lambda match.
 struct SolveCache {
-  double x[4][8];
-  double lambda[4];
+  float x[4][8];
+  float lambda[4];
+  float gn[4];  // max |x_i| of the solution
   int src[4];  // 0: the sums of the pass just merged, 1: the sums kept from an earlier pass
   int ok[4];
   int valid[4];
-  double Ls[4][8][8];  // per-group L of the factorisation (row-major), for the back substitution
+  float Ls[4][8][8];  // per-group L of the factorisation (row-major), for the back substitution
 };
 
 // Row-per-lane LDL^T solve of (H + lambda diag H) x = -g (N <= 7) for the group of 8 lanes starting
-// at `base` (rows 0..N-1; the other lanes of the group mirror row N-1 and their results are dropped).
-// hu: upper triangle of H (row-major), g: right-hand side, both in shared memory.  About 4N FP64 warp
-// instructions plus N reciprocals, whatever the number of groups.
+// at `base` (rows 0..N-1; the other lanes of the group mirror row N-1 and their results are dropped),
+// on the Jacobi-scaled system like ldlt_solve_reg.  hu: upper triangle of H (row-major), g: right-
+// hand side, both float in shared memory.  Also leaves max |x_i| in *gnout.
 template <int N>
-__device__ __forceinline__ void warp_solve(const double* __restrict__ hu, const double* __restrict__ g, double lambda,
-                                           int lane, double (*Ls)[8], double* xout, int* okout) {
+__device__ __forceinline__ void warp_solve(const float* __restrict__ hu, const float* __restrict__ g, float lambda,
+                                           int lane, float (*Ls)[8], float* xout, int* okout, float* gnout) {
   const int base = lane & ~7;
   const int r = (lane & 7) < N ? (lane & 7) : N - 1;
-  double a[N], l[N], wv[N], inv[N];
+  float a[N], l[N], wv[N], inv[N], sc[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    const float h = hu[j * N - (j * (j - 1)) / 2];
+    sc[j] = h > 0.f ? rsqrtf(h) : 1.f;
+  }
+  float sr = sc[0];
+#pragma unroll
+  for (int j = 1; j < N; ++j)
+    if (j == r) sr = sc[j];
 #pragma unroll
   for (int j = 0; j < N; ++j) {
     const int lo = r < j ? r : j, hi = r < j ? j : r;
-    a[j] = hu[lo * N - (lo * (lo - 1)) / 2 + (hi - lo)];
-    l[j] = 0.0;
-    wv[j] = 0.0;
+    a[j] = (hu[lo * N - (lo * (lo - 1)) / 2 + (hi - lo)] * sr) * sc[j];
+    l[j] = 0.0f;
+    wv[j] = 0.0f;
   }
 #pragma unroll
   for (int j = 0; j < N; ++j)
-    if (j == r) a[j] = a[j] * (1.0 + lambda);
+    if (j == r) a[j] = a[j] * (1.0f + lambda);
   bool ok = true;
 #pragma unroll
   for (int j = 0; j < N; ++j) {
-    double t = a[j];
+    float t = a[j];
 #pragma unroll
     for (int k = 0; k < j; ++k) t = t - l[k] * __shfl_sync(0xffffffffu, wv[k], base + j);  // L_rk * (L_jk d_k)
-    const double dj = __shfl_sync(0xffffffffu, t, base + j);
-    ok = ok && (dj > 1e-30);
-    inv[j] = 1.0 / dj;
+    const float dj = __shfl_sync(0xffffffffu, t, base + j);
+    ok = ok && (dj > 1e-20f);
+    inv[j] = 1.0f / dj;
     if (r > j) {
       l[j] = t * inv[j];
       wv[j] = t;
     }
   }
   // forward: y_r = -g_r - sum_{k<r} L_rk y_k, column by column
-  double y = -g[r];
+  float y = -(g[r] * sr);
 #pragma unroll
   for (int k = 0; k < N; ++k) {
-    const double yk = __shfl_sync(0xffffffffu, y, base + k);
+    const float yk = __shfl_sync(0xffffffffu, y, base + k);
     if (r > k) y = y - l[k] * yk;
   }
-  double ir = inv[0];
+  float ir = inv[0];
 #pragma unroll
   for (int j = 1; j < N; ++j)
     if (j == r) ir = inv[j];
@@ -344,14 +416,22 @@ __device__ __forceinline__ void warp_solve(const double* __restrict__ hu, const 
     for (int k = 0; k < N; ++k) Ls[r][k] = l[k];
   }
   __syncwarp();
-  double x = y;
+  float x = y;
 #pragma unroll
   for (int k = N - 1; k >= 0; --k) {
-    const double xk = __shfl_sync(0xffffffffu, x, base + k);
+    const float xk = __shfl_sync(0xffffffffu, x, base + k);
     if (r < k) x = x - Ls[k][r] * xk;
   }
+  x = x * sr;
+  float m = (lane & 7) < N ? fabsf(x) : 0.f;
+  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
+  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
+  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 4));
   if ((lane & 7) < N) xout[r] = x;
-  if ((lane & 7) == 0) *okout = ok ? 1 : 0;
+  if ((lane & 7) == 0) {
+    *okout = ok ? 1 : 0;
+    *gnout = m;
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -438,9 +518,11 @@ __device__ __noinline__ void fetch_pair(const TrackArgs& a, LMState& lm, Ctl& ct
     lm.need_exp = 0;
     lm.s_src = 1;
     lm.it = 0;
-    lm.E = 0;
+    lm.E_num = 0;
+    lm.E_den = 1;
     lm.lambda = a.lambda0;
     for (int i = 0; i < kMaxRec; ++i) lm.S[i] = 0;
+    for (int i = 0; i < kMaxSums; ++i) lm.Sf[i] = 0.f;
     if (a.accumulate_stats) {
       lm.st = a.out_stats[p];  // the coarse levels' pass counts, from the first phase
     } else {
@@ -475,17 +557,22 @@ __device__ void next_level(const TrackArgs& a, LMState& lm, Ctl& ctl) {
 }
 
 template <bool SIM3>
-__device__ __forceinline__ bool cached_solve(LMState& lm, SolveCache& sc, double lambda, double* x) {
+__device__ __forceinline__ bool cached_solve(LMState& lm, SolveCache& sc, float lambda, float* x, float* gn) {
   constexpr int D = Mode<SIM3>::DOF;
 #pragma unroll 1
   for (int k = 0; k < 4; ++k) {
     if (sc.valid[k] && sc.src[k] == lm.s_src && sc.lambda[k] == lambda) {
       for (int i = 0; i < D; ++i) x[i] = sc.x[k][i];
+      *gn = sc.gn[k];
       sc.valid[k] = 0;
       return sc.ok[k] != 0;
     }
   }
-  return ldlt_solve_reg<D>(lm.S, lm.S + Mode<SIM3>::NH, lambda, x);
+  const bool ok = ldlt_solve_reg<D>(lm.Sf, lm.Sf + Mode<SIM3>::NH, lambda, x);
+  float m = 0.f;
+  for (int i = 0; i < D; ++i) m = fmaxf(m, fabsf(x[i]));
+  *gn = m;
+  return ok;
 }
 
 // One LM iteration decision on the current linearisation lm.S (same rules as the CPU oracle):
@@ -494,14 +581,12 @@ __device__ __forceinline__ bool cached_solve(LMState& lm, SolveCache& sc, double
 template <bool SIM3>
 __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& sc) {
   constexpr int D = Mode<SIM3>::DOF;
-  const double thr = a.step_eps * (double)(1 << lm.level);
+  const float thr = a.step_eps * (float)(1 << lm.level);
   for (;;) {
     if (lm.fresh) {
-      double gn[D];
-      lm.gnmax = 1e300;
-      if (cached_solve<SIM3>(lm, sc, 0.0, gn)) {
-        double m = 0;
-        for (int i = 0; i < D; ++i) m = fmax(m, fabs(gn[i]));
+      float gn[D], m = 0.f;
+      lm.gnmax = 3e38f;
+      if (cached_solve<SIM3>(lm, sc, 0.0f, gn, &m)) {
         lm.gnmax = m;
         if (m < thr) break;
       }
@@ -509,8 +594,8 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& 
     }
     if (lm.it >= a.max_iter[lm.level]) break;
     lm.it++;
-    double dx[D];
-    if (!cached_solve<SIM3>(lm, sc, lm.lambda, dx)) {
+    float dx[D], m = 0.f;
+    if (!cached_solve<SIM3>(lm, sc, lm.lambda, dx, &m)) {
       lm.lambda *= a.lambda_up;
       continue;
     }
@@ -526,7 +611,8 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& 
 }
 
 template <bool SIM3>
-__device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ctl, const double* tot, SolveCache& sc) {
+__device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ctl, const double* tot,
+                                       const float* totf, SolveCache& sc) {
   using Md = Mode<SIM3>;
   lm.st.passes[lm.level]++;
   const double N = tot[Md::NS];
@@ -534,8 +620,10 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
   if (lm.phase == PH_INIT) {
     if (N > 0) {
       for (int i = 0; i < Md::REC; ++i) lm.S[i] = tot[i];
+      for (int i = 0; i < Md::NS; ++i) lm.Sf[i] = totf[i];
       lm.s_src = 0;
-      lm.E = En / N;
+      lm.E_num = En;
+      lm.E_den = N;
       lm.lambda = a.lambda0;
       lm.it = 0;
       lm.fresh = 1;
@@ -546,16 +634,18 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
     }
     return;
   }
-  if (N > 0 && En / N < lm.E) {
+  if (N > 0 && En * lm.E_den < lm.E_num * N) {  // En / N below the accepted mean energy
     for (int i = 0; i < 12; ++i) lm.T[i] = lm.Ttry[i];
     for (int i = 0; i < Md::REC; ++i) lm.S[i] = tot[i];
+    for (int i = 0; i < Md::NS; ++i) lm.Sf[i] = totf[i];
     lm.s_src = 0;
-    lm.E = En / N;
+    lm.E_num = En;
+    lm.E_den = N;
     lm.lambda *= a.lambda_down;
     lm.fresh = 1;
   } else {
     lm.s_src = 1;
-    if (lm.gnmax < a.stall_eps * (double)(1 << lm.level)) {  // noise floor of this level
+    if (lm.gnmax < a.stall_eps * (float)(1 << lm.level)) {  // noise floor of this level
       next_level<SIM3>(a, lm, ctl);
       return;
     }
@@ -566,17 +656,17 @@ __device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ct
 
 // Warp 0 of cluster rank 0 solves the four systems the decision may need (see SolveCache).
 template <bool SIM3>
-__device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm, const double* tot, SolveCache& sc,
-                                          int lane) {
+__device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm, const double* tot, const float* totf,
+                                          SolveCache& sc, int lane) {
   using Md = Mode<SIM3>;
   const int grp = lane >> 3;
   const bool init = lm.phase == PH_INIT;
-  const double* S = grp >= 2 ? lm.S : tot;
-  const double lam = grp == 0 ? 0.0
-                   : grp == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down)
-                   : grp == 2 ? lm.lambda * a.lambda_up
-                              : (lm.lambda * a.lambda_up) * a.lambda_up;
-  warp_solve<Md::DOF>(S, S + Md::NH, lam, lane, sc.Ls[grp], sc.x[grp], &sc.ok[grp]);
+  const float* S = grp >= 2 ? lm.Sf : totf;
+  const float lam = grp == 0 ? 0.0f
+                  : grp == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down)
+                  : grp == 2 ? lm.lambda * a.lambda_up
+                             : (lm.lambda * a.lambda_up) * a.lambda_up;
+  warp_solve<Md::DOF>(S, S + Md::NH, lam, lane, sc.Ls[grp], sc.x[grp], &sc.ok[grp], &sc.gn[grp]);
   if ((lane & 7) == 0) {
     sc.lambda[grp] = lam;
     sc.src[grp] = grp >= 2 ? 1 : 0;
@@ -633,6 +723,7 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
   __shared__ CtaPart allpart[kMaxCluster];  // rank 0's copy receives every rank's partial
   __shared__ Ctl ctl;                       // every rank's copy is written by rank 0
   __shared__ double tot[kMaxRec];
+  __shared__ float totf[kMaxSums];
   __shared__ LMState lm;
   __shared__ SolveCache sc;
 
@@ -986,6 +1077,7 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
         float s = 0.f, c = 0.f;
         for (unsigned r = 0; r < C; ++r) kmerge(s, c, allpart[r].s[tid], allpart[r].c[tid]);
         tot[tid] = (double)s - (double)c;
+        totf[tid] = s - c;
       } else if (tid < NS + 3) {
         int v = 0;
         for (unsigned r = 0; r < C; ++r) v += allpart[r].cnt[tid - NS];
@@ -995,12 +1087,13 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
       if (wid == 0) {
         if (lane == 0) tot[NS] = tot[NS + 1] + tot[NS + 2];
         __syncwarp();
-        speculate<SIM3>(a, lm, tot, sc, lane);
+        speculate<SIM3>(a, lm, tot, totf, sc, lane);
         __syncwarp();
-        if (lane == 0) lm_advance<SIM3>(a, lm, ctl, tot, sc);
+        if (lane == 0) lm_advance<SIM3>(a, lm, ctl, tot, totf, sc);
         __syncwarp();
         if (lm.need_exp) {
-          warp_exp_mul<SIM3>(lm.dx, lm.T, lm.Ttry, lane);
+          if (SIM3) warp_exp_mul<true>(lm.dx, lm.T, lm.Ttry, lane);
+          else warp_exp_mul_se3f(lm.dx, lm.T, lm.Ttry, lane);
           __syncwarp();
           if (lane < 12) {  // publish the trial pose as float, one element per lane
             const float f = (float)lm.Ttry[lane];
@@ -1060,7 +1153,7 @@ static int max_clusters_nt(int cluster) {
   return n;
 }
 
-#define LSDG_TRACK_SHAPES(X) X(128, 4) X(128, 8) X(256, 2) X(256, 4) X(512, 1) X(512, 2)
+#define LSDG_TRACK_SHAPES(X) X(128, 4) X(128, 6) X(128, 8) X(256, 2) X(256, 3) X(256, 4) X(512, 1) X(512, 2)
 
 // Per context, outside any stream capture: allows clusters of up to 16 CTAs (non-portable size)
 // for every instantiation and uploads the sim(3) series coefficients.
