@@ -610,48 +610,59 @@ __device__ void try_step(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& 
   next_level<SIM3>(a, lm, ctl);
 }
 
+// What the warp does after the LM decision (lm_decide): copy the pass just merged into the record
+// (and the trial pose into the accepted pose), then take the next step or move to the next level.
+enum { ACT_STEP = 1, ACT_NEXT_LEVEL = 2, ACT_COPY_S = 4, ACT_COPY_T = 8 };
+
+// The accept / reject decision on the pass just merged (lane 0; same rules as the CPU oracle).
+// The copies it asks for are made by the whole warp (lm_copy) before lm_continue runs.
 template <bool SIM3>
-__device__ __noinline__ void lm_advance(const TrackArgs& a, LMState& lm, Ctl& ctl, const double* tot,
-                                       const float* totf, SolveCache& sc) {
+__device__ __noinline__ int lm_decide(const TrackArgs& a, LMState& lm, const double* tot) {
   using Md = Mode<SIM3>;
   lm.st.passes[lm.level]++;
   const double N = tot[Md::NS];
   const double En = tot[Md::NS - 1];
   if (lm.phase == PH_INIT) {
-    if (N > 0) {
-      for (int i = 0; i < Md::REC; ++i) lm.S[i] = tot[i];
-      for (int i = 0; i < Md::NS; ++i) lm.Sf[i] = totf[i];
-      lm.s_src = 0;
-      lm.E_num = En;
-      lm.E_den = N;
-      lm.lambda = a.lambda0;
-      lm.it = 0;
-      lm.fresh = 1;
-      if (lm.level == a.bottom_level) lm.have_final = 1;
-      try_step<SIM3>(a, lm, ctl, sc);
-    } else {
-      next_level<SIM3>(a, lm, ctl);
-    }
-    return;
+    if (!(N > 0)) return ACT_NEXT_LEVEL;
+    lm.s_src = 0;
+    lm.E_num = En;
+    lm.E_den = N;
+    lm.lambda = a.lambda0;
+    lm.it = 0;
+    lm.fresh = 1;
+    if (lm.level == a.bottom_level) lm.have_final = 1;
+    return ACT_STEP | ACT_COPY_S;
   }
   if (N > 0 && En * lm.E_den < lm.E_num * N) {  // En / N below the accepted mean energy
-    for (int i = 0; i < 12; ++i) lm.T[i] = lm.Ttry[i];
-    for (int i = 0; i < Md::REC; ++i) lm.S[i] = tot[i];
-    for (int i = 0; i < Md::NS; ++i) lm.Sf[i] = totf[i];
     lm.s_src = 0;
     lm.E_num = En;
     lm.E_den = N;
     lm.lambda *= a.lambda_down;
     lm.fresh = 1;
-  } else {
-    lm.s_src = 1;
-    if (lm.gnmax < a.stall_eps * (float)(1 << lm.level)) {  // noise floor of this level
-      next_level<SIM3>(a, lm, ctl);
-      return;
-    }
-    lm.lambda *= a.lambda_up;
+    return ACT_STEP | ACT_COPY_S | ACT_COPY_T;
   }
-  try_step<SIM3>(a, lm, ctl, sc);
+  lm.s_src = 1;
+  if (lm.gnmax < a.stall_eps * (float)(1 << lm.level)) return ACT_NEXT_LEVEL;  // noise floor of this level
+  lm.lambda *= a.lambda_up;
+  return ACT_STEP;
+}
+
+// Whole warp: the record / pose copies a decision asked for.
+template <bool SIM3>
+__device__ __forceinline__ void lm_copy(LMState& lm, const double* tot, const float* totf, int act, int lane) {
+  using Md = Mode<SIM3>;
+  if (act & ACT_COPY_S) {
+    for (int i = lane; i < Md::REC; i += 32) lm.S[i] = tot[i];
+    if (lane < Md::NS) lm.Sf[lane] = totf[lane];
+  }
+  if ((act & ACT_COPY_T) && lane < 12) lm.T[lane] = lm.Ttry[lane];
+}
+
+// Lane 0, after the copies: the next LM step of this level, or the next level / pair.
+template <bool SIM3>
+__device__ __noinline__ void lm_continue(const TrackArgs& a, LMState& lm, Ctl& ctl, SolveCache& sc, int act) {
+  if (act & ACT_STEP) try_step<SIM3>(a, lm, ctl, sc);
+  else next_level<SIM3>(a, lm, ctl);
 }
 
 // Warp 0 of cluster rank 0 solves the four systems the decision may need (see SolveCache).
@@ -791,12 +802,17 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
       // threads, warps and CTAs is compensated.
       const int stride = (int)C * NT;
       const float d2 = delta * delta;
-      auto eval = [&](int k, float (&J)[D], float& wgt, float& res, float& rho) {
+      // a point's inputs: its float4 and frozen 1/sigma^2 (index 0 stands in past the end; the level's
+      // arrays are allocated for every pixel, so it is in bounds)
+      auto load = [&](int k, float4& p, float& sig) {
+        const int kk = k < n ? k : 0;
+        sig = first ? 1.f : psig[kk];
+        p = __ldg(&pts[kk]);
+      };
+      auto eval = [&](int k, const float4 p, const float sig, float (&J)[D], float& wgt, float& res, float& rho) {
         const bool in = k < n;
         const int kk = in ? k : 0;
-        const float sig = first ? 1.f : psig[kk];
         const bool act = in && sig > 0.f;
-        const float4 p = __ldg(&pts[kk]);
         const float X = p.x, Y = p.y, Z = p.z, Ik = p.w;
         const float Rpx = (R00 * X + R01 * Y) + R02 * Z;
         const float Rpy = (R10 * X + R11 * Y) + R12 * Z;
@@ -855,10 +871,20 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
         J[4] = ok ? Zp * a0 - Xp * a2 : 0.f;
         J[5] = ok ? Xp * a1 - Yp * a0 : 0.f;
       };
-      for (int k = (int)rank * NT + tid; k < n; k += 2 * stride) {
+      // the next iteration's two points are loaded while this one's are evaluated
+      int k = (int)rank * NT + tid;
+      float4 pa, pb;
+      float sa, sb;
+      load(k, pa, sa);
+      load(k + stride, pb, sb);
+      for (; k < n; k += 2 * stride) {
+        const float4 ca = pa, cb = pb;
+        const float csa = sa, csb = sb;
+        load(k + 2 * stride, pa, sa);
+        load(k + 3 * stride, pb, sb);
         float Ja[D], Jb[D], wa, wb, ra, rb, ea, eb;
-        eval(k, Ja, wa, ra, ea);
-        eval(k + stride, Jb, wb, rb, eb);
+        eval(k, ca, csa, Ja, wa, ra, ea);
+        eval(k + stride, cb, csb, Jb, wb, rb, eb);
         float wJa[D], wJb[D];
 #pragma unroll
         for (int i = 0; i < D; ++i) { wJa[i] = wa * Ja[i]; wJb[i] = wb * Jb[i]; }
@@ -1089,7 +1115,13 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
         __syncwarp();
         speculate<SIM3>(a, lm, tot, totf, sc, lane);
         __syncwarp();
-        if (lane == 0) lm_advance<SIM3>(a, lm, ctl, tot, totf, sc);
+        int act = 0;
+        if (lane == 0) act = lm_decide<SIM3>(a, lm, tot);
+        act = __shfl_sync(0xffffffffu, act, 0);
+        __syncwarp();
+        lm_copy<SIM3>(lm, tot, totf, act, lane);
+        __syncwarp();
+        if (lane == 0) lm_continue<SIM3>(a, lm, ctl, sc, act);
         __syncwarp();
         if (lm.need_exp) {
           if (SIM3) warp_exp_mul<true>(lm.dx, lm.T, lm.Ttry, lane);
