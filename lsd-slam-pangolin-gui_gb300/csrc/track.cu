@@ -130,6 +130,22 @@ __device__ __forceinline__ void se3_coeffs(double th2, double& A, double& B, dou
   }
 }
 
+// The tracker's Catmull-Rom weights and derivative weights (the polynomials of catmull_rom in
+// Horner form: 18 fused operations instead of ~30; the tracker is built with FMA contraction and
+// its parity is by tolerance, the energy kernels keep the oracle's operation order).
+__device__ __forceinline__ void catmull_rom_fma(float t, float w[4], float d[4]) {
+  const float t2 = t * t;
+  const float e = fmaf(-1.5f, t, 2.0f);
+  w[0] = t * fmaf(t, fmaf(-0.5f, t, 1.0f), -0.5f);
+  w[1] = fmaf(t2, fmaf(1.5f, t, -2.5f), 1.0f);
+  w[2] = t * fmaf(t, e, 0.5f);
+  w[3] = t2 * fmaf(0.5f, t, -0.5f);
+  d[0] = fmaf(t, e, -0.5f);
+  d[1] = t * fmaf(4.5f, t, -5.0f);
+  d[2] = fmaf(t, fmaf(-4.5f, t, 4.0f), 0.5f);
+  d[3] = t * fmaf(1.5f, t, -1.0f);
+}
+
 // Float twin of se3_coeffs for the SE3 tracker's increments (same rule: Taylor series below t = 0.05).
 __device__ __forceinline__ void se3_coeffs_f(float th2, float& A, float& B, float& C) {
   if (th2 < 0.0025f) {
@@ -819,7 +835,7 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
         const float Rpz = (R20 * X + R21 * Y) + R22 * Z;
         const float Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
         const bool zok = Zp > minz;
-        const float iz = 1.0f / (zok ? Zp : 1.f);
+        const float iz = __fdividef(1.0f, zok ? Zp : 1.f);  // ~1 ulp reciprocal
         const float u = fx * (Xp * iz) + cx;
         const float v = fy * (Yp * iz) + cy;
         const bool bok = first ? (u >= ulo && v >= vlo && u < uhi && v < vhi)
@@ -833,8 +849,8 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
         const int ix = (int)uc, iy = (int)vc;
         const float ax = uc - (float)ix, ay = vc - (float)iy;
         float wx[4], dxw[4], wy[4], dyw[4];
-        catmull_rom(ax, wx, dxw);
-        catmull_rom(ay, wy, dyw);
+        catmull_rom_fma(ax, wx, dxw);
+        catmull_rom_fma(ay, wy, dyw);
         float rI[4], rD[4];
         const float* q = img + (size_t)(iy - 1) * w + (ix - 1);
 #pragma unroll
@@ -892,7 +908,7 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
 #pragma unroll
         for (int i = 0; i < D; ++i)
 #pragma unroll
-          for (int j = i; j < D; ++j) { hs[q2] += wJa[i] * Ja[j] + wJb[i] * Jb[j]; ++q2; }
+          for (int j = i; j < D; ++j) { hs[q2] = fmaf(wJb[i], Jb[j], fmaf(wJa[i], Ja[j], hs[q2])); ++q2; }
 #pragma unroll
         for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJa[i] * ra + wJb[i] * rb);
         kadd(es, ec, ea + eb);
@@ -936,8 +952,8 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
       const int ix = (int)u, iy = (int)v;
       const float ax = u - (float)ix, ay = v - (float)iy;
       float wx[4], dxw[4], wy[4], dyw[4];
-      catmull_rom(ax, wx, dxw);
-      catmull_rom(ay, wy, dyw);
+      catmull_rom_fma(ax, wx, dxw);
+      catmull_rom_fma(ay, wy, dyw);
       float rI[4], rD[4];
       const float* q = img + (size_t)(iy - 1) * w + (ix - 1);
 #pragma unroll
