@@ -19,12 +19,6 @@
 
 namespace lsdg {
 
-__device__ __forceinline__ float mean4(const float* P, int pw, int x, int y) {
-  const float* r0 = P + (size_t)(2 * y) * pw + 2 * x;
-  const float* r1 = r0 + pw;
-  return ((r0[0] + r0[1]) + (r1[0] + r1[1])) * 0.25f;
-}
-
 // 8-bit input image -> level-0 intensity plane.
 __global__ void u8_to_plane_kernel(const uint8_t* __restrict__ src, float* __restrict__ dst, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -32,69 +26,138 @@ __global__ void u8_to_plane_kernel(const uint8_t* __restrict__ src, float* __res
 }
 
 // Pass 1, one CTA per (band, frame): intensity levels 1..L-1 of the band; for keyframes also the
-// depth pyramid (level 0 sanitised in place: idepth <= 0 or var <= 0 -> -1; level l: inverse-
-// variance weighted mean of the valid 2x2 children, variance = n / sum(1/var)) and the number of
-// valid pixels of the band at every level.
-__global__ void __launch_bounds__(256) band_build_kernel(const FrameDev* __restrict__ frames) {
+// depth pyramid (level 0 sanitised in place: idepth <= 0 or var <= 0 -> -1, written only where the
+// value is not -1 already; level l: inverse-variance weighted mean of the valid 2x2 children,
+// variance = n / sum(1/var)) and the number of valid pixels of the band at every level.  Each
+// thread counts its own pixels of a level; one block reduction per level.  The intensity pyramid
+// (blockIdx.z = 0) and the depth pyramid (blockIdx.z = 1) of a band are built by different CTAs.
+__global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __restrict__ frames) {
   const FrameDev& F = frames[blockIdx.y];
   const int L = F.levels;
   const int band_rows = 1 << (L - 1);
   const int band = blockIdx.x;
   if (band * band_rows >= F.h) return;
+  __shared__ int wsum[8];
+  if (blockIdx.z == 0) {
   for (int l = 1; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
     const float* P = F.plane[l - 1];
-    float* Q = F.plane[l];
-    for (int i = threadIdx.x; i < rows * w; i += blockDim.x) {
-      const int x = i % w, y = y0 + i / w;
-      Q[(size_t)y * w + x] = mean4(P, 2 * w, x, y);
+    float* Q = F.plane[l] + (size_t)y0 * w;
+    const int n = rows * w, pw = 2 * w;
+    // B outputs per thread per round: their 2 B float2 loads are in flight together
+    constexpr int B = 2;
+    for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
+      float2 r0[B], r1[B];
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int i = i0 + u * 256;
+        if (i < n) {
+          const int x = i % w, y = y0 + i / w;
+          const float* a = P + (size_t)(2 * y) * pw + 2 * x;
+          r0[u] = *reinterpret_cast<const float2*>(a);
+          r1[u] = *reinterpret_cast<const float2*>(a + pw);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < B; ++u) {
+        const int i = i0 + u * 256;
+        if (i < n) Q[i] = ((r0[u].x + r0[u].y) + (r1[u].x + r1[u].y)) * 0.25f;
+      }
     }
     __syncthreads();  // level l is read by level l + 1 (other threads of this CTA)
   }
+  return;
+  }
   if (!F.has_depth) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int l = 0; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
     int count = 0;
-    for (int base = 0; base < rows * w; base += blockDim.x) {
-      const int i = base + threadIdx.x;
-      bool valid = false;
-      if (i < rows * w) {
-        const int x = i % w, y = y0 + i / w;
-        const size_t idx = (size_t)y * w + x;
-        if (l == 0) {
-          const float d = F.idepth[0][idx], v = F.ivar[0][idx];
-          valid = d > 0.f && v > 0.f;
-          if (!valid) {
-            F.idepth[0][idx] = -1.f;
-            F.ivar[0][idx] = -1.f;
-          }
-        } else {
-          const int pw = 2 * w;
-          const float* D = F.idepth[l - 1];
-          const float* V = F.ivar[l - 1];
-          const size_t c0 = (size_t)(2 * y) * pw + 2 * x;
-          const size_t c[4] = {c0, c0 + 1, c0 + pw, c0 + pw + 1};
-          float sw = 0.f, swd = 0.f;
-          int n = 0;
+    if (l == 0) {
+      float* D = F.idepth[0] + (size_t)y0 * w;
+      float* V = F.ivar[0] + (size_t)y0 * w;
+      const int n = rows * w;
+      constexpr int B = 4;
+      for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
+        float d[B], v[B];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const float d = D[c[k]], v = V[c[k]];
-            if (d > 0.f && v > 0.f) {
-              const float wt = 1.0f / v;
-              sw = sw + wt;
-              swd = swd + wt * d;
-              ++n;
-            }
+        for (int u = 0; u < B; ++u) {
+          const int i = i0 + u * 256;
+          d[u] = -1.f;
+          v[u] = -1.f;
+          if (i < n) {
+            d[u] = D[i];
+            v[u] = V[i];
           }
-          valid = n > 0;
-          F.idepth[l][idx] = valid ? swd / sw : -1.f;
-          F.ivar[l][idx] = valid ? (float)n / sw : -1.f;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int i = i0 + u * 256;
+          const bool valid = d[u] > 0.f && v[u] > 0.f;
+          count += valid ? 1 : 0;
+          if (i < n && !valid && !(d[u] == -1.f && v[u] == -1.f)) {
+            D[i] = -1.f;
+            V[i] = -1.f;
+          }
         }
       }
-      // block-wide count; the barrier also orders this level's writes before the next level's reads
-      count += __syncthreads_count(valid);
+    } else {
+      const int pw = 2 * w, n = rows * w;
+      const float* Dp = F.idepth[l - 1];
+      const float* Vp = F.ivar[l - 1];
+      float* Dq = F.idepth[l] + (size_t)y0 * w;
+      float* Vq = F.ivar[l] + (size_t)y0 * w;
+      constexpr int B = 2;
+      for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
+        float2 d0[B], d1[B], v0[B], v1[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int i = i0 + u * 256;
+          if (i < n) {
+            const int x = i % w, y = y0 + i / w;
+            const size_t c0 = (size_t)(2 * y) * pw + 2 * x;
+            d0[u] = *reinterpret_cast<const float2*>(Dp + c0);
+            d1[u] = *reinterpret_cast<const float2*>(Dp + c0 + pw);
+            v0[u] = *reinterpret_cast<const float2*>(Vp + c0);
+            v1[u] = *reinterpret_cast<const float2*>(Vp + c0 + pw);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+          const int i = i0 + u * 256;
+          if (i < n) {
+            const float dd[4] = {d0[u].x, d0[u].y, d1[u].x, d1[u].y};
+            const float vv[4] = {v0[u].x, v0[u].y, v1[u].x, v1[u].y};
+            float sw = 0.f, swd = 0.f;
+            int nv = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              if (dd[k] > 0.f && vv[k] > 0.f) {
+                const float wt = 1.0f / vv[k];
+                sw = sw + wt;
+                swd = swd + wt * dd[k];
+                ++nv;
+              }
+            }
+            const bool valid = nv > 0;
+            count += valid ? 1 : 0;
+            Dq[i] = valid ? swd / sw : -1.f;
+            Vq[i] = valid ? (float)nv / sw : -1.f;
+          }
+        }
+      }
     }
-    if (threadIdx.x == 0) F.blk_count[l][band] = count;
+    // block sum of the counts; the barrier also orders this level's writes before the next level's reads
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) count += __shfl_xor_sync(0xffffffffu, count, o);
+    if (lane == 0) wsum[wid] = count;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += wsum[k];
+      F.blk_count[l][band] = t;
+    }
+    __syncthreads();  // wsum is rewritten by the next level
   }
 }
 
@@ -141,7 +204,9 @@ __global__ void __launch_bounds__(32) point_scan_kernel(const FrameDev* __restri
 }
 
 // Pass 2, one CTA per (band, keyframe): the valid pixels of every level of the band as SoA points
-// {X, Y, Z, I} + var, in row-major order, starting at the band's offset.
+// {X, Y, Z, I} + var, in row-major order, starting at the band's offset.  A chunk is 4 x 256 pixels
+// (pixel base + 256 j + thread, j = 0..3): one ballot per j and warp, one warp-wide scan of the
+// 32 (j, warp) counts, so three barriers per 1024 pixels.
 __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __restrict__ frames) {
   const FrameDev& F = frames[blockIdx.y];
   if (!F.has_depth) return;
@@ -149,50 +214,76 @@ __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __res
   const int band_rows = 1 << (L - 1);
   const int band = blockIdx.x;
   if (band * band_rows >= F.h) return;
-  __shared__ int woff[8];
+  constexpr int J = 4, NWARP = 8;  // blockDim.x == 256
+  __shared__ int off[J * NWARP];
   __shared__ int chunk_total;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
   for (int l = 0; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
+    const int npix = rows * w;
+    const float* D = F.idepth[l] + (size_t)y0 * w;
+    const float* V = F.ivar[l] + (size_t)y0 * w;
     int pos0 = F.blk_count[l][band];
     const float cx = F.cx[l], cy = F.cy[l], fxi = F.fxi[l], fyi = F.fyi[l];
-    for (int base = 0; base < rows * w; base += blockDim.x) {
-      const int i = base + threadIdx.x;
-      float d = -1.f, v = -1.f;
-      int x = 0, y = 0;
-      size_t idx = 0;
-      if (i < rows * w) {
-        x = i % w;
-        y = y0 + i / w;
-        idx = (size_t)y * w + x;
-        d = F.idepth[l][idx];
-        v = F.ivar[l][idx];
-      }
-      const bool valid = d > 0.f && v > 0.f;
-      const unsigned m = __ballot_sync(0xffffffffu, valid);
-      if (lane == 0) woff[wid] = __popc(m);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        int s = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
-          const int t = woff[k];
-          woff[k] = s;
-          s += t;
+    for (int base = 0; base < npix; base += J * 256) {
+      float d[J], v[J];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const int i = base + j * 256 + (int)threadIdx.x;
+        d[j] = -1.f;
+        v[j] = -1.f;
+        if (i < npix) {
+          d[j] = D[i];
+          v[j] = V[i];
         }
-        chunk_total = s;
+      }
+      unsigned m[J];
+      float I[J];
+      const float* P = F.plane[l] + (size_t)y0 * w;
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const bool ok = d[j] > 0.f && v[j] > 0.f;
+        m[j] = __ballot_sync(0xffffffffu, ok);
+        I[j] = ok ? P[base + j * 256 + (int)threadIdx.x] : 0.f;  // in flight across the scan
+      }
+      if (lane < J) {
+        unsigned mm = m[0];
+#pragma unroll
+        for (int j = 1; j < J; ++j)
+          if (lane == j) mm = m[j];
+        off[lane * NWARP + wid] = __popc(mm);
       }
       __syncthreads();
-      if (valid) {
-        const int pos = pos0 + woff[wid] + __popc(m & ((1u << lane) - 1u));
-        const float z = 1.0f / d;
-        const float X = (((float)x - cx) * fxi) * z;
-        const float Y = (((float)y - cy) * fyi) * z;
-        F.pxyzi[l][pos] = make_float4(X, Y, z, F.plane[l][idx]);
-        F.pvar[l][pos] = v;
-        if (F.ppix[l]) F.ppix[l][pos] = (int)idx;
+      if (wid == 0) {  // exclusive scan of the (j, warp) counts, j-major = pixel order
+        const int c = off[lane];
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        off[lane] = incl - c;
+        if (lane == 31) chunk_total = incl;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        if ((m[j] >> lane) & 1u) {
+          const int i = base + j * 256 + (int)threadIdx.x;
+          const int x = i % w, y = y0 + i / w;
+          const size_t idx = (size_t)y * w + x;
+          const int pos = pos0 + off[j * NWARP + wid] + __popc(m[j] & lt);
+          const float z = 1.0f / d[j];
+          const float X = (((float)x - cx) * fxi) * z;
+          const float Y = (((float)y - cy) * fyi) * z;
+          F.pxyzi[l][pos] = make_float4(X, Y, z, I[j]);
+          F.pvar[l][pos] = v[j];
+          if (F.ppix[l]) F.ppix[l][pos] = (int)idx;
+        }
       }
       pos0 += chunk_total;
-      __syncthreads();  // woff / chunk_total are rewritten by the next chunk
+      __syncthreads();  // off / chunk_total are rewritten by the next chunk
     }
   }
 }
@@ -212,7 +303,7 @@ void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s) {
 int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, int max_h, bool with_grads,
                          cudaStream_t s) {
   const int bands = max_h >> (levels - 1);
-  band_build_kernel<<<dim3(bands, n), 256, 0, s>>>(frames);
+  band_build_kernel<<<dim3(bands, n, 2), 256, 0, s>>>(frames);
   if (!with_grads) return 1;
   gradient_kernel<<<dim3(cdiv(max_pix, 256), n, levels), 256, 0, s>>>(frames);
   return 2;
