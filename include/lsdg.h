@@ -316,6 +316,13 @@ LSDG_API lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* batch, double* f
 LSDG_API lsdg_status lsdg_batch_submit_se3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
                                            const float* ref_idepth, const float* ref_idepth_var,
                                            const float* new_images, const double* frame_to_ref_init);
+/* Same as lsdg_batch_submit_se3 with 8-bit images (row-major w x h bytes per frame, the camera's
+ * own format: upstream frames are built from 8-bit images and their level-0 float plane is the
+ * byte value, so results are identical to submitting the images as floats).  The bytes cross the
+ * bus, the conversion to float runs on the device behind the copy. */
+LSDG_API lsdg_status lsdg_batch_submit_se3_u8(lsdg_ctx* ctx, lsdg_batch* batch, const uint8_t* ref_images,
+                                              const float* ref_idepth, const float* ref_idepth_var,
+                                              const uint8_t* new_images, const double* frame_to_ref_init);
 LSDG_API lsdg_status lsdg_batch_submit_sim3(lsdg_ctx* ctx, lsdg_batch* batch, const float* ref_images,
                                             const float* ref_idepth, const float* ref_idepth_var,
                                             const float* new_images, const float* new_idepth,

@@ -29,6 +29,7 @@ namespace lsdg {
 int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, int max_h, bool with_grads,
                          cudaStream_t s);
 int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cudaStream_t s);
+void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
 }  // namespace lsdg
 
 #define CK(ctx, expr)                                         \
@@ -48,6 +49,7 @@ struct BatchSlot {
   lsdg_track_stats* d_stats = nullptr;
   int* d_work = nullptr;
   double* d_mid = nullptr;            // coarse-phase poses of a split run
+  uint8_t* d_u8 = nullptr;            // 8-bit staging of the level-0 images (allocated on first use)
   double* h_out = nullptr;            // pinned staging of the results
   lsdg_track_stats* h_stats = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -89,6 +91,7 @@ static void slot_free(BatchSlot& s) {
   if (s.d_stats) cudaFree(s.d_stats);
   if (s.d_work) cudaFree(s.d_work);
   if (s.d_mid) cudaFree(s.d_mid);
+  if (s.d_u8) cudaFree(s.d_u8);
   if (s.h_out) cudaFreeHost(s.h_out);
   if (s.h_stats) cudaFreeHost(s.h_stats);
   for (auto& e : s.ev)
@@ -224,14 +227,27 @@ static lsdg_status slot_run(lsdg_ctx* ctx, lsdg_batch* b, int si) {
 
 // Host -> device copies of one step's inputs into slot s on stream `st` (new_idepth / new_var:
 // Sim3 batches only).
+// Images as floats (ref_images / new_images) or as bytes (ref_u8 / new_u8: copied into the slot's
+// staging, then widened into the level-0 planes by a kernel on the same stream).
 static lsdg_status slot_upload(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, cudaStream_t st, const float* ref_images,
                                const float* ref_idepth, const float* ref_var, const float* new_images,
-                               const float* new_idepth, const float* new_var, const double* init) {
+                               const float* new_idepth, const float* new_var, const double* init,
+                               const uint8_t* ref_u8 = nullptr, const uint8_t* new_u8 = nullptr) {
   // keyframes first; all keyframes carry depth (and, for Sim3, the second half too)
-  const size_t half = (b->sim3 ? s.fs.pix_depth / 2 : s.fs.pix_depth) * 4;
+  const size_t npix = b->sim3 ? s.fs.pix_depth / 2 : s.fs.pix_depth;
+  const size_t half = npix * 4;
   char* base = (char*)s.fs.arena;
-  CK(ctx, cudaMemcpyAsync(s.fs.plane0, ref_images, half, cudaMemcpyHostToDevice, st));
-  CK(ctx, cudaMemcpyAsync((char*)s.fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, st));
+  if (ref_u8) {
+    if (2 * npix > (size_t)INT32_MAX) return ctx_fail(ctx, LSDG_INVALID_ARG, "batch too large for 8-bit staging");
+    if (!s.d_u8) CK(ctx, cudaMalloc(&s.d_u8, 2 * npix));
+    CK(ctx, cudaMemcpyAsync(s.d_u8, ref_u8, npix, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync(s.d_u8 + npix, new_u8, npix, cudaMemcpyHostToDevice, st));
+    launch_u8_to_plane(s.d_u8, s.fs.plane0, (int)(2 * npix), st);
+    CK(ctx, cudaGetLastError());
+  } else {
+    CK(ctx, cudaMemcpyAsync(s.fs.plane0, ref_images, half, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync((char*)s.fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, st));
+  }
   CK(ctx, cudaMemcpyAsync(base + s.fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, st));
   CK(ctx, cudaMemcpyAsync(base + s.fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, st));
   if (b->sim3) {
@@ -303,7 +319,8 @@ static lsdg_status batch_create(lsdg_ctx* ctx, int n, const int* widths, const i
 // One pipelined step: upload into the free slot on the copy stream, run its graph behind the
 // upload, read the results back behind the graph.
 static lsdg_status batch_submit(lsdg_ctx* ctx, lsdg_batch* b, const float* ri, const float* rd, const float* rv,
-                                const float* ni, const float* nd, const float* nv, const double* init) {
+                                const float* ni, const float* nd, const float* nv, const double* init,
+                                const uint8_t* ri8 = nullptr, const uint8_t* ni8 = nullptr) {
   if (b->n_inflight >= 2) return ctx_fail(ctx, LSDG_INVALID_ARG, "two steps in flight: collect one first");
   const int si = b->next;
   BatchSlot& s = b->slot[si];
@@ -314,13 +331,13 @@ static lsdg_status batch_submit(lsdg_ctx* ctx, lsdg_batch* b, const float* ri, c
   if (!b->copy) CK(ctx, cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
   if (!s.exec || s.graph_epoch != ctx->params_epoch) {
     // first use of this slot (or new parameters): upload on the context stream, then tune/capture
-    lsdg_status st = slot_upload(ctx, b, s, ctx->stream, ri, rd, rv, ni, nd, nv, init);
+    lsdg_status st = slot_upload(ctx, b, s, ctx->stream, ri, rd, rv, ni, nd, nv, init, ri8, ni8);
     if (st == LSDG_OK) st = slot_run(ctx, b, si);
     if (st != LSDG_OK) return st;
   } else {
     // the slot's arena is free once its previous step has finished (event `done`)
     CK(ctx, cudaStreamWaitEvent(b->copy, s.done, 0));
-    lsdg_status st = slot_upload(ctx, b, s, b->copy, ri, rd, rv, ni, nd, nv, init);
+    lsdg_status st = slot_upload(ctx, b, s, b->copy, ri, rd, rv, ni, nd, nv, init, ri8, ni8);
     if (st != LSDG_OK) return st;
     CK(ctx, cudaEventRecord(s.copied, b->copy));
     CK(ctx, cudaStreamWaitEvent(ctx->stream, s.copied, 0));
@@ -441,6 +458,14 @@ lsdg_status lsdg_batch_submit_se3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref
     return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
   if (b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 batch: use lsdg_batch_submit_sim3");
   return batch_submit(ctx, b, ref_images, ref_idepth, ref_var, new_images, nullptr, nullptr, init);
+}
+
+lsdg_status lsdg_batch_submit_se3_u8(lsdg_ctx* ctx, lsdg_batch* b, const uint8_t* ref_images, const float* ref_idepth,
+                                     const float* ref_var, const uint8_t* new_images, const double* init) {
+  if (!ctx || !b || !ref_images || !ref_idepth || !ref_var || !new_images || !init)
+    return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (b->sim3) return ctx_fail(ctx, LSDG_INVALID_ARG, "Sim3 batch: use lsdg_batch_submit_sim3");
+  return batch_submit(ctx, b, nullptr, ref_idepth, ref_var, nullptr, nullptr, nullptr, init, ref_images, new_images);
 }
 
 lsdg_status lsdg_batch_submit_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,

@@ -80,6 +80,7 @@ def lib():
     _sig(L, "lsdg_batch_read", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_track_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p, _f64p, C.POINTER(T.TrackStats)])
     _sig(L, "lsdg_batch_submit_se3", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p])
+    _sig(L, "lsdg_batch_submit_se3_u8", st, [_vp, _vp, _vp, _vp, _vp, _vp, _f64p])
     _sig(L, "lsdg_batch_submit_sim3", st, [_vp, _vp] + [_vp] * 6 + [_f64p])
     _sig(L, "lsdg_batch_load_frames", st, [_vp, _vp, _vp, _vp, _f64p])
     _sig(L, "lsdg_batch_collect", st, [_vp, _vp, _f64p, C.POINTER(T.TrackStats)])
@@ -383,6 +384,19 @@ class Batch:
         self._pending = getattr(self, "_pending", []) + [arrs]
         self.ctx.check(lib().lsdg_batch_submit_se3(self.ctx.handle, self._h, *[self._ptr(a) for a in arrs],
                                                    np.ascontiguousarray(init, np.float64).reshape(-1)))
+
+    def submit_u8(self, ref_images, ref_idepth, ref_var, new_images, init):
+        """submit() with 8-bit images (lsdg_batch_submit_se3_u8): the bytes cross the bus and are
+        widened on the device; results equal submit() with the same images as floats."""
+        for a in (ref_images, new_images):
+            assert a.dtype == np.uint8 and a.flags["C_CONTIGUOUS"] and a.size == self.npix, (a.dtype, a.size, self.npix)
+        for a in (ref_idepth, ref_var):
+            assert a.size == self.npix, (a.size, self.npix)
+        arrs = (ref_images, ref_idepth, ref_var, new_images)
+        self._pending = getattr(self, "_pending", []) + [arrs]
+        self.ctx.check(lib().lsdg_batch_submit_se3_u8(self.ctx.handle, self._h, ref_images.ctypes.data,
+                                                      self._ptr(ref_idepth), self._ptr(ref_var), new_images.ctypes.data,
+                                                      np.ascontiguousarray(init, np.float64).reshape(-1)))
 
     def submit_sim3(self, ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var, init):
         arrs = (ref_images, ref_idepth, ref_var, new_images, new_idepth, new_var)

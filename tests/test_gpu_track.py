@@ -159,6 +159,27 @@ def test_pipelined_batch_equals_synchronous(ctx):
     b.close()
 
 
+def test_pipelined_u8_images_equal_float(ctx):
+    """submit_u8 (8-bit images, widened to float on the device behind the copy) gives the float
+    results bit for bit when the float images hold the same byte values, on the first step (graph
+    capture) and on a replay."""
+    pairs = [synth.tracking_pair(400 + i, 320, 240) for i in range(3)]
+    b = lsdg.Batch(ctx, [320] * 3, [240] * 3, [p.intr for p in pairs])
+    init = np.stack([np.eye(3, 4)] * 3)
+    ri, rd, rv, ni = [np.ascontiguousarray(a) for a in lsdg.pack_pairs(pairs)]
+    ri8 = np.clip(np.rint(ri), 0, 255).astype(np.uint8)
+    ni8 = np.clip(np.rint(ni), 0, 255).astype(np.uint8)
+    ref, ref_st = b.track(ri8.astype(np.float32), rd, rv, ni8.astype(np.float32), init)
+    for _ in range(3):
+        b.submit_u8(ri8, rd, rv, ni8, init)
+        out, st = b.collect()
+        np.testing.assert_array_equal(out, ref)
+        assert [s.n_good for s in st] == [s.n_good for s in ref_st]
+    with pytest.raises(AssertionError):
+        b.submit_u8(ri, rd, rv, ni8, init)       # float images refused by the binding
+    b.close()
+
+
 def test_batch_with_lost_pair(ctx):
     pairs = [synth.tracking_pair(200, 320, 240), synth.tracking_pair(201, 320, 240)]
     pairs[1].ref_idepth = np.full_like(pairs[1].ref_idepth, -1.0)
