@@ -19,6 +19,16 @@
 
 namespace lsdg {
 
+// Row of flat pixel index i in a level w pixels wide, without a division per pixel: with
+// M = floor((2^64 - 1) / w) + 1, M w = 2^64 + e (0 <= e < w), so the high word of i M is
+// floor(i / w + i e / (w 2^64)), which is floor(i / w) whenever i e < 2^64 (any 32-bit i).
+struct RowDiv {
+  unsigned long long m;
+  int w;
+  __device__ explicit RowDiv(int w_) : m(0xffffffffffffffffull / (unsigned long long)w_ + 1ull), w(w_) {}
+  __device__ int row(int i) const { return (int)__umul64hi((unsigned long long)i, m); }
+};
+
 // 8-bit input image -> level-0 intensity plane.
 __global__ void u8_to_plane_kernel(const uint8_t* __restrict__ src, float* __restrict__ dst, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -44,6 +54,7 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
     const float* P = F.plane[l - 1];
     float* Q = F.plane[l] + (size_t)y0 * w;
     const int n = rows * w, pw = 2 * w;
+    const RowDiv rd(w);
     // B outputs per thread per round: their 2 B float2 loads are in flight together
     constexpr int B = 2;
     for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
@@ -52,7 +63,7 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
       for (int u = 0; u < B; ++u) {
         const int i = i0 + u * 256;
         if (i < n) {
-          const int x = i % w, y = y0 + i / w;
+          const int r = rd.row(i), x = i - r * w, y = y0 + r;
           const float* a = P + (size_t)(2 * y) * pw + 2 * x;
           r0[u] = *reinterpret_cast<const float2*>(a);
           r1[u] = *reinterpret_cast<const float2*>(a + pw);
@@ -103,6 +114,7 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
       }
     } else {
       const int pw = 2 * w, n = rows * w;
+      const RowDiv rd(w);
       const float* Dp = F.idepth[l - 1];
       const float* Vp = F.ivar[l - 1];
       float* Dq = F.idepth[l] + (size_t)y0 * w;
@@ -114,7 +126,7 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
         for (int u = 0; u < B; ++u) {
           const int i = i0 + u * 256;
           if (i < n) {
-            const int x = i % w, y = y0 + i / w;
+            const int r = rd.row(i), x = i - r * w, y = y0 + r;
             const size_t c0 = (size_t)(2 * y) * pw + 2 * x;
             d0[u] = *reinterpret_cast<const float2*>(Dp + c0);
             d1[u] = *reinterpret_cast<const float2*>(Dp + c0 + pw);
@@ -222,6 +234,7 @@ __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __res
   for (int l = 0; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
     const int npix = rows * w;
+    const RowDiv rd(w);
     const float* D = F.idepth[l] + (size_t)y0 * w;
     const float* V = F.ivar[l] + (size_t)y0 * w;
     int pos0 = F.blk_count[l][band];
@@ -271,7 +284,7 @@ __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __res
       for (int j = 0; j < J; ++j) {
         if ((m[j] >> lane) & 1u) {
           const int i = base + j * 256 + (int)threadIdx.x;
-          const int x = i % w, y = y0 + i / w;
+          const int r = rd.row(i), x = i - r * w, y = y0 + r;
           const size_t idx = (size_t)y * w + x;
           const int pos = pos0 + off[j * NWARP + wid] + __popc(m[j] & lt);
           const float z = 1.0f / d[j];
