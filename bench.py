@@ -630,7 +630,7 @@ def bench_sim3(ctx, stream, sps, args):
     ms = e0.elapsed_time(e1) / k
     out, stats = b.read()
     scale_err = [abs(out[i][12] / sps[i].frame_to_ref13[12] - 1.0) for i in range(len(sps))]
-    res = {"workload": "%d Sim3 trackings 640x480 (7-dof, FP64 7x7 solve) in one launch" % len(sps),
+    res = {"workload": "%d Sim3 trackings 640x480 (7-dof, 7x7 solve) in one launch" % len(sps),
            "ms_per_batch": ms, "trackings_per_s": len(sps) / (ms / 1e3), "shape": b.shape(),
            "max_gt_scale_err": float(max(scale_err)), "lost": sum(1 for s in stats if s.status != 0)}
     b.close()
