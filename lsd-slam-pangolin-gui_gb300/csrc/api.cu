@@ -378,11 +378,11 @@ lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc,
   return launch_phase(ctx, a, tc.threads, tc.minblocks, tc.cluster, tc.max_clusters, sim3);
 }
 
-// Times one launch shape on `a` (best of two runs).
+// Times one launch shape on `a` (best of three runs).
 static lsdg_status time_phase(lsdg_ctx* ctx, const TrackArgs& a, int nt, int mb, int c, int mc, bool sim3,
                               cudaEvent_t e0, cudaEvent_t e1, float* ms_out) {
   float t_best = 1e30f;
-  for (int rep = 0; rep < 2; ++rep) {
+  for (int rep = 0; rep < 3; ++rep) {
     CK(ctx, cudaEventRecord(e0, ctx->stream));
     lsdg_status st = launch_phase(ctx, a, nt, mb, c, mc, sim3);
     if (st != LSDG_OK) return st;
@@ -428,7 +428,7 @@ static lsdg_status best_phase(lsdg_ctx* ctx, const TrackArgs& a, const int* clus
 // The environment variable LSDG_TRACK_SHAPE="threads,cluster" pins the shape instead (used to
 // profile one known configuration); it is ignored when that shape does not fit the device.
 // Picks the tracker's launch plan for a workload signature by timing candidates on the caller's
-// own data (two runs each, best kept): the best single launch over all levels, and, when the caller
+// own data (three runs each, best kept): the best single launch over all levels, and, when the caller
 // provides pose scratch, split runs (coarse levels first with each pair on a cluster of 1, 2 or 4 CTAs,
 // then the finer levels with their own best shape).  The fastest plan is cached per context.
 // LSDG_TRACK_SHAPE="threads,cluster[,minblocks]" pins a single-launch shape;

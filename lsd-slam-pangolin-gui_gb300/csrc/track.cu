@@ -1201,7 +1201,7 @@ static int max_clusters_nt(int cluster) {
   return n;
 }
 
-#define LSDG_TRACK_SHAPES(X) X(128, 4) X(128, 6) X(128, 8) X(256, 2) X(256, 3) X(256, 4) X(512, 1) X(512, 2)
+#define LSDG_TRACK_SHAPES(X) X(128, 4) X(128, 8) X(256, 2) X(256, 4) X(512, 1) X(512, 2)
 
 // Per context, outside any stream capture: allows clusters of up to 16 CTAs (non-portable size)
 // for every instantiation and uploads the sim(3) series coefficients.
