@@ -366,6 +366,10 @@ LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* thr
  * (split = -1: a single launch over all levels). */
 LSDG_API lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* batch, int* split, int* threads, int* minblocks,
                                       int* cluster);
+/* Read back the tracking reference points the batch's last step built for pair `pair`'s keyframe at
+ * one level (the layout of lsdg_frame_get_points; synchronises the context stream). */
+LSDG_API lsdg_status lsdg_batch_get_points(lsdg_ctx* ctx, lsdg_batch* batch, int pair, int level, float* xyzi,
+                                           float* var, int capacity, int* count);
 /* Residual passes the last lsdg_batch_run executed, summed over pairs and levels, and the
  * algorithmic bytes those passes read (points + frame levels + sums). */
 LSDG_API lsdg_status lsdg_batch_work(lsdg_ctx* ctx, lsdg_batch* batch, int64_t* passes,

@@ -30,6 +30,9 @@ int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix
                          cudaStream_t s);
 int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cudaStream_t s);
 void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
+size_t frame_build_ws_bytes(int n, int levels, int max_h);
+int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
+                       unsigned long long* ws, cudaStream_t s);
 }  // namespace lsdg
 
 #define CK(ctx, expr)                                         \
@@ -50,6 +53,8 @@ struct BatchSlot {
   int* d_work = nullptr;
   double* d_mid = nullptr;            // coarse-phase poses of a split run
   uint8_t* d_u8 = nullptr;            // 8-bit staging of the level-0 images (allocated on first use)
+  unsigned long long* d_scan = nullptr;  // one-launch build workspace (ticket, error word, band counts)
+  unsigned* h_err = nullptr;          // pinned copy of the build's error word
   double* h_out = nullptr;            // pinned staging of the results
   lsdg_track_stats* h_stats = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -92,6 +97,8 @@ static void slot_free(BatchSlot& s) {
   if (s.d_work) cudaFree(s.d_work);
   if (s.d_mid) cudaFree(s.d_mid);
   if (s.d_u8) cudaFree(s.d_u8);
+  if (s.d_scan) cudaFree(s.d_scan);
+  if (s.h_err) cudaFreeHost(s.h_err);
   if (s.h_out) cudaFreeHost(s.h_out);
   if (s.h_stats) cudaFreeHost(s.h_stats);
   for (auto& e : s.ev)
@@ -133,6 +140,9 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   if (e == cudaSuccess) e = cudaMalloc(&s.d_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_stats, sizeof(lsdg_track_stats) * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_work, sizeof(int) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_scan, frame_build_ws_bytes(2 * b->n, s.fs.levels, s.fs.max_h));
+  if (e == cudaSuccess) e = cudaMallocHost(&s.h_err, sizeof(unsigned));
+  if (e == cudaSuccess) *s.h_err = 0;
   if (e == cudaSuccess) e = cudaMalloc(&s.d_mid, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_stats, sizeof(lsdg_track_stats) * n);
@@ -163,11 +173,9 @@ static TrackArgs slot_track_args(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
 }
 
 static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, int* launches) {
-  // band pass over all 2n frames (also the depth pyramids of the second keyframes in Sim3 mode);
-  // reference points only for the first n
-  const int L = ctx->params.levels;
-  int k = launch_frame_pyramid(s.fs.d_frames, 2 * b->n, L, s.fs.max_pix, s.fs.max_h, false, ctx->stream);
-  k += launch_frame_points(s.fs.d_frames, b->n, L, s.fs.max_h, ctx->stream);
+  // one launch over all 2n frames: pyramids (also the depth pyramids of the second keyframes in
+  // Sim3 mode), reference points only for the first n
+  int k = launch_frame_build(s.fs.d_frames, 2 * b->n, b->n, s.fs.levels, s.fs.max_h, s.d_scan, ctx->stream);
   CK(ctx, cudaGetLastError());
   *launches = k;
   return LSDG_OK;
@@ -255,6 +263,14 @@ static lsdg_status slot_upload(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, cudaS
     CK(ctx, cudaMemcpyAsync(base + s.fs.off_var0 + half, new_var, half, cudaMemcpyHostToDevice, st));
   }
   CK(ctx, cudaMemcpyAsync(s.d_init, init, sizeof(double) * b->pose_len * b->n, cudaMemcpyHostToDevice, st));
+  return LSDG_OK;
+}
+
+// The step's one-launch build reports a band wait that ran out (its error word, copied back with
+// the results): the poses of that step are not to be trusted.
+static lsdg_status build_error(lsdg_ctx* ctx, const BatchSlot& s) {
+  if (s.h_err && *s.h_err)
+    return ctx_fail(ctx, LSDG_TIMEOUT, "keyframe build: a band's wait for the point counts of the bands before it ran out");
   return LSDG_OK;
 }
 
@@ -346,6 +362,8 @@ static lsdg_status batch_submit(lsdg_ctx* ctx, lsdg_batch* b, const float* ri, c
   }
   CK(ctx, cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaMemcpyAsync(s.h_stats, s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(s.h_err, reinterpret_cast<unsigned*>(s.d_scan) + 1, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                          ctx->stream));
   CK(ctx, cudaEventRecord(s.done, ctx->stream));
   b->inflight[b->n_inflight++] = si;
   b->next = si ^ 1;
@@ -446,10 +464,12 @@ lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* b, double* out, lsdg_trac
   BatchSlot& s = b->slot[0];
   CK(ctx, cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
   CK(ctx, cudaMemcpyAsync(s.h_stats, s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaMemcpyAsync(s.h_err, reinterpret_cast<unsigned*>(s.d_scan) + 1, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                          ctx->stream));
   CK(ctx, cudaStreamSynchronize(ctx->stream));
   if (out) std::memcpy(out, s.h_out, sizeof(double) * b->pose_len * b->n);
   if (stats) std::memcpy(stats, s.h_stats, sizeof(lsdg_track_stats) * b->n);
-  return LSDG_OK;
+  return build_error(ctx, s);
 }
 
 lsdg_status lsdg_batch_submit_se3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
@@ -490,7 +510,7 @@ lsdg_status lsdg_batch_collect(lsdg_ctx* ctx, lsdg_batch* b, double* out, lsdg_t
   b->inflight[0] = b->inflight[1];
   b->inflight[1] = -1;
   --b->n_inflight;
-  return LSDG_OK;
+  return build_error(ctx, s);
 }
 
 lsdg_status lsdg_batch_track_sim3(lsdg_ctx* ctx, lsdg_batch* b, const float* ref_images, const float* ref_idepth,
@@ -567,6 +587,27 @@ lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* b, int* split, int* thre
   if (threads) *threads = b->tc.c_threads;
   if (minblocks) *minblocks = b->tc.c_minblocks;
   if (cluster) *cluster = b->tc.c_cluster;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_get_points(lsdg_ctx* ctx, lsdg_batch* b, int pair, int level, float* xyzi, float* var,
+                                  int capacity, int* count) {
+  if (!ctx || !b || !count) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (pair < 0 || pair >= b->n) return ctx_fail(ctx, LSDG_INVALID_ARG, "pair out of range");
+  const BatchSlot& s = b->slot[b->last];
+  if (!s.ready) return ctx_fail(ctx, LSDG_INVALID_ARG, "the batch has not run");
+  const FrameDev& F = s.fs.h_frames[pair];
+  if (level < 0 || level >= F.levels) return ctx_fail(ctx, LSDG_INVALID_ARG, "level out of range");
+  if (b->n_inflight) CK(ctx, cudaEventSynchronize(s.done));
+  int c = 0;
+  CK(ctx, cudaMemcpyAsync(ctx->h_small, F.pcount + level, 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
+  std::memcpy(&c, ctx->h_small, 4);
+  *count = c;
+  if (c > capacity) return ctx_fail(ctx, LSDG_INVALID_ARG, "capacity %d < %d points", capacity, c);
+  if (xyzi && c) CK(ctx, cudaMemcpyAsync(xyzi, F.pxyzi[level], (size_t)c * 16, cudaMemcpyDeviceToHost, ctx->stream));
+  if (var && c) CK(ctx, cudaMemcpyAsync(var, F.pvar[level], (size_t)c * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(ctx, cudaStreamSynchronize(ctx->stream));
   return LSDG_OK;
 }
 

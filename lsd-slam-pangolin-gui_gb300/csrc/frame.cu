@@ -35,20 +35,14 @@ __global__ void u8_to_plane_kernel(const uint8_t* __restrict__ src, float* __res
   if (i < n) dst[i] = (float)src[i];
 }
 
-// Pass 1, one CTA per (band, frame): intensity levels 1..L-1 of the band; for keyframes also the
-// depth pyramid (level 0 sanitised in place: idepth <= 0 or var <= 0 -> -1, written only where the
-// value is not -1 already; level l: inverse-variance weighted mean of the valid 2x2 children,
-// variance = n / sum(1/var)) and the number of valid pixels of the band at every level.  Each
-// thread counts its own pixels of a level; one block reduction per level.  The intensity pyramid
-// (blockIdx.z = 0) and the depth pyramid (blockIdx.z = 1) of a band are built by different CTAs.
-__global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __restrict__ frames) {
-  const FrameDev& F = frames[blockIdx.y];
+// ------------------------------------------------------------------------------------------
+// The per-band steps (one CTA of 256 threads owns one band of 2^(L-1) level-0 rows)
+// ------------------------------------------------------------------------------------------
+
+// Intensity levels 1..L-1 of the band (2x2 means of the level above, rows of the same band).
+__device__ __forceinline__ void band_intensity(const FrameDev& F, int band) {
   const int L = F.levels;
   const int band_rows = 1 << (L - 1);
-  const int band = blockIdx.x;
-  if (band * band_rows >= F.h) return;
-  __shared__ int wsum[8];
-  if (blockIdx.z == 0) {
   for (int l = 1; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
     const float* P = F.plane[l - 1];
@@ -77,9 +71,15 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
     }
     __syncthreads();  // level l is read by level l + 1 (other threads of this CTA)
   }
-  return;
-  }
-  if (!F.has_depth) return;
+}
+
+// Depth pyramid of the band (level 0 sanitised in place: idepth <= 0 or var <= 0 -> -1, written
+// only where the value is not -1 already; level l: inverse-variance weighted mean of the valid 2x2
+// children, variance = n / sum(1/var)) and its valid pixels per level into cnt[l] (shared memory,
+// visible to the whole CTA on return).  Each thread counts its own pixels; one block sum per level.
+__device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt, int* wsum) {
+  const int L = F.levels;
+  const int band_rows = 1 << (L - 1);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int l = 0; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
@@ -89,11 +89,11 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
       float* V = F.ivar[0] + (size_t)y0 * w;
       const int n = rows * w;
       constexpr int B = 4;
-      for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
+      for (int base = 0; base < n; base += 256 * B) {
         float d[B], v[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-          const int i = i0 + u * 256;
+          const int i = base + u * 256 + (int)threadIdx.x;
           d[u] = -1.f;
           v[u] = -1.f;
           if (i < n) {
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
         }
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-          const int i = i0 + u * 256;
+          const int i = base + u * 256 + (int)threadIdx.x;
           const bool valid = d[u] > 0.f && v[u] > 0.f;
           count += valid ? 1 : 0;
           if (i < n && !valid && !(d[u] == -1.f && v[u] == -1.f)) {
@@ -120,11 +120,11 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
       float* Dq = F.idepth[l] + (size_t)y0 * w;
       float* Vq = F.ivar[l] + (size_t)y0 * w;
       constexpr int B = 2;
-      for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
+      for (int base = 0; base < n; base += 256 * B) {
         float2 d0[B], d1[B], v0[B], v1[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-          const int i = i0 + u * 256;
+          const int i = base + u * 256 + (int)threadIdx.x;
           if (i < n) {
             const int r = rd.row(i), x = i - r * w, y = y0 + r;
             const size_t c0 = (size_t)(2 * y) * pw + 2 * x;
@@ -136,7 +136,8 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
         }
 #pragma unroll
         for (int u = 0; u < B; ++u) {
-          const int i = i0 + u * 256;
+          const int i = base + u * 256 + (int)threadIdx.x;
+          bool valid = false;
           if (i < n) {
             const float dd[4] = {d0[u].x, d0[u].y, d1[u].x, d1[u].y};
             const float vv[4] = {v0[u].x, v0[u].y, v1[u].x, v1[u].y};
@@ -151,7 +152,7 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
                 ++nv;
               }
             }
-            const bool valid = nv > 0;
+            valid = nv > 0;
             count += valid ? 1 : 0;
             Dq[i] = valid ? swd / sw : -1.f;
             Vq[i] = valid ? (float)nv / sw : -1.f;
@@ -167,10 +168,111 @@ __global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __re
     if (threadIdx.x == 0) {
       int t = 0;
       for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += wsum[k];
-      F.blk_count[l][band] = t;
+      cnt[l] = t;
     }
-    __syncthreads();  // wsum is rewritten by the next level
+    __syncthreads();  // wsum is rewritten by the next level; cnt[l] is visible
   }
+}
+
+// The band's valid pixels of every level as SoA points {X, Y, Z, I} + var, in row-major order,
+// level l starting at pos[l] (shared memory).  A chunk is 4 x 256 pixels (pixel base + 256 j +
+// thread, j = 0..3): one ballot per j and warp, one warp-wide scan of the 32 (j, warp) counts, so
+// three barriers per 1024 pixels.  off: 32 ints of shared memory, total: one.
+__device__ __forceinline__ void band_points(const FrameDev& F, int band, const int* pos, int* off, int* total) {
+  const int L = F.levels;
+  const int band_rows = 1 << (L - 1);
+  constexpr int J = 4, NWARP = 8;  // blockDim.x == 256
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int l = 0; l < L; ++l) {
+    const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
+    const int npix = rows * w;
+    const RowDiv rd(w);
+    const float* D = F.idepth[l] + (size_t)y0 * w;
+    const float* V = F.ivar[l] + (size_t)y0 * w;
+    const float* P = F.plane[l] + (size_t)y0 * w;
+    int pos0 = pos[l];
+    const float cx = F.cx[l], cy = F.cy[l], fxi = F.fxi[l], fyi = F.fyi[l];
+    for (int base = 0; base < npix; base += J * 256) {
+      float d[J], v[J];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const int i = base + j * 256 + (int)threadIdx.x;
+        d[j] = -1.f;
+        v[j] = -1.f;
+        if (i < npix) {
+          d[j] = D[i];
+          v[j] = V[i];
+        }
+      }
+      unsigned m[J];
+      float I[J];
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        const bool ok = d[j] > 0.f && v[j] > 0.f;
+        m[j] = __ballot_sync(0xffffffffu, ok);
+        I[j] = ok ? P[base + j * 256 + (int)threadIdx.x] : 0.f;  // in flight across the scan
+      }
+      if (lane < J) {
+        unsigned mm = m[0];
+#pragma unroll
+        for (int j = 1; j < J; ++j)
+          if (lane == j) mm = m[j];
+        off[lane * NWARP + wid] = __popc(mm);
+      }
+      __syncthreads();
+      if (wid == 0) {  // exclusive scan of the (j, warp) counts, j-major = pixel order
+        const int c = off[lane];
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        off[lane] = incl - c;
+        if (lane == 31) *total = incl;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < J; ++j) {
+        if ((m[j] >> lane) & 1u) {
+          const int i = base + j * 256 + (int)threadIdx.x;
+          const int r = rd.row(i), x = i - r * w, y = y0 + r;
+          const size_t idx = (size_t)y * w + x;
+          const int p = pos0 + off[j * NWARP + wid] + __popc(m[j] & lt);
+          const float z = 1.0f / d[j];
+          const float X = (((float)x - cx) * fxi) * z;
+          const float Y = (((float)y - cy) * fyi) * z;
+          F.pxyzi[l][p] = make_float4(X, Y, z, I[j]);
+          F.pvar[l][p] = v[j];
+          if (F.ppix[l]) F.ppix[l][p] = (int)idx;
+        }
+      }
+      pos0 += *total;
+      __syncthreads();  // off / total are rewritten by the next chunk
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Three-launch build (single frames): pyramids and band counts, scan, scatter
+// ------------------------------------------------------------------------------------------
+
+// One CTA per (band, frame, part): part 0 the intensity pyramid, part 1 (frames with depth) the
+// depth pyramid and the band's valid pixels per level (blk_count).
+__global__ void __launch_bounds__(256, 5) band_build_kernel(const FrameDev* __restrict__ frames) {
+  const FrameDev& F = frames[blockIdx.y];
+  const int band = blockIdx.x;
+  if (band * (1 << (F.levels - 1)) >= F.h) return;
+  __shared__ int wsum[8];
+  __shared__ int cnt[kMaxLevels];
+  if (blockIdx.z == 0) {
+    band_intensity(F, band);
+    return;
+  }
+  if (!F.has_depth) return;
+  band_depth(F, band, cnt, wsum);
+  if ((int)threadIdx.x < F.levels) F.blk_count[threadIdx.x][band] = cnt[threadIdx.x];
 }
 
 // Gradients of every level for frames that keep the float4 {I, gx, gy, 0} pyramid (central
@@ -215,90 +317,83 @@ __global__ void __launch_bounds__(32) point_scan_kernel(const FrameDev* __restri
   if (lane == 0) F.pcount[level] = carry;
 }
 
-// Pass 2, one CTA per (band, keyframe): the valid pixels of every level of the band as SoA points
-// {X, Y, Z, I} + var, in row-major order, starting at the band's offset.  A chunk is 4 x 256 pixels
-// (pixel base + 256 j + thread, j = 0..3): one ballot per j and warp, one warp-wide scan of the
-// 32 (j, warp) counts, so three barriers per 1024 pixels.
+// One CTA per (band, keyframe): the band's points from the offsets point_scan_kernel left.
 __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __restrict__ frames) {
   const FrameDev& F = frames[blockIdx.y];
   if (!F.has_depth) return;
-  const int L = F.levels;
-  const int band_rows = 1 << (L - 1);
   const int band = blockIdx.x;
-  if (band * band_rows >= F.h) return;
-  constexpr int J = 4, NWARP = 8;  // blockDim.x == 256
-  __shared__ int off[J * NWARP];
-  __shared__ int chunk_total;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int l = 0; l < L; ++l) {
-    const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
-    const int npix = rows * w;
-    const RowDiv rd(w);
-    const float* D = F.idepth[l] + (size_t)y0 * w;
-    const float* V = F.ivar[l] + (size_t)y0 * w;
-    int pos0 = F.blk_count[l][band];
-    const float cx = F.cx[l], cy = F.cy[l], fxi = F.fxi[l], fyi = F.fyi[l];
-    for (int base = 0; base < npix; base += J * 256) {
-      float d[J], v[J];
-#pragma unroll
-      for (int j = 0; j < J; ++j) {
-        const int i = base + j * 256 + (int)threadIdx.x;
-        d[j] = -1.f;
-        v[j] = -1.f;
-        if (i < npix) {
-          d[j] = D[i];
-          v[j] = V[i];
+  if (band * (1 << (F.levels - 1)) >= F.h) return;
+  __shared__ int pos[kMaxLevels];
+  __shared__ int off[32];
+  __shared__ int total;
+  if ((int)threadIdx.x < F.levels) pos[threadIdx.x] = F.blk_count[threadIdx.x][band];
+  __syncthreads();
+  band_points(F, band, pos, off, &total);
+}
+
+// ------------------------------------------------------------------------------------------
+// One-launch build (batches): every band's pyramids, then its points at offsets found in the
+// same launch by a decoupled look-back over the bands before it
+// ------------------------------------------------------------------------------------------
+// Workspace (zeroed before the launch): word 0 = {ticket, error}, then one status word per
+// (frame, band, level): 0 = nothing yet, 1 << 32 | n = the band's own count, 2 << 32 | n = the
+// count of bands 0..band inclusive.  A CTA takes the next ticket as its (frame, band) in
+// frame-major, band-minor order, so every band it waits for has started (tickets are issued in CTA
+// start order) and waits only for bands that started before it: no wait can be circular.  Each
+// wait is bounded; when one runs out the CTA records the error word, counts what it has, and its
+// point writes stay inside the level's arrays (offsets never exceed the true ones).
+constexpr int kBuildSpinLimit = 1 << 20;
+
+__global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __restrict__ frames, int n_frames,
+                                                             int n_point_frames, int bands,
+                                                             unsigned long long* __restrict__ ws) {
+  __shared__ int s_ticket;
+  __shared__ int wsum[8];
+  __shared__ int cnt[kMaxLevels];
+  __shared__ int pos[kMaxLevels];
+  __shared__ int off[32];
+  __shared__ int total;
+  if (threadIdx.x == 0) s_ticket = (int)atomicAdd(reinterpret_cast<unsigned int*>(ws), 1u);
+  __syncthreads();
+  const int t = s_ticket;
+  const int fi = t / bands, band = t % bands;
+  if (fi >= n_frames) return;
+  const FrameDev& F = frames[fi];
+  const int L = F.levels;
+  const int nb = F.h >> (L - 1);
+  if (band >= nb) return;
+  band_intensity(F, band);
+  if (!F.has_depth) return;
+  band_depth(F, band, cnt, wsum);
+  if (fi >= n_point_frames) return;
+  if ((int)threadIdx.x < L) {
+    const int l = threadIdx.x;
+    volatile unsigned long long* st = ws + 1 + (size_t)fi * bands * kMaxLevels;
+    const unsigned c = (unsigned)cnt[l];
+    unsigned prefix = 0;
+    if (band > 0) {
+      st[band * kMaxLevels + l] = (1ull << 32) | c;
+      for (int j = band - 1; j >= 0; --j) {
+        unsigned long long wv = st[j * kMaxLevels + l];
+        for (int it = 0; (wv >> 32) == 0ull; ++it) {
+          if (it == kBuildSpinLimit) {
+            atomicExch(reinterpret_cast<unsigned int*>(ws) + 1, 1u);
+            wv = 2ull << 32;  // give up on the bands before: offsets stay below the true ones
+            break;
+          }
+          __nanosleep(128);
+          wv = st[j * kMaxLevels + l];
         }
+        prefix += (unsigned)wv;
+        if ((wv >> 32) == 2ull) break;
       }
-      unsigned m[J];
-      float I[J];
-      const float* P = F.plane[l] + (size_t)y0 * w;
-#pragma unroll
-      for (int j = 0; j < J; ++j) {
-        const bool ok = d[j] > 0.f && v[j] > 0.f;
-        m[j] = __ballot_sync(0xffffffffu, ok);
-        I[j] = ok ? P[base + j * 256 + (int)threadIdx.x] : 0.f;  // in flight across the scan
-      }
-      if (lane < J) {
-        unsigned mm = m[0];
-#pragma unroll
-        for (int j = 1; j < J; ++j)
-          if (lane == j) mm = m[j];
-        off[lane * NWARP + wid] = __popc(mm);
-      }
-      __syncthreads();
-      if (wid == 0) {  // exclusive scan of the (j, warp) counts, j-major = pixel order
-        const int c = off[lane];
-        int incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int t = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += t;
-        }
-        off[lane] = incl - c;
-        if (lane == 31) chunk_total = incl;
-      }
-      __syncthreads();
-#pragma unroll
-      for (int j = 0; j < J; ++j) {
-        if ((m[j] >> lane) & 1u) {
-          const int i = base + j * 256 + (int)threadIdx.x;
-          const int r = rd.row(i), x = i - r * w, y = y0 + r;
-          const size_t idx = (size_t)y * w + x;
-          const int pos = pos0 + off[j * NWARP + wid] + __popc(m[j] & lt);
-          const float z = 1.0f / d[j];
-          const float X = (((float)x - cx) * fxi) * z;
-          const float Y = (((float)y - cy) * fyi) * z;
-          F.pxyzi[l][pos] = make_float4(X, Y, z, I[j]);
-          F.pvar[l][pos] = v[j];
-          if (F.ppix[l]) F.ppix[l][pos] = (int)idx;
-        }
-      }
-      pos0 += chunk_total;
-      __syncthreads();  // off / chunk_total are rewritten by the next chunk
     }
+    st[band * kMaxLevels + l] = (2ull << 32) | (prefix + c);
+    pos[l] = (int)prefix;
+    if (band == nb - 1) F.pcount[l] = (int)(prefix + c);
   }
+  __syncthreads();
+  band_points(F, band, pos, off, &total);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -320,6 +415,22 @@ int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix
   if (!with_grads) return 1;
   gradient_kernel<<<dim3(cdiv(max_pix, 256), n, levels), 256, 0, s>>>(frames);
   return 2;
+}
+
+// Bytes of the one-launch build's workspace for n frames of at most max_h rows.
+size_t frame_build_ws_bytes(int n, int levels, int max_h) {
+  return sizeof(unsigned long long) * (1 + (size_t)n * (max_h >> (levels - 1)) * kMaxLevels);
+}
+
+// One launch: intensity pyramids of frames[0..n), depth pyramids of those that carry depth,
+// reference points of the first n_point_frames (which must all carry depth).  ws: the zeroed
+// workspace (frame_build_ws_bytes; zeroed here on the stream).  Returns the launches issued.
+int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
+                       unsigned long long* ws, cudaStream_t s) {
+  const int bands = max_h >> (levels - 1);
+  cudaMemsetAsync(ws, 0, frame_build_ws_bytes(n, levels, max_h), s);
+  frame_build_kernel<<<bands * n, 256, 0, s>>>(frames, n, n_point_frames, bands, ws);
+  return 1;
 }
 
 // Reference points of the frames among frames[0..n) that carry depth (band_build_kernel must have

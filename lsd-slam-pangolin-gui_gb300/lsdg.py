@@ -87,6 +87,7 @@ def lib():
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
     _sig(L, "lsdg_batch_split", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 4)
+    _sig(L, "lsdg_batch_get_points", st, [_vp, _vp, C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.POINTER(C.c_int)])
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
     _sig(L, "lsdg_depth_create", st, [_vp, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
     _sig(L, "lsdg_depth_destroy", st, [_vp, _vp])
@@ -459,6 +460,15 @@ class Batch:
             out["coarse_phase"] = {"levels_from": sp.value, "threads": ct.value, "minblocks": cm.value,
                                    "cluster": cc.value}
         return out
+
+    def points(self, pair: int, l: int):
+        """Reference points the last step built for pair `pair`'s keyframe at level l: (n, 4), (n,)."""
+        cap = (int(self.widths[pair]) >> l) * (int(self.heights[pair]) >> l)
+        xyzi = np.zeros(4 * cap, np.float32)
+        var = np.zeros(cap, np.float32)
+        n = C.c_int()
+        self.ctx.check(lib().lsdg_batch_get_points(self.ctx.handle, self._h, pair, l, xyzi, var, cap, C.byref(n)))
+        return xyzi[:4 * n.value].reshape(-1, 4), var[:n.value]
 
     def work(self):
         p, b, u = C.c_int64(), C.c_double(), C.c_double()

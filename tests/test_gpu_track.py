@@ -111,6 +111,26 @@ def _mixed_pairs():
     return [synth.tracking_pair(100 + i, w, h) for i, (w, h) in enumerate(sizes)]
 
 
+def test_batch_build_points_bit_exact(ctx):
+    """The batch's one-launch build (pyramids, then each band's points at offsets found by a look-back
+    over the bands before it) gives every keyframe's points bit for bit, mixed sizes, every level;
+    again after a graph replay."""
+    pairs = _mixed_pairs()
+    b = lsdg.Batch(ctx, [p.w for p in pairs], [p.h for p in pairs], [p.intr for p in pairs])
+    ri, rd, rv, ni = lsdg.pack_pairs(pairs)
+    init = np.stack([np.eye(3, 4)] * len(pairs))
+    for _ in range(2):
+        b.track(ri, rd, rv, ni, init)
+        for i in (0, 3, 7, 8):
+            p = pairs[i]
+            _, _, P, PV = lsdo.keyframe(p.ref_image, p.ref_idepth, p.ref_idepth_var, p.intr, 5)
+            for l in range(5):
+                xyzi, pv = b.points(i, l)
+                np.testing.assert_array_equal(xyzi, P[l])
+                np.testing.assert_array_equal(pv, PV[l])
+    b.close()
+
+
 def test_batch_matches_oracle_per_pair(ctx):
     pairs = _mixed_pairs()
     b = lsdg.Batch(ctx, [p.w for p in pairs], [p.h for p in pairs], [p.intr for p in pairs])
