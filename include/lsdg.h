@@ -366,6 +366,11 @@ LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* thr
  * (split = -1: a single launch over all levels). */
 LSDG_API lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* batch, int* split, int* threads, int* minblocks,
                                       int* cluster);
+/* Test hook for the batch build's bounded wait: in the following steps band 0 of keyframe `frame`
+ * publishes no point counts, so the other bands of that keyframe wait until their limit and the
+ * step reports LSDG_TIMEOUT from lsdg_batch_read / _collect (the context stays usable; -1 turns it
+ * off).  The step's graph is captured again. */
+LSDG_API lsdg_status lsdg_batch_test_withhold(lsdg_ctx* ctx, lsdg_batch* batch, int frame);
 /* Read back the tracking reference points the batch's last step built for pair `pair`'s keyframe at
  * one level (the layout of lsdg_frame_get_points; synchronises the context stream). */
 LSDG_API lsdg_status lsdg_batch_get_points(lsdg_ctx* ctx, lsdg_batch* batch, int pair, int level, float* xyzi,

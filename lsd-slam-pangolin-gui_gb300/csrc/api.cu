@@ -281,6 +281,7 @@ lsdg_status frameset_alloc(lsdg_ctx* ctx, FrameSet& fs, int n, const int* w, con
         F.ppix[l] = grads ? (int*)(base + r.ppix[l]) : nullptr;
         F.blk_count[l] = (int*)(base + r.blk[l]);
       }
+      F.rowdiv[l] = 0xffffffffffffffffull / (unsigned long long)(w[i] >> l) + 1ull;
       F.fx[l] = (float)fx; F.fy[l] = (float)fy; F.cx[l] = (float)cx; F.cy[l] = (float)cy;
       F.fxi[l] = (float)(1.0 / fx); F.fyi[l] = (float)(1.0 / fy);
       fx *= 0.5; fy *= 0.5;

@@ -32,7 +32,7 @@ int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cu
 void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
 size_t frame_build_ws_bytes(int n, int levels, int max_h);
 int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
-                       unsigned long long* ws, cudaStream_t s);
+                       unsigned long long* ws, cudaStream_t s, int withhold_frame);
 }  // namespace lsdg
 
 #define CK(ctx, expr)                                         \
@@ -76,6 +76,7 @@ struct lsdg_batch {
   BatchSlot slot[2];
   int last = 0;                 // slot of the last run (timing / work)
   int* d_order = nullptr;
+  int test_withhold = -1;  // lsdg_batch_test_withhold: keyframe whose band 0 publishes no counts
   int* h_counts = nullptr;
   cudaStream_t copy = nullptr;  // upload stream of the pipelined form
   int inflight[2] = {-1, -1};   // slots of the submitted, not yet collected steps (oldest first)
@@ -175,7 +176,8 @@ static TrackArgs slot_track_args(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
 static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, int* launches) {
   // one launch over all 2n frames: pyramids (also the depth pyramids of the second keyframes in
   // Sim3 mode), reference points only for the first n
-  int k = launch_frame_build(s.fs.d_frames, 2 * b->n, b->n, s.fs.levels, s.fs.max_h, s.d_scan, ctx->stream);
+  int k = launch_frame_build(s.fs.d_frames, 2 * b->n, b->n, s.fs.levels, s.fs.max_h, s.d_scan, ctx->stream,
+                             b->test_withhold);
   CK(ctx, cudaGetLastError());
   *launches = k;
   return LSDG_OK;
@@ -587,6 +589,16 @@ lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* b, int* split, int* thre
   if (threads) *threads = b->tc.c_threads;
   if (minblocks) *minblocks = b->tc.c_minblocks;
   if (cluster) *cluster = b->tc.c_cluster;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_batch_test_withhold(lsdg_ctx* ctx, lsdg_batch* b, int frame) {
+  if (!ctx || !b) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (frame < -1 || frame >= b->n) return ctx_fail(ctx, LSDG_INVALID_ARG, "frame out of range");
+  lsdg_status st = no_pipeline(ctx, b);
+  if (st != LSDG_OK) return st;
+  b->test_withhold = frame;
+  for (auto& s : b->slot) s.graph_epoch = -1;  // capture again with the new launch argument
   return LSDG_OK;
 }
 

@@ -19,13 +19,12 @@
 
 namespace lsdg {
 
-// Row of flat pixel index i in a level w pixels wide, without a division per pixel: with
-// M = floor((2^64 - 1) / w) + 1, M w = 2^64 + e (0 <= e < w), so the high word of i M is
+// Row of flat pixel index i at level l, without a division: with M = floor((2^64 - 1) / w) + 1
+// (FrameDev::rowdiv, from the host), M w = 2^64 + e (0 <= e < w), so the high word of i M is
 // floor(i / w + i e / (w 2^64)), which is floor(i / w) whenever i e < 2^64 (any 32-bit i).
 struct RowDiv {
   unsigned long long m;
-  int w;
-  __device__ explicit RowDiv(int w_) : m(0xffffffffffffffffull / (unsigned long long)w_ + 1ull), w(w_) {}
+  __device__ RowDiv(const FrameDev& F, int l) : m(F.rowdiv[l]) {}
   __device__ int row(int i) const { return (int)__umul64hi((unsigned long long)i, m); }
 };
 
@@ -48,7 +47,7 @@ __device__ __forceinline__ void band_intensity(const FrameDev& F, int band) {
     const float* P = F.plane[l - 1];
     float* Q = F.plane[l] + (size_t)y0 * w;
     const int n = rows * w, pw = 2 * w;
-    const RowDiv rd(w);
+    const RowDiv rd(F, l);
     // B outputs per thread per round: their 2 B float2 loads are in flight together
     constexpr int B = 2;
     for (int i0 = threadIdx.x; i0 < n; i0 += 256 * B) {
@@ -114,7 +113,7 @@ __device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt
       }
     } else {
       const int pw = 2 * w, n = rows * w;
-      const RowDiv rd(w);
+      const RowDiv rd(F, l);
       const float* Dp = F.idepth[l - 1];
       const float* Vp = F.ivar[l - 1];
       float* Dq = F.idepth[l] + (size_t)y0 * w;
@@ -187,7 +186,7 @@ __device__ __forceinline__ void band_points(const FrameDev& F, int band, const i
   for (int l = 0; l < L; ++l) {
     const int w = F.w >> l, rows = band_rows >> l, y0 = (band * band_rows) >> l;
     const int npix = rows * w;
-    const RowDiv rd(w);
+    const RowDiv rd(F, l);
     const float* D = F.idepth[l] + (size_t)y0 * w;
     const float* V = F.ivar[l] + (size_t)y0 * w;
     const float* P = F.plane[l] + (size_t)y0 * w;
@@ -344,9 +343,11 @@ __global__ void __launch_bounds__(256) band_scatter_kernel(const FrameDev* __res
 // point writes stay inside the level's arrays (offsets never exceed the true ones).
 constexpr int kBuildSpinLimit = 1 << 20;
 
+// withhold_frame (>= 0 only in tests of the bounded wait): band 0 of that frame publishes nothing,
+// so the frame's other bands wait until their limit and the error word is set.
 __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __restrict__ frames, int n_frames,
                                                              int n_point_frames, int bands,
-                                                             unsigned long long* __restrict__ ws) {
+                                                             unsigned long long* __restrict__ ws, int withhold_frame) {
   __shared__ int s_ticket;
   __shared__ int wsum[8];
   __shared__ int cnt[kMaxLevels];
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __r
         if ((wv >> 32) == 2ull) break;
       }
     }
-    st[band * kMaxLevels + l] = (2ull << 32) | (prefix + c);
+    if (!(band == 0 && fi == withhold_frame)) st[band * kMaxLevels + l] = (2ull << 32) | (prefix + c);
     pos[l] = (int)prefix;
     if (band == nb - 1) F.pcount[l] = (int)(prefix + c);
   }
@@ -426,10 +427,10 @@ size_t frame_build_ws_bytes(int n, int levels, int max_h) {
 // reference points of the first n_point_frames (which must all carry depth).  ws: the zeroed
 // workspace (frame_build_ws_bytes; zeroed here on the stream).  Returns the launches issued.
 int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
-                       unsigned long long* ws, cudaStream_t s) {
+                       unsigned long long* ws, cudaStream_t s, int withhold_frame) {
   const int bands = max_h >> (levels - 1);
   cudaMemsetAsync(ws, 0, frame_build_ws_bytes(n, levels, max_h), s);
-  frame_build_kernel<<<bands * n, 256, 0, s>>>(frames, n, n_point_frames, bands, ws);
+  frame_build_kernel<<<bands * n, 256, 0, s>>>(frames, n, n_point_frames, bands, ws, withhold_frame);
   return 1;
 }
 

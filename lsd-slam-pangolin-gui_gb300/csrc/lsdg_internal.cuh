@@ -42,6 +42,9 @@ struct FrameDev {
   int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per band, then offsets
   float fx[kMaxLevels], fy[kMaxLevels], cx[kMaxLevels], cy[kMaxLevels];
   float fxi[kMaxLevels], fyi[kMaxLevels];
+  // floor((2^64 - 1) / (w >> l)) + 1: the row of a flat pixel index at level l is the high word of
+  // index * rowdiv[l] (computed on the host; a 64-bit division per thread is costly on the GPU)
+  unsigned long long rowdiv[kMaxLevels];
 };
 
 struct PairDev {

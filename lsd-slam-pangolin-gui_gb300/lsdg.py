@@ -87,6 +87,7 @@ def lib():
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
     _sig(L, "lsdg_batch_split", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 4)
+    _sig(L, "lsdg_batch_test_withhold", st, [_vp, _vp, C.c_int])
     _sig(L, "lsdg_batch_get_points", st, [_vp, _vp, C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.POINTER(C.c_int)])
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
     _sig(L, "lsdg_depth_create", st, [_vp, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(_vp)])
@@ -460,6 +461,10 @@ class Batch:
             out["coarse_phase"] = {"levels_from": sp.value, "threads": ct.value, "minblocks": cm.value,
                                    "cluster": cc.value}
         return out
+
+    def test_withhold(self, frame: int):
+        """Test hook of the build's bounded wait (lsdg_batch_test_withhold; -1 turns it off)."""
+        self.ctx.check(lib().lsdg_batch_test_withhold(self.ctx.handle, self._h, frame))
 
     def points(self, pair: int, l: int):
         """Reference points the last step built for pair `pair`'s keyframe at level l: (n, 4), (n,)."""

@@ -131,6 +131,27 @@ def test_batch_build_points_bit_exact(ctx):
     b.close()
 
 
+def test_build_wait_that_runs_out_is_reported(ctx):
+    """A band whose predecessor never publishes its counts (the test hook withholds band 0's) waits
+    until its limit; the step reports TIMEOUT, nothing faults, and the next step is correct."""
+    pairs = [synth.tracking_pair(600 + i, 320, 240) for i in range(2)]
+    ri, rd, rv, ni = [np.ascontiguousarray(a) for a in lsdg.pack_pairs(pairs)]
+    init = np.stack([np.eye(3, 4)] * 2)
+    ref = lsdg.Batch(ctx, [320] * 2, [240] * 2, [p.intr for p in pairs])
+    want, _ = ref.track(ri, rd, rv, ni, init)
+    ref.close()
+    b = lsdg.Batch(ctx, [320] * 2, [240] * 2, [p.intr for p in pairs])
+    b.test_withhold(1)
+    with pytest.raises(lsdg.LsdgError) as e:
+        b.track(ri, rd, rv, ni, init)
+    assert e.value.status == T.TIMEOUT
+    b.test_withhold(-1)
+    got, st = b.track(ri, rd, rv, ni, init)
+    np.testing.assert_array_equal(got, want)
+    assert all(s.status == T.OK for s in st)
+    b.close()
+
+
 def test_batch_matches_oracle_per_pair(ctx):
     pairs = _mixed_pairs()
     b = lsdg.Batch(ctx, [p.w for p in pairs], [p.h for p in pairs], [p.intr for p in pairs])
