@@ -302,7 +302,7 @@ __device__ __forceinline__ void warp_exp_mul(const X* xi, const double* Tin, dou
 // (H + lambda diag H) x = -g for N x N symmetric H given as its upper triangle (row-major), by an
 // LDL^T factorisation of the Jacobi-scaled system (row and column j times 1/sqrt(H_jj), so the
 // factorised matrix has the diagonal 1 + lambda) held in float registers.  Returns false when a
-// pivot is not positive.  The warp's four-system solve (warp_solve) computes the same thing.
+// pivot is not positive.  The LM step's four speculative solves and its rare further solves use it.
 template <int N>
 __device__ __forceinline__ bool ldlt_solve_reg(const float* __restrict__ hu, const float* __restrict__ g,
                                                float lambda, float* x) {
@@ -357,8 +357,8 @@ __device__ __forceinline__ bool ldlt_solve_reg(const float* __restrict__ hu, con
   return ok;
 }
 
-// Solves computed ahead of the LM decision by warp 0, four systems at once (lanes 8g .. 8g+N-1 own
-// the rows of system g): [0] undamped step of the pass just merged, [1] damped step if that pass is
+// Solves computed ahead of the LM decision by warp 0, four systems at once (lane g solves system
+// g): [0] undamped step of the pass just merged, [1] damped step if that pass is
 // accepted (or is a level's first pass), [2] and [3] damped steps on the kept linearisation after
 // one or two rejections.  The decision logic takes an entry only when source and lambda match.
 struct SolveCache {
@@ -368,87 +368,7 @@ struct SolveCache {
   int src[4];  // 0: the sums of the pass just merged, 1: the sums kept from an earlier pass
   int ok[4];
   int valid[4];
-  float Ls[4][8][8];  // per-group L of the factorisation (row-major), for the back substitution
 };
-
-// Row-per-lane LDL^T solve of (H + lambda diag H) x = -g (N <= 7) for the group of 8 lanes starting
-// at `base` (rows 0..N-1; the other lanes of the group mirror row N-1 and their results are dropped),
-// on the Jacobi-scaled system like ldlt_solve_reg.  hu: upper triangle of H (row-major), g: right-
-// hand side, both float in shared memory.  Also leaves max |x_i| in *gnout.
-template <int N>
-__device__ __forceinline__ void warp_solve(const float* __restrict__ hu, const float* __restrict__ g, float lambda,
-                                           int lane, float (*Ls)[8], float* xout, int* okout, float* gnout) {
-  const int base = lane & ~7;
-  const int r = (lane & 7) < N ? (lane & 7) : N - 1;
-  float a[N], l[N], wv[N], inv[N], sc[N];
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-    const float h = hu[j * N - (j * (j - 1)) / 2];
-    sc[j] = h > 0.f ? rsqrtf(h) : 1.f;
-  }
-  float sr = sc[0];
-#pragma unroll
-  for (int j = 1; j < N; ++j)
-    if (j == r) sr = sc[j];
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-    const int lo = r < j ? r : j, hi = r < j ? j : r;
-    a[j] = (hu[lo * N - (lo * (lo - 1)) / 2 + (hi - lo)] * sr) * sc[j];
-    l[j] = 0.0f;
-    wv[j] = 0.0f;
-  }
-#pragma unroll
-  for (int j = 0; j < N; ++j)
-    if (j == r) a[j] = a[j] * (1.0f + lambda);
-  bool ok = true;
-#pragma unroll
-  for (int j = 0; j < N; ++j) {
-    float t = a[j];
-#pragma unroll
-    for (int k = 0; k < j; ++k) t = t - l[k] * __shfl_sync(0xffffffffu, wv[k], base + j);  // L_rk * (L_jk d_k)
-    const float dj = __shfl_sync(0xffffffffu, t, base + j);
-    ok = ok && (dj > 1e-20f);
-    inv[j] = 1.0f / dj;
-    if (r > j) {
-      l[j] = t * inv[j];
-      wv[j] = t;
-    }
-  }
-  // forward: y_r = -g_r - sum_{k<r} L_rk y_k, column by column
-  float y = -(g[r] * sr);
-#pragma unroll
-  for (int k = 0; k < N; ++k) {
-    const float yk = __shfl_sync(0xffffffffu, y, base + k);
-    if (r > k) y = y - l[k] * yk;
-  }
-  float ir = inv[0];
-#pragma unroll
-  for (int j = 1; j < N; ++j)
-    if (j == r) ir = inv[j];
-  y = y * ir;
-  // backward: x_r = y_r - sum_{k>r} L_kr x_k (L rows exchanged through shared memory)
-  if ((lane & 7) < N) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) Ls[r][k] = l[k];
-  }
-  __syncwarp();
-  float x = y;
-#pragma unroll
-  for (int k = N - 1; k >= 0; --k) {
-    const float xk = __shfl_sync(0xffffffffu, x, base + k);
-    if (r < k) x = x - Ls[k][r] * xk;
-  }
-  x = x * sr;
-  float m = (lane & 7) < N ? fabsf(x) : 0.f;
-  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));
-  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 2));
-  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 4));
-  if ((lane & 7) < N) xout[r] = x;
-  if ((lane & 7) == 0) {
-    *okout = ok ? 1 : 0;
-    *gnout = m;
-  }
-}
 
 // ------------------------------------------------------------------------------------------
 // LM control (thread 0 of cluster rank 0)
@@ -681,24 +601,33 @@ __device__ __noinline__ void lm_continue(const TrackArgs& a, LMState& lm, Ctl& c
   else next_level<SIM3>(a, lm, ctl);
 }
 
-// Warp 0 of cluster rank 0 solves the four systems the decision may need (see SolveCache).
+// Warp 0 of cluster rank 0 solves the four systems the decision may need (see SolveCache): lane g
+// solves system g in registers (a dependency chain of ~N pivots, no shuffles).
 template <bool SIM3>
 __device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm, const double* tot, const float* totf,
                                           SolveCache& sc, int lane) {
   using Md = Mode<SIM3>;
-  const int grp = lane >> 3;
+  if (lane >= 4) return;
+  const int grp = lane;
   const bool init = lm.phase == PH_INIT;
   const float* S = grp >= 2 ? lm.Sf : totf;
   const float lam = grp == 0 ? 0.0f
                   : grp == 1 ? (init ? a.lambda0 : lm.lambda * a.lambda_down)
                   : grp == 2 ? lm.lambda * a.lambda_up
                              : (lm.lambda * a.lambda_up) * a.lambda_up;
-  warp_solve<Md::DOF>(S, S + Md::NH, lam, lane, sc.Ls[grp], sc.x[grp], &sc.ok[grp], &sc.gn[grp]);
-  if ((lane & 7) == 0) {
-    sc.lambda[grp] = lam;
-    sc.src[grp] = grp >= 2 ? 1 : 0;
-    sc.valid[grp] = (tot[Md::NS] > 0 && (grp < 2 || !init)) ? 1 : 0;
+  float x[Md::DOF];
+  const bool ok = ldlt_solve_reg<Md::DOF>(S, S + Md::NH, lam, x);
+  float m = 0.f;
+#pragma unroll
+  for (int i = 0; i < Md::DOF; ++i) {
+    sc.x[grp][i] = x[i];
+    m = fmaxf(m, fabsf(x[i]));
   }
+  sc.ok[grp] = ok ? 1 : 0;
+  sc.gn[grp] = m;
+  sc.lambda[grp] = lam;
+  sc.src[grp] = grp >= 2 ? 1 : 0;
+  sc.valid[grp] = (tot[Md::NS] > 0 && (grp < 2 || !init)) ? 1 : 0;
 }
 
 // ------------------------------------------------------------------------------------------
