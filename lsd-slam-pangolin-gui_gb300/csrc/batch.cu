@@ -29,10 +29,10 @@ namespace lsdg {
 int launch_frame_pyramid(const FrameDev* frames, int n, int levels, long max_pix, int max_h, bool with_grads,
                          cudaStream_t s);
 int launch_frame_points(const FrameDev* frames, int n, int levels, int max_h, cudaStream_t s);
-void launch_u8_to_plane(const uint8_t* src, float* dst, int n, cudaStream_t s);
 size_t frame_build_ws_bytes(int n, int levels, int max_h);
 int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
-                       unsigned long long* ws, cudaStream_t s, int withhold_frame);
+                       unsigned long long* ws, cudaStream_t s, int withhold_frame, const uint8_t* u8,
+                       const float* plane0, const int* mode);
 }  // namespace lsdg
 
 #define CK(ctx, expr)                                         \
@@ -52,7 +52,9 @@ struct BatchSlot {
   lsdg_track_stats* d_stats = nullptr;
   int* d_work = nullptr;
   double* d_mid = nullptr;            // coarse-phase poses of a split run
-  uint8_t* d_u8 = nullptr;            // 8-bit staging of the level-0 images (allocated on first use)
+  uint8_t* d_u8 = nullptr;            // 8-bit staging of the level-0 images (SE3 batches)
+  int* d_mode = nullptr;              // 1: this step's level-0 images are the bytes in d_u8
+  int* h_mode = nullptr;              // pinned {0, 1}: the sources of the mode word
   unsigned long long* d_scan = nullptr;  // one-launch build workspace (ticket, error word, band counts)
   unsigned* h_err = nullptr;          // pinned copy of the build's error word
   double* h_out = nullptr;            // pinned staging of the results
@@ -98,6 +100,8 @@ static void slot_free(BatchSlot& s) {
   if (s.d_work) cudaFree(s.d_work);
   if (s.d_mid) cudaFree(s.d_mid);
   if (s.d_u8) cudaFree(s.d_u8);
+  if (s.d_mode) cudaFree(s.d_mode);
+  if (s.h_mode) cudaFreeHost(s.h_mode);
   if (s.d_scan) cudaFree(s.d_scan);
   if (s.h_err) cudaFreeHost(s.h_err);
   if (s.h_out) cudaFreeHost(s.h_out);
@@ -144,6 +148,14 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   if (e == cudaSuccess) e = cudaMalloc(&s.d_scan, frame_build_ws_bytes(2 * b->n, s.fs.levels, s.fs.max_h));
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_err, sizeof(unsigned));
   if (e == cudaSuccess) *s.h_err = 0;
+  if (e == cudaSuccess && !b->sim3) e = cudaMalloc(&s.d_u8, s.fs.pix_total);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_mode, sizeof(int));
+  if (e == cudaSuccess) e = cudaMallocHost(&s.h_mode, 2 * sizeof(int));
+  if (e == cudaSuccess) {
+    s.h_mode[0] = 0;
+    s.h_mode[1] = 1;
+    e = cudaMemsetAsync(s.d_mode, 0, sizeof(int), ctx->stream);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&s.d_mid, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_stats, sizeof(lsdg_track_stats) * n);
@@ -177,7 +189,7 @@ static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, int
   // one launch over all 2n frames: pyramids (also the depth pyramids of the second keyframes in
   // Sim3 mode), reference points only for the first n
   int k = launch_frame_build(s.fs.d_frames, 2 * b->n, b->n, s.fs.levels, s.fs.max_h, s.d_scan, ctx->stream,
-                             b->test_withhold);
+                             b->test_withhold, s.d_u8, s.fs.plane0, s.d_mode);
   CK(ctx, cudaGetLastError());
   *launches = k;
   return LSDG_OK;
@@ -248,15 +260,15 @@ static lsdg_status slot_upload(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, cudaS
   const size_t half = npix * 4;
   char* base = (char*)s.fs.arena;
   if (ref_u8) {
-    if (2 * npix > (size_t)INT32_MAX) return ctx_fail(ctx, LSDG_INVALID_ARG, "batch too large for 8-bit staging");
-    if (!s.d_u8) CK(ctx, cudaMalloc(&s.d_u8, 2 * npix));
+    // the bytes go to the staging (laid out like the level-0 planes); the build widens them
+    if (!s.d_u8) return ctx_fail(ctx, LSDG_INVALID_ARG, "8-bit images need an SE3 batch");
     CK(ctx, cudaMemcpyAsync(s.d_u8, ref_u8, npix, cudaMemcpyHostToDevice, st));
     CK(ctx, cudaMemcpyAsync(s.d_u8 + npix, new_u8, npix, cudaMemcpyHostToDevice, st));
-    launch_u8_to_plane(s.d_u8, s.fs.plane0, (int)(2 * npix), st);
-    CK(ctx, cudaGetLastError());
+    CK(ctx, cudaMemcpyAsync(s.d_mode, s.h_mode + 1, sizeof(int), cudaMemcpyHostToDevice, st));
   } else {
     CK(ctx, cudaMemcpyAsync(s.fs.plane0, ref_images, half, cudaMemcpyHostToDevice, st));
     CK(ctx, cudaMemcpyAsync((char*)s.fs.plane0 + half, new_images, half, cudaMemcpyHostToDevice, st));
+    CK(ctx, cudaMemcpyAsync(s.d_mode, s.h_mode, sizeof(int), cudaMemcpyHostToDevice, st));
   }
   CK(ctx, cudaMemcpyAsync(base + s.fs.off_id0, ref_idepth, half, cudaMemcpyHostToDevice, st));
   CK(ctx, cudaMemcpyAsync(base + s.fs.off_var0, ref_var, half, cudaMemcpyHostToDevice, st));
@@ -439,6 +451,7 @@ lsdg_status lsdg_batch_load_frames(lsdg_ctx* ctx, lsdg_batch* b, const lsdg_fram
     const FrameDev& Kj = s.fs.h_frames[b->n + i];
     const size_t bytes = (size_t)b->w[i] * b->h[i] * 4;
     const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    if (i == 0) CK(ctx, cudaMemcpyAsync(s.d_mode, s.h_mode, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     CK(ctx, cudaMemcpyAsync(Ki.plane[0], R.plane[0], bytes, d2d, ctx->stream));
     CK(ctx, cudaMemcpyAsync(Ki.idepth[0], R.idepth[0], bytes, d2d, ctx->stream));
     CK(ctx, cudaMemcpyAsync(Ki.ivar[0], R.ivar[0], bytes, d2d, ctx->stream));

@@ -39,7 +39,10 @@ __global__ void u8_to_plane_kernel(const uint8_t* __restrict__ src, float* __res
 // ------------------------------------------------------------------------------------------
 
 // Intensity levels 1..L-1 of the band (2x2 means of the level above, rows of the same band).
-__device__ __forceinline__ void band_intensity(const FrameDev& F, int band) {
+// src8 (or nullptr): the frame's 8-bit level-0 image; level 1 then reads the bytes and also writes
+// the level-0 float plane (each level-0 pixel belongs to exactly one 2x2 block), so an 8-bit upload
+// needs no separate widening pass.  (float)byte is exact: the planes equal a float upload's.
+__device__ __forceinline__ void band_intensity(const FrameDev& F, int band, const uint8_t* src8 = nullptr) {
   const int L = F.levels;
   const int band_rows = 1 << (L - 1);
   for (int l = 1; l < L; ++l) {
@@ -57,9 +60,18 @@ __device__ __forceinline__ void band_intensity(const FrameDev& F, int band) {
         const int i = i0 + u * 256;
         if (i < n) {
           const int r = rd.row(i), x = i - r * w, y = y0 + r;
-          const float* a = P + (size_t)(2 * y) * pw + 2 * x;
-          r0[u] = *reinterpret_cast<const float2*>(a);
-          r1[u] = *reinterpret_cast<const float2*>(a + pw);
+          const size_t o = (size_t)(2 * y) * pw + 2 * x;
+          if (l == 1 && src8) {
+            const uchar2 b0 = *reinterpret_cast<const uchar2*>(src8 + o);
+            const uchar2 b1 = *reinterpret_cast<const uchar2*>(src8 + o + pw);
+            r0[u] = make_float2((float)b0.x, (float)b0.y);
+            r1[u] = make_float2((float)b1.x, (float)b1.y);
+            *reinterpret_cast<float2*>(F.plane[0] + o) = r0[u];
+            *reinterpret_cast<float2*>(F.plane[0] + o + pw) = r1[u];
+          } else {
+            r0[u] = *reinterpret_cast<const float2*>(P + o);
+            r1[u] = *reinterpret_cast<const float2*>(P + o + pw);
+          }
         }
       }
 #pragma unroll
@@ -345,9 +357,13 @@ constexpr int kBuildSpinLimit = 1 << 20;
 
 // withhold_frame (>= 0 only in tests of the bounded wait): band 0 of that frame publishes nothing,
 // so the frame's other bands wait until their limit and the error word is set.
+// u8 / plane0 / mode: when *mode is 1 the level-0 images are the bytes at u8 (laid out like the
+// float planes from plane0 on) and the build widens them (band_intensity).
 __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __restrict__ frames, int n_frames,
                                                              int n_point_frames, int bands,
-                                                             unsigned long long* __restrict__ ws, int withhold_frame) {
+                                                             unsigned long long* __restrict__ ws, int withhold_frame,
+                                                             const uint8_t* __restrict__ u8,
+                                                             const float* __restrict__ plane0, const int* __restrict__ mode) {
   __shared__ int s_ticket;
   __shared__ int wsum[8];
   __shared__ int cnt[kMaxLevels];
@@ -363,7 +379,8 @@ __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __r
   const int L = F.levels;
   const int nb = F.h >> (L - 1);
   if (band >= nb) return;
-  band_intensity(F, band);
+  const uint8_t* src8 = (mode && *mode == 1) ? u8 + (F.plane[0] - plane0) : nullptr;
+  band_intensity(F, band, src8);
   if (!F.has_depth) return;
   band_depth(F, band, cnt, wsum);
   if (fi >= n_point_frames) return;
@@ -427,10 +444,12 @@ size_t frame_build_ws_bytes(int n, int levels, int max_h) {
 // reference points of the first n_point_frames (which must all carry depth).  ws: the zeroed
 // workspace (frame_build_ws_bytes; zeroed here on the stream).  Returns the launches issued.
 int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
-                       unsigned long long* ws, cudaStream_t s, int withhold_frame) {
+                       unsigned long long* ws, cudaStream_t s, int withhold_frame, const uint8_t* u8,
+                       const float* plane0, const int* mode) {
   const int bands = max_h >> (levels - 1);
   cudaMemsetAsync(ws, 0, frame_build_ws_bytes(n, levels, max_h), s);
-  frame_build_kernel<<<bands * n, 256, 0, s>>>(frames, n, n_point_frames, bands, ws, withhold_frame);
+  frame_build_kernel<<<bands * n, 256, 0, s>>>(frames, n, n_point_frames, bands, ws, withhold_frame, u8, plane0,
+                                               mode);
   return 1;
 }
 
