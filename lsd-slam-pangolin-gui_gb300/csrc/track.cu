@@ -11,21 +11,25 @@
 // GB300 design.  One persistent kernel tracks any number of pairs.  Each pair is owned by one
 // thread-block cluster (C CTAs of NT threads, C up to 16); clusters pull pairs from an atomic work
 // queue (largest first).  A residual pass over a level's points is:
-//   1. every thread walks the SoA points with stride C*NT (coalesced float4 loads), warps the point
-//      with the current pose, samples the new frame's intensity with the C1 Catmull-Rom
-//      interpolant and its exact derivative (4x4 taps, L1/L2 resident), and accumulates the
-//      21 + 6 + 1 Kahan-compensated float sums of J^T W J, J^T W r and the Huber energy.  The
-//      first pass of a level fixes each point's residual variance in the psig scratch array (and
-//      leaves out points that do not land border_margin pixels inside the image), so each level
-//      minimises one fixed, continuous energy whose gradient is exactly 2 J^T W r;
+//   1. every thread walks the SoA points with stride C*NT (coalesced float4 loads; SE3: two points
+//      per iteration without branches, the next two prefetched), warps the point with the current
+//      pose, samples the new frame's intensity with the C1 Catmull-Rom interpolant and its exact
+//      derivative (4x4 taps, L1/L2 resident), and accumulates the 21 + 6 + 1 float sums of J^T W J,
+//      J^T W r and the Huber energy (gradient and energy Kahan-compensated; SE3 Hessian sums plain
+//      per thread).  The first pass of a level fixes each point's residual variance in the psig
+//      scratch array (and leaves out points that do not land border_margin pixels inside the
+//      image), so each level minimises one fixed, continuous energy whose gradient is exactly
+//      2 J^T W r;
 //   2. warp shuffles merge the compensated pairs (reduce-scatter), then a fixed-order block merge;
 //   2'. every CTA stores its partial straight into rank 0's shared memory (distributed shared
 //      memory stores, no global-memory scratch); cluster.sync(); rank 0 merges the C partials in
 //      fixed rank order, so the result is deterministic for a given C and NT;
-//   4. warp 0 of rank 0 runs the LM step in FP64: three lanes solve the 6x6 systems the decision
-//      may need (undamped; damped if accepted; damped if rejected) in parallel with register-
-//      resident LDL^T, then lane 0 decides (accept / reject, convergence, level changes), applies
-//      the se(3) exp and composition, and writes the next pose into every rank's shared memory;
+//   4. warp 0 of rank 0 runs the LM step: four lanes solve the systems the decision may need
+//      (undamped; damped if accepted; damped after one or two rejections) with register-resident
+//      LDL^T of the Jacobi-scaled system in float, lane 0 decides (accept / reject by an FP64
+//      energy comparison, convergence, level changes), the warp copies the record and the pose,
+//      12 lanes compose exp(step) with the FP64 pose, and the next pose goes into every rank's
+//      shared memory;
 //   5. cluster.sync(); every CTA reads the pose from its own shared memory and starts the next pass.
 // The whole LM loop over all levels therefore runs on the device without a host round trip and
 // without global-memory scratch for the reduction.  The one-pair form (lsdg_track_se3) is the same
@@ -33,7 +37,7 @@
 //
 // Arithmetic: FP32 residuals/weights/Jacobians (this translation unit is built with FMA contraction,
 // so per-point values differ from the CPU oracle in the last bits; parity is by tolerance),
-// Kahan-compensated sums, FP64 only in the LM step.
+// compensated merges, float LM solves and schedule, FP64 for the pose and the energy comparison.
 #include <cooperative_groups.h>
 
 #include "lsdg_internal.cuh"
@@ -96,7 +100,7 @@ struct LMState {
 };
 
 // ------------------------------------------------------------------------------------------
-// FP64 SE(3) helpers (thread 0 of rank 0 only)
+// Pose helpers (warp 0 of rank 0 only)
 // ------------------------------------------------------------------------------------------
 // [M | t]^-1 for M = R (SE3) or M = sR (Sim3: M^-1 = M^T / s^2; s^2 = 1 for a rotation).
 __device__ __noinline__ void se3_inv_d(const double* A, double* B, bool sim3) {
