@@ -52,6 +52,7 @@ struct BatchSlot {
   lsdg_track_stats* d_stats = nullptr;
   int* d_work = nullptr;
   double* d_mid = nullptr;            // coarse-phase poses of a split run
+  int* d_order = nullptr;             // processing order of the pairs (by reference points, set on the device)
   uint8_t* d_u8 = nullptr;            // 8-bit staging of the level-0 images (SE3 batches)
   int* d_mode = nullptr;              // 1: this step's level-0 images are the bytes in d_u8
   int* h_mode = nullptr;              // pinned {0, 1}: the sources of the mode word
@@ -77,7 +78,6 @@ struct lsdg_batch {
   std::vector<lsdg_intrinsics> intr;
   BatchSlot slot[2];
   int last = 0;                 // slot of the last run (timing / work)
-  int* d_order = nullptr;
   int test_withhold = -1;  // lsdg_batch_test_withhold: keyframe whose band 0 publishes no counts
   int* h_counts = nullptr;
   cudaStream_t copy = nullptr;  // upload stream of the pipelined form
@@ -99,6 +99,7 @@ static void slot_free(BatchSlot& s) {
   if (s.d_stats) cudaFree(s.d_stats);
   if (s.d_work) cudaFree(s.d_work);
   if (s.d_mid) cudaFree(s.d_mid);
+  if (s.d_order) cudaFree(s.d_order);
   if (s.d_u8) cudaFree(s.d_u8);
   if (s.d_mode) cudaFree(s.d_mode);
   if (s.h_mode) cudaFreeHost(s.h_mode);
@@ -115,7 +116,6 @@ static void slot_free(BatchSlot& s) {
 
 static void batch_free(lsdg_batch* b) {
   for (auto& s : b->slot) slot_free(s);
-  if (b->d_order) cudaFree(b->d_order);
   if (b->h_counts) cudaFreeHost(b->h_counts);
   if (b->copy) cudaStreamDestroy(b->copy);
   delete b;
@@ -145,6 +145,7 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   if (e == cudaSuccess) e = cudaMalloc(&s.d_out, sizeof(double) * b->pose_len * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_stats, sizeof(lsdg_track_stats) * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_work, sizeof(int) * 4);
+  if (e == cudaSuccess) e = cudaMalloc(&s.d_order, sizeof(int) * n);
   if (e == cudaSuccess) e = cudaMalloc(&s.d_scan, frame_build_ws_bytes(2 * b->n, s.fs.levels, s.fs.max_h));
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_err, sizeof(unsigned));
   if (e == cudaSuccess) *s.h_err = 0;
@@ -174,7 +175,7 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
 static TrackArgs slot_track_args(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   TrackArgs a = make_track_args(ctx->params);
   a.pairs = s.d_pairs;
-  a.order = b->d_order;
+  a.order = s.d_order;
   a.n_pairs = b->n;
   a.work_counter = s.d_work;
   a.init = s.d_init;
@@ -185,11 +186,29 @@ static TrackArgs slot_track_args(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   return a;
 }
 
+// Processing order of a batch's pairs: by the reference keyframe's level-0 points, largest first
+// (ties by pair index), so that the persistent tracker's queue hands out the longest pairs first
+// (longest-processing-time-first: with more pairs than resident clusters the last round is short).
+// One CTA; rank of pair i = the pairs ordered before it.
+__global__ void order_by_points_kernel(const PairDev* __restrict__ pairs, int n, int* __restrict__ order) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int ki = pairs[i].ref->pcount[0];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const int kj = pairs[j].ref->pcount[0];
+      rank += (kj > ki || (kj == ki && j < i)) ? 1 : 0;
+    }
+    order[rank] = i;
+  }
+}
+
 static lsdg_status enqueue_build(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, int* launches) {
   // one launch over all 2n frames: pyramids (also the depth pyramids of the second keyframes in
   // Sim3 mode), reference points only for the first n
   int k = launch_frame_build(s.fs.d_frames, 2 * b->n, b->n, s.fs.levels, s.fs.max_h, s.d_scan, ctx->stream,
                              b->test_withhold, s.d_u8, s.fs.plane0, s.d_mode);
+  order_by_points_kernel<<<1, 256, 0, ctx->stream>>>(s.d_pairs, b->n, s.d_order);
+  ++k;
   CK(ctx, cudaGetLastError());
   *launches = k;
   return LSDG_OK;
@@ -317,14 +336,7 @@ static lsdg_status batch_create(lsdg_ctx* ctx, int n, const int* widths, const i
     batch_free(b);
     return st;
   }
-  std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int c) { return (long)widths[a] * heights[a] > (long)widths[c] * heights[c]; });
-  cudaError_t e = cudaMalloc(&b->d_order, sizeof(int) * n);
-  if (e == cudaSuccess) e = cudaMallocHost(&b->h_counts, sizeof(int) * kMaxLevels * n);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaError_t e = cudaMallocHost(&b->h_counts, sizeof(int) * kMaxLevels * n);
   if (e != cudaSuccess) {
     st = ctx_cuda(ctx, e, "batch allocation");
     batch_free(b);
