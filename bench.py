@@ -243,6 +243,12 @@ def run_ours(args, rank, world, local_rank):
     batch.load(ri, rd, rv, ni, init)
     batch.run()  # autotune + graph capture
     out, stats = batch.read()
+    # both input slots of the pipelined form (their arenas, staging, captured graphs) set up and used
+    # with both kinds of step before the soak, so no first use falls into a timed region
+    for submit in (lambda: batch.submit_u8(ri8, rd, rv, ni8, init), lambda: batch.submit(ri, rd, rv, ni, init)):
+        for _ in range(4):
+            submit()
+            batch.collect()
 
     def barrier():
         torch.cuda.synchronize()
@@ -284,10 +290,11 @@ def run_ours(args, rank, world, local_rank):
     # pipelined (lsdg_batch_submit_se3_u8 / lsdg_batch_collect): step k+1's upload overlaps step k;
     # the images cross the bus as bytes (the camera's format), the depth maps as floats
     def pipelined(submit):
-        for _ in range(2):
+        for _ in range(4):
             submit()
-        for _ in range(2):
-            batch.collect()
+            if _ >= 1:
+                batch.collect()
+        batch.collect()
         barrier()
         t0 = time.time()
         for k in range(args.steps):
@@ -298,8 +305,17 @@ def run_ours(args, rank, world, local_rank):
         barrier()
         return max_over_ranks(time.time() - t0), out, st
 
-    e2e_s, out_e, stats_e = pipelined(lambda: batch.submit_u8(ri8, rd, rv, ni8, init))
-    e2e_f32_s, out_f, _ = pipelined(lambda: batch.submit(ri, rd, rv, ni, init))
+    # three timed runs of K steps each, the median reported (all three in the line): one stall of the
+    # shared host in a ~30 ms loop would otherwise stand for the path's rate
+    E2E_REPEATS = 3
+
+    def pipelined_median(submit):
+        runs = [pipelined(submit) for _ in range(E2E_REPEATS)]
+        times = sorted(r[0] for r in runs)
+        return times[len(times) // 2], runs[-1][1], runs[-1][2], [r[0] for r in runs]
+
+    e2e_s, out_e, stats_e, e2e_runs = pipelined_median(lambda: batch.submit_u8(ri8, rd, rv, ni8, init))
+    e2e_f32_s, out_f, _, e2e_f32_runs = pipelined_median(lambda: batch.submit(ri, rd, rv, ni, init))
     assert np.array_equal(out_e, out_f), "8-bit and float image uploads disagree"
     # synchronous (lsdg_batch_track_se3: upload, track, read back, one step at a time)
     barrier()
@@ -399,9 +415,12 @@ def run_ours(args, rank, world, local_rank):
                    "tile_shape": batch.shape()},
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "repeats": {"steps_each": args.steps, "value_per_run": [N_PAIRS * world * args.steps / t for t in e2e_runs],
+                            "reported": "median of the runs"},
                 "api": "lsdg_batch_submit_se3_u8 + lsdg_batch_collect (pinned host buffers: 8-bit images, float "
                        "depth maps; the next step's upload overlaps the current step's tracking)",
                 "float_images": {"value": N_PAIRS * world * args.steps / e2e_f32_s, "h2d_bytes_per_step": int(h2d_f32),
+                                 "value_per_run": [N_PAIRS * world * args.steps / t for t in e2e_f32_runs],
                                  "api": "lsdg_batch_submit_se3 + lsdg_batch_collect (the same images as floats)"},
                 "synchronous": {"value": N_PAIRS * world * args.steps / e2e_sync_s,
                                 "api": "lsdg_batch_track_se3 (upload, track, read back per step)"}},
