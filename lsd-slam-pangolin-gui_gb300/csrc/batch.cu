@@ -2,11 +2,13 @@
 //
 // A batch slot owns one arena with 2n frames: frames 0..n-1 are the keyframes (with depth), n..2n-1
 // the frames to track.  The level-0 inputs of all pairs sit back to back per kind, so a batch upload
-// is four host->device copies.  A run is one CUDA graph: image pyramids of all 2n frames, depth
-// pyramids + point compaction of the keyframes, then ONE persistent cluster launch that runs every
-// pair's full coarse-to-fine LM loop on the device (pairs taken largest first from an atomic queue).
-// The graph is captured after the autotuner has picked the (threads, cluster) shape for the batch's
-// size mix, and it is recaptured when the parameters change.
+// is four host->device copies (two byte copies for 8-bit images).  A run is one CUDA graph: one
+// launch builds the image pyramids of all 2n frames, the depth pyramids and the compacted points of
+// the keyframes (frame.cu), a one-CTA kernel ranks the pairs by their keyframes' points, then the
+// persistent cluster tracker runs every pair's full coarse-to-fine LM loop on the device (pairs
+// taken largest first from an atomic queue; coarse and fine levels in two launches when the tuner
+// splits them).  The graph is captured after the autotuner has picked the launch plan for the
+// batch's size mix, and it is recaptured when the parameters change.
 //
 // Two slots make the pipelined form (lsdg_batch_submit_* / lsdg_batch_collect): step k+1's inputs
 // are uploaded into the other slot on a copy stream while step k's graph runs, and each step's
@@ -17,7 +19,6 @@
 #include <algorithm>
 #include <cstring>
 #include <new>
-#include <numeric>
 #include <string>
 #include <vector>
 

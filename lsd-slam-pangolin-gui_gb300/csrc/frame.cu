@@ -8,10 +8,12 @@
 // GB300 layout of the work: a CTA owns one BAND of 2^(levels-1) level-0 rows of one frame.  Every
 // coarser level of that band is built from rows of the same band (2x2 means nest), so one launch
 // builds all levels of all frames, with __syncthreads between levels instead of a launch per level.
-// The point compaction is band-ordered too: pass 1 counts the valid pixels of every (band, level),
-// a scan turns the counts into offsets, pass 2 writes the points -- bands in order, pixels in
-// row-major order inside a band, so the point arrays are in global row-major order.  Three launches
-// build a keyframe, whatever the number of levels or frames; all are memory-bound streaming.
+// The point compaction is band-ordered too: the valid pixels of every (band, level) are counted,
+// the counts of the bands before give the band's offsets, and the band writes its points -- bands
+// in order, pixels in row-major order inside a band, so the point arrays are in global row-major
+// order.  Single frames do it in three launches (counts, scan, scatter); a batch step in one
+// (frame_build_kernel: the offsets come from a bounded look-back over the bands before, inside the
+// launch), whatever the number of levels or frames.
 //
 // Operation order matches the CPU oracle exactly (this translation unit is built with
 // -fmad=false), so pyramids and points are bit-identical to it.
