@@ -7,9 +7,9 @@
 //   idepth[l], ivar[l]  float [h_l * w_l]  keyframe depth pyramid (idepth <= 0: none)
 //   pxyzi[l]   float4 [n_l]         tracking reference points, SoA: {X, Y, Z, I_keyframe}
 //   pvar[l]    float  [n_l]         inverse-depth variance of each point
-//   psig[l]    float  [n_l]         tracker scratch: residual variance of each point, fixed by the
-//                                   first pass of a level (0 = the point sits out the level)
-//   psigd[l]   float  [n_l]         Sim3 tracker scratch: variance of the inverse-depth residual
+//   psig[l]    float  [n_l]         tracker scratch: 1 / residual variance of each point, fixed by
+//                                   the first pass of a level (0 = the point sits out the level)
+//   psigd[l]   float  [n_l]         Sim3 tracker scratch: 1 / variance of the inverse-depth residual
 //   ppix[l]    int    [n_l]         row-major pixel index of each point (single frames only; the
 //                                   photometric energy maps its points back to pixels with it)
 //   pcount[l]  int                  n_l, written on the device by the compaction
@@ -36,7 +36,7 @@ struct FrameDev {
   float4* pxyzi[kMaxLevels];
   float* pvar[kMaxLevels];
   float* psig[kMaxLevels];
-  float* psigd[kMaxLevels];      // Sim3 tracker scratch: variance of the inverse-depth residual
+  float* psigd[kMaxLevels];      // Sim3 tracker scratch: 1 / variance of the inverse-depth residual
   int* ppix[kMaxLevels];         // pixel index of each point, or nullptr (batch frames)
   int* pcount;                   // [kMaxLevels]
   int* blk_count[kMaxLevels];    // compaction scratch: valid pixels per band, then offsets

@@ -911,17 +911,22 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
       J[4] = Zp * a0 - Xp * a2;
       J[5] = Xp * a1 - Yp * a0;
       if (SIM3) J[D - 1] = (a0 * Xp + a1 * Yp) + a2 * Zp;
+      // as in the SE3 loop: psig (and psigd) hold 1/sigma^2 frozen at the level's first pass
+      float isig = s2;
       if (first) {
         const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
-        s2 = pvr + (drd * drd) * __ldg(&pvar[k]);
-        psig[k] = s2;
+        isig = 1.0f / (pvr + (drd * drd) * __ldg(&pvar[k]));
+        psig[k] = isig;
       }
-      const float e2 = (r * r) / s2;
-      const float ae = sqrtf(e2);
-      float wh, rho;
-      if (ae <= delta) { wh = 1.f; rho = e2; ++good; }
-      else { wh = delta / ae; rho = delta * (2.f * ae - delta); ++bad; }
-      const float wgt = wh / s2;
+      const float e2 = (r * r) * isig;
+      float wgt, rho;
+      if (e2 <= delta * delta) { wgt = isig; rho = e2; ++good; }
+      else {
+        const float ir = rsqrtf(e2);
+        wgt = (delta * ir) * isig;
+        rho = delta * (2.f * (e2 * ir) - delta);
+        ++bad;
+      }
       float wJ[D];
 #pragma unroll
       for (int i = 0; i < D; ++i) wJ[i] = wgt * J[i];
@@ -961,13 +966,16 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
             const float bdd = -(((b0 * Rpx + b1 * Rpy) + b2 * Rpz) * Z);
             float sd = Vv + (bdd * bdd) * __ldg(&pvar[k]);
             if (sd < dfloor) sd = dfloor;
-            psigd[k] = sd;
-            s2d = sd;
+            s2d = 1.0f / sd;
+            psigd[k] = s2d;
           }
-          const float e2d = (rd * rd) / s2d;
-          const float aed = sqrtf(e2d);
-          if (aed <= delta) { wgd = wdep / s2d; rhod = e2d; }
-          else { wgd = (wdep * (delta / aed)) / s2d; rhod = delta * (2.f * aed - delta); }
+          const float e2d = (rd * rd) * s2d;
+          if (e2d <= delta * delta) { wgd = wdep * s2d; rhod = e2d; }
+          else {
+            const float ir = rsqrtf(e2d);
+            wgd = (wdep * (delta * ir)) * s2d;
+            rhod = delta * (2.f * (e2d * ir) - delta);
+          }
         } else if (first) {
           psigd[k] = 0.f;
         }
@@ -975,7 +983,7 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
 #pragma unroll
         for (int i = 0; i < D; ++i)
 #pragma unroll
-          for (int j = i; j < D; ++j) { kadd(hs[q2], hc[q2], wJ[i] * J[j] + (wgd * Jd[i]) * Jd[j]); ++q2; }
+          for (int j = i; j < D; ++j) { hs[q2] = fmaf(wgd * Jd[i], Jd[j], fmaf(wJ[i], J[j], hs[q2])); ++q2; }
 #pragma unroll
         for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJ[i] * r + (wgd * Jd[i]) * rd);
         kadd(es, ec, rho + wdep * rhod);
