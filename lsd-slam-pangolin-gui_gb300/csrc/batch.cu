@@ -12,8 +12,8 @@
 //
 // Two slots make the pipelined form (lsdg_batch_submit_* / lsdg_batch_collect): step k+1's inputs
 // are uploaded into the other slot on a copy stream while step k's graph runs, and each step's
-// poses come back on the context stream behind its graph, so the host<->device copies overlap the
-// tracking.  The synchronous calls (load / run / read / track) use slot 0.
+// poses come back on a read-back stream behind its graph (off the graphs' stream), so the
+// host<->device copies overlap the tracking.  The synchronous calls (load / run / read / track) use slot 0.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -65,7 +65,8 @@ struct BatchSlot {
   int graph_epoch = -1;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // run start, build done, track done (timing)
   cudaEvent_t copied = nullptr;       // inputs are in the arena (copy stream)
-  cudaEvent_t done = nullptr;         // graph + result read-back finished (context stream)
+  cudaEvent_t done = nullptr;         // graph + result read-back finished (read-back stream)
+  cudaEvent_t graph_done = nullptr;   // the step's graph finished (context stream)
   bool ran = false;
 };
 
@@ -81,7 +82,8 @@ struct lsdg_batch {
   int last = 0;                 // slot of the last run (timing / work)
   int test_withhold = -1;  // lsdg_batch_test_withhold: keyframe whose band 0 publishes no counts
   int* h_counts = nullptr;
-  cudaStream_t copy = nullptr;  // upload stream of the pipelined form
+  cudaStream_t copy = nullptr;      // upload stream of the pipelined form
+  cudaStream_t readback = nullptr;  // result stream of the pipelined form (off the graphs' stream)
   int inflight[2] = {-1, -1};   // slots of the submitted, not yet collected steps (oldest first)
   int n_inflight = 0;
   int next = 0;                 // slot of the next submit
@@ -112,6 +114,7 @@ static void slot_free(BatchSlot& s) {
     if (e) cudaEventDestroy(e);
   if (s.copied) cudaEventDestroy(s.copied);
   if (s.done) cudaEventDestroy(s.done);
+  if (s.graph_done) cudaEventDestroy(s.graph_done);
   s = BatchSlot{};
 }
 
@@ -119,6 +122,7 @@ static void batch_free(lsdg_batch* b) {
   for (auto& s : b->slot) slot_free(s);
   if (b->h_counts) cudaFreeHost(b->h_counts);
   if (b->copy) cudaStreamDestroy(b->copy);
+  if (b->readback) cudaStreamDestroy(b->readback);
   delete b;
 }
 
@@ -165,6 +169,7 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
     if (e == cudaSuccess) e = cudaEventCreate(&ev);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.copied, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.graph_done, cudaEventDisableTiming);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(s.d_pairs, pairs.data(), sizeof(PairDev) * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -372,6 +377,7 @@ static lsdg_status batch_submit(lsdg_ctx* ctx, lsdg_batch* b, const float* ri, c
     if (st != LSDG_OK) return st;
   }
   if (!b->copy) CK(ctx, cudaStreamCreateWithFlags(&b->copy, cudaStreamNonBlocking));
+  if (!b->readback) CK(ctx, cudaStreamCreateWithFlags(&b->readback, cudaStreamNonBlocking));
   if (!s.exec || s.graph_epoch != ctx->params_epoch) {
     // first use of this slot (or new parameters): upload on the context stream, then tune/capture
     lsdg_status st = slot_upload(ctx, b, s, ctx->stream, ri, rd, rv, ni, nd, nv, init, ri8, ni8);
@@ -387,11 +393,15 @@ static lsdg_status batch_submit(lsdg_ctx* ctx, lsdg_batch* b, const float* ri, c
     st = slot_run(ctx, b, si);
     if (st != LSDG_OK) return st;
   }
-  CK(ctx, cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(ctx, cudaMemcpyAsync(s.h_stats, s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, ctx->stream));
+  // the results come back on the read-back stream, so the next step's graph does not queue behind
+  // these copies; the slot's next upload waits for them (event done)
+  CK(ctx, cudaEventRecord(s.graph_done, ctx->stream));
+  CK(ctx, cudaStreamWaitEvent(b->readback, s.graph_done, 0));
+  CK(ctx, cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * b->pose_len * b->n, cudaMemcpyDeviceToHost, b->readback));
+  CK(ctx, cudaMemcpyAsync(s.h_stats, s.d_stats, sizeof(lsdg_track_stats) * b->n, cudaMemcpyDeviceToHost, b->readback));
   CK(ctx, cudaMemcpyAsync(s.h_err, reinterpret_cast<unsigned*>(s.d_scan) + 1, sizeof(unsigned), cudaMemcpyDeviceToHost,
-                          ctx->stream));
-  CK(ctx, cudaEventRecord(s.done, ctx->stream));
+                          b->readback));
+  CK(ctx, cudaEventRecord(s.done, b->readback));
   b->inflight[b->n_inflight++] = si;
   b->next = si ^ 1;
   return LSDG_OK;
@@ -413,6 +423,7 @@ lsdg_status lsdg_batch_destroy(lsdg_ctx* ctx, lsdg_batch* b) {
   if (!ctx || !b) return LSDG_INVALID_ARG;
   cudaStreamSynchronize(ctx->stream);
   if (b->copy) cudaStreamSynchronize(b->copy);
+  if (b->readback) cudaStreamSynchronize(b->readback);
   batch_free(b);
   return LSDG_OK;
 }
