@@ -2,8 +2,8 @@
 
 The reference ships no golden vectors for this path (its only test is ASSERT_TRUE(true),
 test/unit/test_test.cpp:4-7) and its lsd-slam code cannot be built here, so these fixtures freeze
-the oracle's own outputs on small seeded cases: they pin the oracle across machines (x86 container,
-Arm GPU machine) and over time, and the GPU tests compare the library against them.
+the oracle's own outputs on small seeded cases: they pin the oracle across machines (x86 and Arm
+hosts) and over time, and the GPU tests compare the library against them.
 
 Inputs are stored in a platform-independent form (images rounded to uint8, depths as float32), so
 the fixtures do not depend on the synthetic renderer's floating-point details.  Outputs that are
