@@ -302,13 +302,16 @@ LSDG_API lsdg_status lsdg_batch_load(lsdg_ctx* ctx, lsdg_batch* batch, const flo
  * the persistent LM tracker over all pairs and levels.  Asynchronous; replayed from a CUDA graph
  * after the first call. */
 LSDG_API lsdg_status lsdg_batch_run(lsdg_ctx* ctx, lsdg_batch* batch);
-/* Device -> host results (synchronises the context stream). */
+/* Device -> host results (synchronises the context stream).  LSDG_TIMEOUT: the step's keyframe
+ * build ran out of one of its bounded waits (the poses of that step are not to be used; the
+ * context stays usable). */
 LSDG_API lsdg_status lsdg_batch_read(lsdg_ctx* ctx, lsdg_batch* batch, double* frame_to_ref_out,
                             lsdg_track_stats* stats);
 /* Pipelined form: lsdg_batch_submit_* enqueues one step (the upload of its inputs on the batch's
  * copy stream into whichever of the batch's two input slots the previous step is not using, the
- * step's graph behind the upload, the read-back of its poses and stats behind the graph) and
- * returns; lsdg_batch_collect waits for the oldest submitted step and copies its results out.  At
+ * step's graph behind the upload, the read-back of its poses and stats behind the graph on a
+ * read-back stream) and returns; lsdg_batch_collect waits for the oldest submitted step and copies
+ * its results out (LSDG_TIMEOUT as for lsdg_batch_read).  At
  * most two steps are in flight (a third submit fails with LSDG_INVALID_ARG); results come back in
  * submission order.  For the copies to overlap the tracking, the host arrays must be pinned
  * (page-locked) and stay untouched until the step is collected.  The synchronous calls
