@@ -37,21 +37,19 @@ import numpy as np  # noqa: E402
 
 METRIC = "tracked frame pairs/s @640x480"
 UNIT = "pairs/s"
-N_PAIRS = 64
+import synth  # noqa: E402  (the seeded synthetic workloads)
+
+N_PAIRS = synth.HEADLINE_PAIRS
 W, H = 640, 480
-MIXED = [(320, 240)] * 20 + [(640, 480)] * 32 + [(1280, 960)] * 12
-N_SIM3 = 10        # Sim3 constraint search: a new keyframe against 10 candidate keyframes
+MIXED = synth.MIXED_SIZES
+N_SIM3 = synth.SIM3_CANDIDATES  # Sim3 constraint search: a new keyframe against 10 candidate keyframes
 REFINE_STEPS = 50  # inverse-depth refinement steps over 8 observing frames
 
 
 def _gen(seed, w, h):
     """A tracking pair whose two images are 8-bit (a camera's format): rounded and clipped to
     0..255, held as floats for the float calls and as bytes for the 8-bit one."""
-    import synth
-    p = synth.tracking_pair(seed, w, h)
-    p.ref_image = np.clip(np.rint(p.ref_image), 0, 255).astype(np.float32)
-    p.new_image = np.clip(np.rint(p.new_image), 0, 255).astype(np.float32)
-    return p
+    return synth.camera_pair(seed, w, h)
 
 
 def _gen_depth(seed, w, h):
@@ -209,11 +207,11 @@ def run_ours(args, rank, world, local_rank):
     pairs = gen_pairs([(1000 * rank + i, W, H) for i in range(N_PAIRS)], workers)
     # the mixed batch is one fixed set of 64 pairs partitioned across the ranks (shard.partition)
     mixed_idx = shard.my_share([shard.pair_cost(w, h) for w, h in MIXED], rank, world)
-    mixed = gen_pairs([(5000 + i, MIXED[i][0], MIXED[i][1]) for i in mixed_idx], workers) if not args.quick else []
+    mixed = gen_pairs([(synth.MIXED_SEED0 + i, MIXED[i][0], MIXED[i][1]) for i in mixed_idx], workers) if not args.quick else []
     with mp.get_context("spawn").Pool(min(workers, 12)) as pool:
         dseq_r = pool.apply_async(_gen_depth, (7 + rank, W, H))
         rprob_r = pool.apply_async(_gen_refine, (rank, W, H))
-        sim3_r = pool.starmap_async(_gen_sim3, [(2000 + 1000 * rank + i, W, H) for i in range(N_SIM3)])
+        sim3_r = pool.starmap_async(_gen_sim3, [(synth.SIM3_SEED0 + 1000 * rank + i, W, H) for i in range(N_SIM3)])
         dseq, rprob, sim3_pairs = dseq_r.get(), rprob_r.get(), sim3_r.get()
 
     torch.cuda.set_device(local_rank)
@@ -372,7 +370,7 @@ def run_ours(args, rank, world, local_rank):
     del frames
 
     # ---- mixed-size batch (20 x 320x240, 32 x 640x480, 12 x 1280x960) ----
-    mixed_res = None
+    mixed_res, mo = None, None
     if mixed:
         mb = lsdg.Batch(ctx, [p.w for p in mixed], [p.h for p in mixed], [p.intr for p in mixed])
         mb.load(*[np.ascontiguousarray(x) for x in lsdg.pack_pairs(mixed)], np.stack([np.eye(3, 4)] * len(mixed)))
@@ -397,10 +395,14 @@ def run_ours(args, rank, world, local_rank):
                      "lost": int(mlost.sum()), "scaling": "strong (one 64-pair set split across ranks)"}
         mb.close()
 
-    depth_res = bench_depth(ctx, stream, dseq, args)
+    depth_res, depth_state = bench_depth(ctx, stream, dseq, args)
     energy_res = bench_energy(ctx, stream, pairs[0], rprob, args)
     input_res = bench_input(ctx, stream, pairs[0], args)
-    sim3_res = bench_sim3(ctx, stream, sim3_pairs, args)
+    sim3_res, sim3_out = bench_sim3(ctx, stream, sim3_pairs, args)
+    # accuracy of every result against the FP64 oracle (outside every timed region)
+    fp64 = accuracy_vs_fp64(pairs, out_e, mixed, mo, sim3_pairs, sim3_out, dseq, depth_state)
+    for k in ("max_rot_err_rad", "max_trans_err_m"):
+        fp64["headline"][k] = max_over_ranks(fp64["headline"][k])
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -440,6 +442,7 @@ def run_ours(args, rank, world, local_rank):
         "energy": energy_res,
         "input_step": input_res,
         "sim3_constraint_batch": sim3_res,
+        "accuracy_vs_fp64": fp64,
         "accuracy": {"max_gt_rot_err_rad": max_over_ranks(max(e[0] for e in errs)),
                      "max_gt_trans_err_m": max_over_ranks(max(e[1] for e in errs)),
                      "lost": int(shard.sum_over_ranks(lost, dist, device="cuda")), "pairs": N_PAIRS * world},
@@ -535,7 +538,7 @@ def bench_depth(ctx, stream, seq, args):
             "create_keyframe_ms_e2e": statistics.median(prop),
             "well_observed_pixels": int(good.sum()), "median_rel_idepth_err_vs_truth": float(np.median(rel)),
             "cloud_ms": statistics.median(cl), "cloud_vertices": int(n_vertices),
-            "cloud_api": "lsdg_cloud_from_depthmap (Keyframe::computeVbo into a device buffer; call incl. count read-back)"}
+            "cloud_api": "lsdg_cloud_from_depthmap (Keyframe::computeVbo into a device buffer; call incl. count read-back)"}, st
 
 
 def bench_energy(ctx, stream, pair, rp, args):
@@ -653,6 +656,52 @@ def bench_sim3(ctx, stream, sps, args):
            "ms_per_batch": ms, "trackings_per_s": len(sps) / (ms / 1e3), "shape": b.shape(),
            "max_gt_scale_err": float(max(scale_err)), "lost": sum(1 for s in stats if s.status != 0)}
     b.close()
+    return res, out
+
+
+def accuracy_vs_fp64(pairs, out, mixed, mixed_out, sim3_pairs, sim3_out, dseq, depth_state):
+    """Every tracked pose against the FP64 oracle run on the same inputs (rotation angle, translation
+    distance; Sim3 also |scale ratio - 1|), and the keyframe update's state against the FP64 depth
+    pipeline: relative inverse-depth and variance error where both hold a hypothesis, and flag
+    agreement.  Bars: 1e-4 rad / 1e-4 m / 1e-4 scale; 1e-3 relative inverse depth; 99.9 % flags."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lsdo
+
+    cores = os.cpu_count() or 1
+
+    def poses(ps, got):
+        ref, _ = lsdo.track_batch(ps, threads=cores, double=True)
+        e = np.array([synth.pose_error(got[i], ref[i]) for i in range(len(ps))])
+        return {"pairs": len(ps), "max_rot_err_rad": float(e[:, 0].max()), "max_trans_err_m": float(e[:, 1].max()),
+                "median_rot_err_rad": float(np.median(e[:, 0])), "median_trans_err_m": float(np.median(e[:, 1]))}
+
+    res = {"oracle": "the project's CPU restatement instantiated in double (FP64 pyramids, sampling, sums, solves)",
+           "headline": poses(pairs, out)}
+    if mixed:
+        res["mixed_batch_this_rank"] = poses(mixed, mixed_out)
+    s3 = []
+    for i, q in enumerate(sim3_pairs):
+        _, o, _ = lsdo.track_sim3(q, double=True)
+        s3.append(lsdo.sim3_error(sim3_out[i], o))
+    s3 = np.array(s3)
+    res["sim3_constraint_batch"] = {"pairs": len(sim3_pairs), "max_rot_err_rad": float(s3[:, 0].max()),
+                                    "max_trans_err_m": float(s3[:, 1].max()), "max_scale_err": float(s3[:, 2].max())}
+    ref, _ = lsdo.depth_pipeline(dseq, propagate=False, double=True, threads=cores)
+    g = depth_state
+    # pixels the update changed (in either run): every pixel starts with a hypothesis, the
+    # untextured ones keep it untouched
+    moved = (ref["var"] != dseq.init_var) | (g["var"] != dseq.init_var)
+    both = (g["validity"] > 0) & (ref["validity"] > 0) & moved
+    rel_d = np.abs(g["idepth"][both] / ref["idepth"][both] - 1.0)
+    rel_v = np.abs(g["var"][both] / ref["var"][both] - 1.0)
+    res["keyframe_update"] = {
+        "observed_pixels_with_depth_in_both": int(both.sum()),
+        "median_rel_idepth_err": float(np.median(rel_d)), "max_rel_idepth_err": float(rel_d.max()),
+        "frac_rel_idepth_err_le_1e-3": float(np.mean(rel_d <= 1e-3)),
+        "median_rel_var_err": float(np.median(rel_v)), "max_rel_var_err": float(rel_v.max()),
+        "validity_agreement": float(np.mean(g["validity"] == ref["validity"])),
+        "blacklist_agreement": float(np.mean(g["blacklist"] == ref["blacklist"])),
+        "has_depth_agreement": float(np.mean((g["validity"] > 0) == (ref["validity"] > 0)))}
     return res
 
 
@@ -663,7 +712,7 @@ def cpu_refine_baseline(rp):
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
     lsdo.energy_refine(rp.key_image, rp.key_idepth, rp.key_idepth_var, rp.frame_images, rp.ref_to_frame, rp.intr,
-                       rp.w, rp.h, steps=REFINE_STEPS, threads=cores)
+                       rp.w, rp.h, steps=REFINE_STEPS, threads=cores, fast=True)
     return (time.perf_counter() - t0) * 1e3, cores
 
 
@@ -675,36 +724,35 @@ def cpu_depth_baseline(seq):
     ts = []
     for _ in range(3):
         t0 = time.perf_counter()
-        lsdo.depth_pipeline(seq, propagate=False, threads=cores)
+        lsdo.depth_pipeline(seq, propagate=False, threads=cores, fast=True)
         ts.append((time.perf_counter() - t0) * 1e3)
     return statistics.median(ts), cores
 
 
 def cpu_baseline(pairs, args, min_seconds=10.0):
-    """The float CPU restatement of the same path on the host cores (pairs spread over threads)."""
+    """The float CPU restatement of the same path on the host cores (pairs spread over threads),
+    the speed build (-O3, FMA contraction, the host core's instruction set)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import lsdo
-    import synth
 
     cores = os.cpu_count() or 1
     n = 0
     t0 = time.time()
     reps = 0
     while True:
-        out, stats = lsdo.track_batch(pairs, threads=cores)
+        out, stats = lsdo.track_batch(pairs, threads=cores, fast=True)
         n += len(pairs)
         reps += 1
         if time.time() - t0 >= min_seconds or args.quick:
             break
     dt = time.time() - t0
-    # FP64 restatement on a sample, for the accuracy report
-    errs = []
-    for i in range(4):
-        _, Td, _ = lsdo.track_se3(pairs[i], double=True)
-        errs.append(synth.pose_error(out[i], Td))
+    ref, _ = lsdo.track_batch(pairs, threads=cores, double=True)
+    errs = [synth.pose_error(out[i], ref[i]) for i in range(len(pairs))]
     return {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{reps} x the {len(pairs)}-pair 640x480 batch (float CPU restatement, pairs over {cores} threads)",
-            "float_vs_fp64_max_rot_err_rad": max(e[0] for e in errs)}
+            "build": "g++ " + lsdo.fast_build_flags(),
+            "sample": f"{reps} x the {len(pairs)}-pair 640x480 batch (float CPU restatement, speed build, pairs "
+                      f"over {cores} threads)",
+            "vs_fp64_max_rot_err_rad": max(e[0] for e in errs), "vs_fp64_max_trans_err_m": max(e[1] for e in errs)}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -721,17 +769,17 @@ def run_reference(args, rank, world):
     cores = workers
     # bound the run: a step is the full 64-pair batch unless K steps would exceed ~150 s
     t0 = time.time()
-    lsdo.track_batch(pairs[:cores], threads=cores)
+    lsdo.track_batch(pairs[:cores], threads=cores, fast=True)
     est_pair = (time.time() - t0) / max(1, min(cores, len(pairs))) * cores  # seconds per pair per thread
     per_step = len(pairs)
     while per_step > cores and (args.steps + args.warmup) * per_step * est_pair / cores > 150:
         per_step //= 2
     sample = pairs[:per_step]
     for _ in range(args.warmup):
-        lsdo.track_batch(sample, threads=cores)
+        lsdo.track_batch(sample, threads=cores, fast=True)
     t0 = time.time()
     for _ in range(args.steps):
-        lsdo.track_batch(sample, threads=cores)
+        lsdo.track_batch(sample, threads=cores, fast=True)
     dt = time.time() - t0
     value = per_step * args.steps / dt
     res = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
@@ -739,9 +787,10 @@ def run_reference(args, rank, world):
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": f"SE3 trackFrame on CPU, {per_step} pairs 640x480 per step, 5 levels"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "build": "g++ " + lsdo.fast_build_flags(),
                             "sample": f"{per_step} pairs per step of the 64-pair 640x480 workload; the reference's own "
                                       "lsd-slam CPU code is an unvendored import (fips.yml:2-4), so this is the "
-                                      "project's float C++ restatement"},
+                                      "project's float C++ restatement, speed build, pairs over all host threads"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(res), flush=True)
 

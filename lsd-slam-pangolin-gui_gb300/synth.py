@@ -305,6 +305,36 @@ def tracking_pair(seed: int = 0, w: int = BASE_W, h: int = BASE_H, noise_sigma: 
     return TrackingPair(w, h, intr, img0, idepth.astype(np.float32), var.astype(np.float32), img1, T, depth0)
 
 
+# The benchmark's workloads, defined once for bench.py and the accuracy tests:
+# the headline batch is 64 pairs at 640x480 with seeds 0..63 (rank r of a sharded run: 1000 r + i),
+# the mixed batch 20 x 320x240, 32 x 640x480, 12 x 1280x960 with seeds 5000 + i, the Sim3 constraint
+# batch 10 pairs at 640x480 with seeds 2000 + i.
+HEADLINE_PAIRS = 64
+MIXED_SIZES = [(320, 240)] * 20 + [(640, 480)] * 32 + [(1280, 960)] * 12
+MIXED_SEED0 = 5000
+SIM3_CANDIDATES = 10
+SIM3_SEED0 = 2000
+
+
+def camera_pair(seed: int, w: int = BASE_W, h: int = BASE_H) -> TrackingPair:
+    """A tracking pair whose two images are 8-bit values (a camera's format): rounded and clipped
+    to 0..255, held as float32."""
+    p = tracking_pair(seed, w, h)
+    p.ref_image = np.clip(np.rint(p.ref_image), 0, 255).astype(np.float32)
+    p.new_image = np.clip(np.rint(p.new_image), 0, 255).astype(np.float32)
+    return p
+
+
+def generate(fn, specs, workers: int):
+    """fn(*spec) for every spec in a pool of `workers` spawned processes (never forked: the caller
+    may already hold a CUDA context)."""
+    import multiprocessing as mp
+    if workers <= 1 or len(specs) <= 1:
+        return [fn(*s) for s in specs]
+    with mp.get_context("spawn").Pool(min(workers, len(specs))) as pool:
+        return pool.starmap(fn, specs)
+
+
 @dataclasses.dataclass
 class DepthSequence:
     w: int

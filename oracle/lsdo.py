@@ -15,6 +15,7 @@ if PKG not in sys.path:
 import lsdg_types as T  # noqa: E402
 
 _lib = None
+_fast_lib = None
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -22,71 +23,96 @@ _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
 def lib():
+    """The parity oracle (oracle/liblsdo.so: no FMA contraction, the kernels' operation order)."""
     global _lib
     if _lib is None:
         sys.path.insert(0, HERE)
         import build as _b  # oracle/build.py
-        path = _b.build()
-        L = C.CDLL(path)
-        L.lsdo_default_params.argtypes = [C.POINTER(T.Params)]
-        L.lsdo_pyramid_f.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, _f32p]
-        L.lsdo_pyramid_d.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, _f64p]
-        L.lsdo_keyframe_f.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.c_int,
-                                      _f32p, _f32p, _f32p, _f32p, C.c_int, _i32p]
-        L.lsdo_keyframe_f.restype = C.c_int
-        for nm in ("lsdo_se3_normal_equations_f", "lsdo_se3_normal_equations_d"):
-            f = getattr(L, nm)
-            f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                          C.POINTER(T.Params), C.c_int, _f64p, _f64p]
-            f.restype = C.c_int
-        for nm in ("lsdo_track_se3_f", "lsdo_track_se3_d"):
-            f = getattr(L, nm)
-            f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                          C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), C.c_int]
-            f.restype = C.c_int
-        L.lsdo_se3_fixed_energy_d.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                                              C.POINTER(T.Params), C.c_int, _f64p, _f64p, _f64p]
-        L.lsdo_se3_fixed_energy_d.restype = C.c_int
-        L.lsdo_track_trace.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                                       C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), _f64p, C.c_int,
-                                       C.POINTER(C.c_int)]
-        L.lsdo_track_trace.restype = C.c_int
-        L.lsdo_track_batch_f.argtypes = [C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), _f32p, _f32p, _f32p,
-                                         _f32p, _f64p, _f64p, C.POINTER(T.TrackStats), C.POINTER(T.Params), C.c_int]
-        L.lsdo_track_batch_f.restype = C.c_int
-        for nm in ("lsdo_depth_pipeline_f", "lsdo_depth_pipeline_d"):
-            f = getattr(L, nm)
-            f.argtypes = [C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(T.Params), _f32p, _f32p, _f32p, C.c_int,
-                          _f32p, _f64p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
-            f.restype = C.c_int
-        L.lsdo_sim3_normal_equations.argtypes = [C.c_int] + [_f32p] * 6 + [C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                                                                             C.POINTER(T.Params), C.c_int, _f64p, _f64p]
-        L.lsdo_sim3_normal_equations.restype = C.c_int
-        L.lsdo_track_sim3.argtypes = [C.c_int] + [_f32p] * 6 + [C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                                                                C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats)]
-        L.lsdo_track_sim3.restype = C.c_int
-        L.lsdo_sim3_exp.argtypes = [_f64p, _f64p]
-        _vp = C.c_void_p
-        L.lsdo_energy_points.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                                         C.POINTER(T.Params), C.c_int, _vp, _vp]
-        L.lsdo_energy_points.restype = C.c_int
-        L.lsdo_energy.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
-                                  C.POINTER(T.Params), C.c_int, _f64p, C.c_int] + [_vp] * 8 + \
-                                 [C.POINTER(C.c_int), C.POINTER(C.c_int)]
-        L.lsdo_energy.restype = C.c_int
-        L.lsdo_energy_refine.argtypes = [C.c_int, _f32p, _f32p, _f32p, C.c_int, _f32p, C.c_int, C.c_int,
-                                         C.POINTER(T.Intrinsics), C.POINTER(T.Params), C.c_int, _f64p, C.c_int, _vp,
-                                         _f32p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_long),
-                                         C.c_int]
-        L.lsdo_energy_refine.restype = C.c_int
-        L.lsdo_cloud_build.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
-                                       _vp, _vp, _vp]
-        L.lsdo_cloud_build.restype = C.c_int
-        L.lsdo_undistort_map.argtypes = [C.POINTER(T.Calibration), C.c_int, C.c_int, C.POINTER(T.Intrinsics), _f32p]
-        L.lsdo_undistort.argtypes = [_vp, C.c_int, C.c_int, _f32p, C.c_int, _vp]
-        L.lsdo_hardware_threads.restype = C.c_int
-        _lib = L
+        _lib = _bind(C.CDLL(_b.build()))
     return _lib
+
+
+def fast_lib():
+    """The same restatement built for speed (oracle/liblsdo_fast.so: -O3, FMA contraction, the
+    host CPU's instruction set named explicitly): the timed CPU baseline.  Its results are checked
+    against the FP64 oracle by tolerance, never used as the parity reference."""
+    global _fast_lib
+    if _fast_lib is None:
+        sys.path.insert(0, HERE)
+        import build as _b  # oracle/build.py
+        _fast_lib = _bind(C.CDLL(_b.build_fast()))
+    return _fast_lib
+
+
+def fast_build_flags() -> str:
+    sys.path.insert(0, HERE)
+    import build as _b  # oracle/build.py
+    fast_lib()
+    return " ".join(_b.fast_flags_used())
+
+
+def _bind(L):
+    """ctypes signatures of the oracle's entry points."""
+    L.lsdo_default_params.argtypes = [C.POINTER(T.Params)]
+    L.lsdo_pyramid_f.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, _f32p]
+    L.lsdo_pyramid_d.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, _f64p]
+    L.lsdo_keyframe_f.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.c_int,
+                                  _f32p, _f32p, _f32p, _f32p, C.c_int, _i32p]
+    L.lsdo_keyframe_f.restype = C.c_int
+    for nm in ("lsdo_se3_normal_equations_f", "lsdo_se3_normal_equations_d"):
+        f = getattr(L, nm)
+        f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                      C.POINTER(T.Params), C.c_int, _f64p, _f64p]
+        f.restype = C.c_int
+    for nm in ("lsdo_track_se3_f", "lsdo_track_se3_d"):
+        f = getattr(L, nm)
+        f.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                      C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), C.c_int]
+        f.restype = C.c_int
+    L.lsdo_se3_fixed_energy_d.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                          C.POINTER(T.Params), C.c_int, _f64p, _f64p, _f64p]
+    L.lsdo_se3_fixed_energy_d.restype = C.c_int
+    L.lsdo_track_trace.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                   C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats), _f64p, C.c_int,
+                                   C.POINTER(C.c_int)]
+    L.lsdo_track_trace.restype = C.c_int
+    for nm in ("lsdo_track_batch_f", "lsdo_track_batch_d"):
+        f = getattr(L, nm)
+        f.argtypes = [C.c_int, _i32p, _i32p, C.POINTER(T.Intrinsics), _f32p, _f32p, _f32p,
+                      _f32p, _f64p, _f64p, C.POINTER(T.TrackStats), C.POINTER(T.Params), C.c_int]
+        f.restype = C.c_int
+    for nm in ("lsdo_depth_pipeline_f", "lsdo_depth_pipeline_d"):
+        f = getattr(L, nm)
+        f.argtypes = [C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(T.Params), _f32p, _f32p, _f32p, C.c_int,
+                      _f32p, _f64p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        f.restype = C.c_int
+    L.lsdo_sim3_normal_equations.argtypes = [C.c_int] + [_f32p] * 6 + [C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                                                         C.POINTER(T.Params), C.c_int, _f64p, _f64p]
+    L.lsdo_sim3_normal_equations.restype = C.c_int
+    L.lsdo_track_sim3.argtypes = [C.c_int] + [_f32p] * 6 + [C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                                            C.POINTER(T.Params), _f64p, _f64p, C.POINTER(T.TrackStats)]
+    L.lsdo_track_sim3.restype = C.c_int
+    L.lsdo_sim3_exp.argtypes = [_f64p, _f64p]
+    _vp = C.c_void_p
+    L.lsdo_energy_points.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                                     C.POINTER(T.Params), C.c_int, _vp, _vp]
+    L.lsdo_energy_points.restype = C.c_int
+    L.lsdo_energy.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_int, C.POINTER(T.Intrinsics),
+                              C.POINTER(T.Params), C.c_int, _f64p, C.c_int] + [_vp] * 8 + \
+                             [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.lsdo_energy.restype = C.c_int
+    L.lsdo_energy_refine.argtypes = [C.c_int, _f32p, _f32p, _f32p, C.c_int, _f32p, C.c_int, C.c_int,
+                                     C.POINTER(T.Intrinsics), C.POINTER(T.Params), C.c_int, _f64p, C.c_int, _vp,
+                                     _f32p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_long),
+                                     C.c_int]
+    L.lsdo_energy_refine.restype = C.c_int
+    L.lsdo_cloud_build.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                   _vp, _vp, _vp]
+    L.lsdo_cloud_build.restype = C.c_int
+    L.lsdo_undistort_map.argtypes = [C.POINTER(T.Calibration), C.c_int, C.c_int, C.POINTER(T.Intrinsics), _f32p]
+    L.lsdo_undistort.argtypes = [_vp, C.c_int, C.c_int, _f32p, C.c_int, _vp]
+    L.lsdo_hardware_threads.restype = C.c_int
+    return L
 
 
 def default_params() -> T.Params:
@@ -198,8 +224,10 @@ def track_trace(pair, init=None, params=None, double=False):
     return rc, out.reshape(3, 4), st, buf[:8 * n.value].reshape(-1, 8)
 
 
-def track_batch(pairs, inits=None, params: T.Params = None, threads: int = None):
-    """CPU baseline of the batched workload (float, pairs spread over threads)."""
+def track_batch(pairs, inits=None, params: T.Params = None, threads: int = None, double: bool = False,
+                fast: bool = False):
+    """The batched workload on the CPU, pairs spread over threads: float (the CPU baseline; `fast`
+    selects the speed build) or double (the FP64 oracle of the whole batch)."""
     p = params or default_params()
     n = len(pairs)
     threads = threads or hardware_threads()
@@ -210,8 +238,10 @@ def track_batch(pairs, inits=None, params: T.Params = None, threads: int = None)
     init = np.concatenate([np.eye(3, 4).ravel() for _ in range(n)]) if inits is None else np.ascontiguousarray(inits, np.float64).ravel()
     out = np.zeros(12 * n, np.float64)
     stats = (T.TrackStats * n)()
-    lib().lsdo_track_batch_f(n, widths, heights, intr, cat("ref_image"), cat("ref_idepth"), cat("ref_idepth_var"),
-                             cat("new_image"), init, out, stats, C.byref(p), threads)
+    L = fast_lib() if fast else lib()
+    f = L.lsdo_track_batch_d if double else L.lsdo_track_batch_f
+    f(n, widths, heights, intr, cat("ref_image"), cat("ref_idepth"), cat("ref_idepth_var"),
+      cat("new_image"), init, out, stats, C.byref(p), threads)
     return out.reshape(n, 3, 4), stats
 
 
@@ -232,7 +262,7 @@ def _planes(buf, h, w):
 
 
 def depth_pipeline(seq, params=None, double=False, regularize=True, propagate=True, n_refs=None, threads=1,
-                   init_idepth=None, init_var=None):
+                   init_idepth=None, init_var=None, fast=False):
     """DepthMap::updateKeyframe over the sequence's references (+ regularize), then createKeyFrame
     (propagate + regularize) into the next frame.  Returns (after_update, after_propagate) dicts."""
     p = params or default_params()
@@ -245,7 +275,8 @@ def depth_pipeline(seq, params=None, double=False, regularize=True, propagate=Tr
     nimg = np.ascontiguousarray(seq.next_image, np.float32) if propagate else None
     knew = np.ascontiguousarray(_inv(seq.next_to_key), np.float64).ravel() if propagate else None
     flags = (1 if regularize else 0) | (2 if regularize else 0)
-    f = lib().lsdo_depth_pipeline_d if double else lib().lsdo_depth_pipeline_f
+    L = fast_lib() if fast else lib()
+    f = L.lsdo_depth_pipeline_d if double else L.lsdo_depth_pipeline_f
     d0 = seq.init_idepth if init_idepth is None else init_idepth
     v0 = seq.init_var if init_var is None else init_var
     f(w, h, C.byref(_intr(seq.intr)), C.byref(p), np.ascontiguousarray(seq.key_image, np.float32),
@@ -349,7 +380,7 @@ def energy(key_image, key_idepth, key_var, frame_image, intr, w, h, ref_to_frame
 
 
 def energy_refine(key_image, key_idepth, key_var, frame_images, ref_to_frames, intr, w, h, level=0, steps=50,
-                  rho=None, sigma2=None, params=None, double=False, threads=None):
+                  rho=None, sigma2=None, params=None, double=False, threads=None, fast=False):
     """Per-point inverse-depth refinement over the frames; returns (rho, E_before, E_after, refined)."""
     p = params or default_params()
     f = lambda a: np.ascontiguousarray(a, np.float32)
@@ -360,7 +391,7 @@ def energy_refine(key_image, key_idepth, key_var, frame_images, ref_to_frames, i
     poses = np.ascontiguousarray(np.stack([np.asarray(T_, np.float64).reshape(3, 4) for T_ in ref_to_frames]))
     sigma2 = None if sigma2 is None else f(sigma2)
     e0, e1, cnt = C.c_double(), C.c_double(), C.c_long()
-    rc = lib().lsdo_energy_refine(int(double), f(key_image), f(key_idepth), f(key_var), len(frame_images), imgs, w, h,
+    rc = (fast_lib() if fast else lib()).lsdo_energy_refine(int(double), f(key_image), f(key_idepth), f(key_var), len(frame_images), imgs, w, h,
                                   C.byref(_intr(intr)), C.byref(p), level, poses.ravel(), steps, _ptr(sigma2), rho,
                                   C.byref(e0), C.byref(e1), C.byref(cnt), threads or hardware_threads())
     assert rc == 0

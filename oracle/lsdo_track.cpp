@@ -695,13 +695,17 @@ int lsdo_track_se3_d(const float* kimg, const float* idepth, const float* var, c
   return track_impl<double>(kimg, idepth, var, fimg, w, h, k, p, init, out, st, threads);
 }
 
-// CPU baseline for the batched workload: n independent pairs (arrays back to back, like
-// lsdg_batch_load), pairs spread over `threads` std::threads, each pair tracked single-threaded
-// in float.  Includes both pyramids and the reference points, as the GPU batch step does.
-int lsdo_track_batch_f(int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
-                       const float* ref_images, const float* ref_idepth, const float* ref_var,
-                       const float* new_images, const double* init, double* out,
-                       lsdg_track_stats* stats, const lsdg_params* p, int threads) {
+// The batched workload on the CPU: n independent pairs (arrays back to back, like
+// lsdg_batch_load), pairs spread over `threads` std::threads, each pair tracked single-threaded.
+// Includes both pyramids and the reference points, as the GPU batch step does.  The float form is
+// the CPU baseline, the double form the FP64 oracle of a whole batch.
+}  // extern "C"
+
+template <class T>
+static int track_batch_impl(int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
+                            const float* ref_images, const float* ref_idepth, const float* ref_var,
+                            const float* new_images, const double* init, double* out,
+                            lsdg_track_stats* stats, const lsdg_params* p, int threads) {
   std::vector<size_t> off(n + 1, 0);
   for (int i = 0; i < n; ++i) off[i + 1] = off[i] + (size_t)widths[i] * heights[i];
   std::vector<std::thread> th;
@@ -710,14 +714,32 @@ int lsdo_track_batch_f(int n, const int* widths, const int* heights, const lsdg_
     for (;;) {
       int i = next.fetch_add(1);
       if (i >= n) break;
-      track_impl<float>(ref_images + off[i], ref_idepth + off[i], ref_var + off[i], new_images + off[i],
-                        widths[i], heights[i], &intr[i], p, init + 12 * i, out + 12 * i, &stats[i], 1);
+      track_impl<T>(ref_images + off[i], ref_idepth + off[i], ref_var + off[i], new_images + off[i],
+                    widths[i], heights[i], &intr[i], p, init + 12 * i, out + 12 * i, &stats[i], 1);
     }
   };
   int nt = std::max(1, threads);
   for (int k = 0; k < nt; ++k) th.emplace_back(work);
   for (auto& t : th) t.join();
   return 0;
+}
+
+extern "C" {
+
+int lsdo_track_batch_f(int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
+                       const float* ref_images, const float* ref_idepth, const float* ref_var,
+                       const float* new_images, const double* init, double* out,
+                       lsdg_track_stats* stats, const lsdg_params* p, int threads) {
+  return track_batch_impl<float>(n, widths, heights, intr, ref_images, ref_idepth, ref_var, new_images, init, out,
+                                 stats, p, threads);
+}
+
+int lsdo_track_batch_d(int n, const int* widths, const int* heights, const lsdg_intrinsics* intr,
+                       const float* ref_images, const float* ref_idepth, const float* ref_var,
+                       const float* new_images, const double* init, double* out,
+                       lsdg_track_stats* stats, const lsdg_params* p, int threads) {
+  return track_batch_impl<double>(n, widths, heights, intr, ref_images, ref_idepth, ref_var, new_images, init, out,
+                                  stats, p, threads);
 }
 
 int lsdo_hardware_threads(void) { return (int)std::thread::hardware_concurrency(); }
