@@ -369,10 +369,11 @@ LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* thr
  * (split = -1: a single launch over all levels). */
 LSDG_API lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* batch, int* split, int* threads, int* minblocks,
                                       int* cluster);
-/* Test hook for the batch build's bounded wait: in the following steps band 0 of keyframe `frame`
- * publishes no point counts, so the other bands of that keyframe wait until their limit and the
- * step reports LSDG_TIMEOUT from lsdg_batch_read / _collect (the context stays usable; -1 turns it
- * off).  The step's graph is captured again. */
+/* TEST HOOK -- not part of the tracking API; the library's own tests call it, applications never
+ * should.  It exercises the batch build's bounded wait: in the following steps band 0 of keyframe
+ * `frame` publishes no point counts, so the other bands of that keyframe wait until their limit and
+ * the step reports LSDG_TIMEOUT from lsdg_batch_read / _collect (the context stays usable; -1 turns
+ * it off).  The step's graph is captured again and the tile shape is tuned again at the next run. */
 LSDG_API lsdg_status lsdg_batch_test_withhold(lsdg_ctx* ctx, lsdg_batch* batch, int frame);
 /* Read back the tracking reference points the batch's last step built for pair `pair`'s keyframe at
  * one level (the layout of lsdg_frame_get_points; synchronises the context stream). */
@@ -436,9 +437,13 @@ LSDG_API lsdg_status lsdg_depth_create_keyframe(lsdg_ctx* ctx, lsdg_depthmap* dm
  * that every GPU which loads the library holds until the process exits: at most 1280 x 960 =
  * 1,228,800 pixels (9.8 MB); larger sizes return LSDG_INVALID_ARG.  The first call on a device looks
  * up that array's device address (cudaGetSymbolAddress), so make the first call on each device before
- * any stream capture.  All calls share the array: calls that overlap on the GPU (different streams,
- * or different host threads, on one device) race on it -- serialise them.  Errors are reported by the
- * return value only (there is no context for lsdg_last_error). */
+ * any stream capture.  The looked-up address is kept per device number for the life of the
+ * process: it belongs to the device's primary context (the one the CUDA runtime uses), so do not call
+ * this from another context on the same device, nor after cudaDeviceReset.  All calls share the
+ * array: calls that overlap on the GPU (different streams, or different host threads, on one device)
+ * race on it -- serialise them.  Errors are reported by the return value only (there is no context
+ * for lsdg_last_error); a CUDA error already pending on the calling thread when the call starts is
+ * left in place and the call returns LSDG_CUDA_ERROR without enqueuing anything. */
 LSDG_API lsdg_status lsdg_depth_propagate_noalloc(void* stream, int width, int height, const lsdg_intrinsics* intr,
                                                   const lsdg_params* params, const double old_to_new[12],
                                                   const float* old_image, const float* new_image,

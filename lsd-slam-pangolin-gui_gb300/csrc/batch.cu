@@ -636,6 +636,7 @@ lsdg_status lsdg_batch_test_withhold(lsdg_ctx* ctx, lsdg_batch* b, int frame) {
   if (st != LSDG_OK) return st;
   b->test_withhold = frame;
   for (auto& s : b->slot) s.graph_epoch = -1;  // capture again with the new launch argument
+  b->tune_epoch = -1;  // a shape tuned on withheld (incomplete) points is not kept: tune again
   return LSDG_OK;
 }
 

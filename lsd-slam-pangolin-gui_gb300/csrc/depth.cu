@@ -780,6 +780,9 @@ extern "C" lsdg_status lsdg_depth_propagate_noalloc(void* stream, int width, int
     return LSDG_INVALID_ARG;
   if (width < 1 || height < 1 || (long)width * height > kNoAllocMaxPixels) return LSDG_INVALID_ARG;
   if (!(intr->fx > 0) || !(intr->fy > 0)) return LSDG_INVALID_ARG;
+  // an error someone else left pending stays theirs: the final cudaGetLastError then reports this
+  // call's launches only
+  if (cudaPeekAtLastError() != cudaSuccess) return LSDG_CUDA_ERROR;
   unsigned long long* keys = nullptr;
   const lsdg_status st = noalloc_zbuffer(&keys);
   if (st != LSDG_OK) return st;

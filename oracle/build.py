@@ -6,8 +6,9 @@ and those kernels then round every operation identically), no -ffast-math, the d
 set (the same source gives the same results on x86_64 and aarch64 hosts).
 
 oracle/liblsdo_fast.so, the timed CPU baseline: the same sources with -O3, FMA contraction allowed
-and the instruction set of the benchmark host's cores named explicitly (-mcpu=neoverse-v2 for the
-Grace cores of an aarch64 GB300 host; other hosts keep their default target).  It stands in for the
+and code scheduled for the benchmark host's cores (-mtune=neoverse-v2 for the Grace cores of an
+aarch64 GB300 host, on the base Armv8-A instruction set with NEON; other hosts keep their default
+target).  It stands in for the
 upstream CPU path's SSE build flags (CMakeLists.txt:57-59).  Its results differ from the parity
 build in the last bits and are only ever checked by tolerance against the FP64 oracle.
 
@@ -33,7 +34,10 @@ COMMON = ["-std=c++17", "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-fu
 def fast_flags() -> list:
     flags = ["-O3", "-ffp-contract=fast", "-fno-math-errno", "-funroll-loops"]
     if platform.machine() in ("aarch64", "arm64"):
-        flags.append("-mcpu=neoverse-v2")
+        # scheduled for the Grace cores, on the base Armv8-A instruction set with NEON: a build for
+        # the full neoverse-v2 target (-mcpu) stopped with SIGILL on a GB300 host whose cores do not
+        # expose every extension of that target
+        flags.append("-mtune=neoverse-v2")
     return flags
 
 
@@ -68,8 +72,8 @@ def build_fast(force: bool = False) -> str:
         _fast_used = fast_flags()
         return _build(FAST_LIB, _fast_used, force)
     except subprocess.CalledProcessError:
-        # a compiler that does not know the named core: the same build on its default target
-        _fast_used = [f for f in fast_flags() if not f.startswith("-mcpu")]
+        # a compiler that does not know the named core: the same build without the tuning
+        _fast_used = [f for f in fast_flags() if not f.startswith("-mtune")]
         return _build(FAST_LIB, _fast_used, True)
 
 

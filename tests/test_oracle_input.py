@@ -70,12 +70,15 @@ def test_calibration_xml_reader():
 
 
 def test_reference_sample_calibration_parses():
-    """The reference's own sample calibration file, where the reference tree is present."""
-    path = "/root/reference/d2_camera.xml"
-    if not os.path.exists(path):
-        pytest.skip("reference tree not present")
+    """The reference's own sample calibration (d2_camera.xml at the reference's top level, named by
+    d2_ex1605l3_one.conf), kept as a fixture in tests/golden/."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "d2_camera.xml")
     c = lsdg.calibration_load_xml(path)
-    assert c.model == T.CALIB_FRAME and (c.width, c.height) == (1920, 1080) and c.f > 1000
+    assert c.model == T.CALIB_FRAME and (c.width, c.height) == (1920, 1080)
+    assert (c.f, c.cx, c.cy, c.b2) == (1430.15016509976, -24.1342060175983, 17.5452248329602, -4.25145544487403)
+    assert (c.k1, c.k2, c.p1, c.p2) == (-0.118322055927498, 0.293632083518507, 0.000330080086304322,
+                                        0.00182154893322038)
+    assert (c.b1, c.k3, c.k4) == (0.0, 0.0, 0.0)
 
 
 def test_map_matches_numpy_restatement():
