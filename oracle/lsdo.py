@@ -112,6 +112,10 @@ def _bind(L):
     L.lsdo_undistort_map.argtypes = [C.POINTER(T.Calibration), C.c_int, C.c_int, C.POINTER(T.Intrinsics), _f32p]
     L.lsdo_undistort.argtypes = [_vp, C.c_int, C.c_int, _f32p, C.c_int, _vp]
     L.lsdo_hardware_threads.restype = C.c_int
+    L.lsdo_depth_trace.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(T.Intrinsics), C.POINTER(T.Params), _f32p,
+                                   _f32p, _f32p, C.c_int, _f32p, _f64p, C.c_void_p, C.c_void_p, C.c_int,
+                                   np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS"), C.c_void_p, C.c_long]
+    L.lsdo_depth_trace.restype = C.c_long
     return L
 
 
@@ -284,6 +288,38 @@ def depth_pipeline(seq, params=None, double=False, regularize=True, propagate=Tr
       nimg.ctypes.data if propagate else None, knew.ctypes.data if propagate else None, flags,
       upd.ctypes.data, prop.ctypes.data if propagate else None, threads)
     return _planes(upd, h, w), (_planes(prop, h, w) if propagate else None)
+
+
+# One record of the depth filter's decision trace (lsdo_depth.cpp, DecisionRec).
+DECISION_DTYPE = np.dtype([("pixel", np.int32), ("stage", np.int32), ("ref", np.int32), ("id", np.int32),
+                           ("outcome", np.int32), ("aux", np.int32), ("q", np.float64), ("thr", np.float64)])
+
+
+def depth_trace(seq, mask, double=False, params=None, regularize=True, propagate=True, n_refs=None):
+    """The depth_pipeline of `seq` with every threshold decision recorded for the pixels where
+    `mask` is true (stage 0 observe, 1 the update's regularisation, 2 propagation keyed by the old
+    keyframe pixel, 3 the new keyframe's regularisation), in execution order."""
+    p = params or default_params()
+    h, w = seq.h, seq.w
+    n = len(seq.ref_images) if n_refs is None else n_refs
+    refs = np.ascontiguousarray(np.concatenate([r.ravel() for r in seq.ref_images[:n]]), np.float32)
+    poses = np.concatenate([np.ascontiguousarray(_inv(T_), np.float64).ravel() for T_ in seq.ref_frame_to_key[:n]])
+    nimg = np.ascontiguousarray(seq.next_image, np.float32) if propagate else None
+    knew = np.ascontiguousarray(_inv(seq.next_to_key), np.float64).ravel() if propagate else None
+    flags = (1 if regularize else 0) | (2 if regularize else 0)
+    m = np.ascontiguousarray(np.asarray(mask, bool).ravel(), np.uint8)
+    cap = 1 << 16
+    while True:
+        out = np.zeros(cap, DECISION_DTYPE)
+        got = lib().lsdo_depth_trace(int(double), w, h, C.byref(_intr(seq.intr)), C.byref(p),
+                                     np.ascontiguousarray(seq.key_image, np.float32),
+                                     np.ascontiguousarray(seq.init_idepth, np.float32),
+                                     np.ascontiguousarray(seq.init_var, np.float32), n, refs, poses,
+                                     nimg.ctypes.data if propagate else None, knew.ctypes.data if propagate else None,
+                                     flags, m, out.ctypes.data, cap)
+        if got <= cap:
+            return out[:got]
+        cap = int(got)
 
 
 def _inv(T_):

@@ -35,6 +35,48 @@ struct DepthState {
   }
 };
 
+// ---------------------------------------------------------------------------------------------
+// Decision trace (tests only): every threshold decision of the filter can be recorded for the
+// pixels of a mask, with the quantity it compares and its threshold, so that a test can find, for
+// a pixel whose flags differ between the float and the FP64 runs, the first decision the two runs
+// took differently and check that it straddles its threshold by a rounding-sized margin.  Tracing
+// runs single-threaded; with no trace installed `note` is one predictable branch and changes no
+// arithmetic (it receives values already computed).
+// ---------------------------------------------------------------------------------------------
+enum DecisionId {
+  D_GRAD = 1, D_EPL, D_COS, D_AZ, D_EPLLEN, D_RANGE, D_Z, D_PAD, D_MAXLEN, D_ORIENT, D_NWIN, D_SAMPLE, D_WIN,
+  D_ARGMIN, D_MAXSSD, D_UNIQUE, D_DEN, D_CLAMP_HI, D_CLAMP_LO, D_AXIS, D_DOBS, D_INIT, D_CHI2, D_VALDROP,
+  D_BLLIMIT,
+  D_R_HASDEPTH = 40, D_R_NVAL, D_R_COMPAT, D_R_SUPPORT, D_R_FILL,
+  D_P_Z = 60, D_P_RX, D_P_RY, D_P_BOUND, D_P_PHOTO
+};
+
+struct DecisionRec {
+  int32_t pixel, stage, ref, id, outcome, aux;
+  double q, thr;
+};
+
+struct TraceSink {
+  std::vector<DecisionRec>* out = nullptr;
+  const uint8_t* mask = nullptr;
+  int pixel = 0, stage = 0, ref = 0;
+};
+static thread_local TraceSink t_sink;
+
+static inline bool tracing() { return t_sink.out && t_sink.mask[t_sink.pixel]; }
+
+template <class T>
+static inline bool note(int id, T q, T thr, bool outcome, int aux = 0) {
+  if (tracing())
+    t_sink.out->push_back({t_sink.pixel, t_sink.stage, t_sink.ref, id, outcome ? 1 : 0, aux, (double)q, (double)thr});
+  return outcome;
+}
+
+template <class T>
+static inline void note_value(int id, int value, T q, T thr, int aux = 0) {
+  if (tracing()) t_sink.out->push_back({t_sink.pixel, t_sink.stage, t_sink.ref, id, value, aux, (double)q, (double)thr});
+}
+
 // Per-reference geometry: a(u) = K R K^-1 (x, y, 1), b = K t: the reference pixel of inverse depth
 // d is (a.xy + b.xy d) / (a.z + b.z d).  c = -R^T t is the reference camera centre in the keyframe.
 template <class T>
@@ -83,28 +125,28 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
   const T gx = gxk[i], gy = gyk[i];
   const T g2 = gx * gx + gy * gy;
   const T mg = (T)p.min_grad;
-  if (!(g2 >= mg * mg)) return;
+  if (!note(D_GRAD, g2, mg * mg, g2 >= mg * mg)) return;
   const T xf = (T)x, yf = (T)y;
   // keyframe epipolar direction (away from the epipole of the reference camera)
   T lkx = G.c[2] * (xf - cx) - fx * G.c[0];
   T lky = G.c[2] * (yf - cy) - fy * G.c[1];
   const T el2 = lkx * lkx + lky * lky;
-  if (!(el2 > (T)1e-12)) return;
+  if (!note(D_EPL, el2, (T)1e-12, el2 > (T)1e-12)) return;
   const T einv = (T)1 / std::sqrt(el2);
   lkx = lkx * einv;
   lky = lky * einv;
   const T gp = gx * lkx + gy * lky;
   const T cos2 = (gp * gp) / g2;
-  if (!(cos2 >= (T)p.min_grad_along_epl2)) return;
+  if (!note(D_COS, cos2, (T)p.min_grad_along_epl2, cos2 >= (T)p.min_grad_along_epl2)) return;
   const T ax = (G.M[0] * xf + G.M[1] * yf) + G.M[2];
   const T ay = (G.M[3] * xf + G.M[4] * yf) + G.M[5];
   const T az = (G.M[6] * xf + G.M[7] * yf) + G.M[8];
   const T bx = G.b[0], by = G.b[1], bz = G.b[2];
-  if (!(az > (T)0)) return;
+  if (!note(D_AZ, az, (T)0, az > (T)0)) return;
   // reference epipolar direction (increasing inverse depth) and disparity per unit inverse depth
   const T rx = bx * az - ax * bz, ry = by * az - ay * bz;
   const T rn = std::sqrt(rx * rx + ry * ry);
-  if (!(rn / (az * az) >= (T)p.min_epl_length)) return;
+  if (!note(D_EPLLEN, rn / (az * az), (T)p.min_epl_length, rn / (az * az) >= (T)p.min_epl_length)) return;
   const T lrx = rx / rn, lry = ry / rn;
   // search range in inverse depth
   T dlo, dhi;
@@ -118,19 +160,19 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
     dlo = (T)p.min_idepth;
     dhi = (T)p.max_idepth;
   }
-  if (!(dlo < dhi)) return;
+  if (!note(D_RANGE, dlo, dhi, dlo < dhi)) return;
   const T zlo = az + bz * dlo, zhi = az + bz * dhi;
-  if (!(zlo > (T)0 && zhi > (T)0)) return;
+  if (!note(D_Z, zlo < zhi ? zlo : zhi, (T)0, zlo > (T)0 && zhi > (T)0)) return;
   T pfx = (ax + bx * dlo) / zlo, pfy = (ay + by * dlo) / zlo;
   const T pnx = (ax + bx * dhi) / zhi, pny = (ay + by * dhi) / zhi;
   T L = (pnx - pfx) * lrx + (pny - pfy) * lry;
-  if (L < (T)p.min_search_len) {
+  if (note(D_PAD, L, (T)p.min_search_len, L < (T)p.min_search_len)) {
     const T pad = ((T)p.min_search_len - L) * (T)0.5;
     pfx = pfx - lrx * pad;
     pfy = pfy - lry * pad;
     L = (T)p.min_search_len;
   }
-  if (L > (T)p.max_search_len) L = (T)p.max_search_len;
+  if (note(D_MAXLEN, L, (T)p.max_search_len, L > (T)p.max_search_len)) L = (T)p.max_search_len;
   // orient the keyframe template so that its image runs along +lr (checked at the mid depth)
   {
     const T dm = (dlo + dhi) * (T)0.5;
@@ -140,7 +182,7 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
     const T z1 = a1z + bz * dm;
     const T qx = (a1x + bx * dm) / z1 - (ax + bx * dm) / z0;
     const T qy = (a1y + by * dm) / z1 - (ay + by * dm) / z0;
-    if (qx * lrx + qy * lry < (T)0) {
+    if (note(D_ORIENT, qx * lrx + qy * lry, (T)0, qx * lrx + qy * lry < (T)0)) {
       lkx = -lkx;
       lky = -lky;
     }
@@ -150,6 +192,7 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
   // slide the 5-sample window along the reference line: window s (0 <= s <= n) is centred at
   // pf + s lr and uses samples s-2 .. s+2
   const int n = (int)L;
+  note_value(D_NWIN, n, L, (T)n);
   const T INF = (T)INFINITY;
   const T umax = (T)(w - 1), vmax = (T)(h - 1);
   T r[5] = {0, 0, 0, 0, 0};
@@ -163,6 +206,13 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
     }
     const T sx = pfx + (T)j * lrx, sy = pfy + (T)j * lry;
     ok[4] = sx >= (T)0 && sy >= (T)0 && sx < umax && sy < vmax;
+    if (tracing()) {  // distance of the sample to the image border (negative: outside)
+      T m = sx;
+      if (sy < m) m = sy;
+      if (umax - sx < m) m = umax - sx;
+      if (vmax - sy < m) m = vmax - sy;
+      note(D_SAMPLE, m, (T)0, ok[4], j);
+    }
     r[4] = ok[4] ? bilinear(Ir, w, sx, sy) : (T)0;
     if (j < 2) continue;
     const int s = j - 2;
@@ -171,6 +221,7 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
       const T d0 = r[0] - tk[0], d1 = r[1] - tk[1], d2 = r[2] - tk[2], d3 = r[3] - tk[3], d4 = r[4] - tk[4];
       e = (((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3) + d4 * d4;
     }
+    note_value(D_WIN, s, e, (T)0);
     if (e < e1) {
       if (s1 >= 0 && s - s1 >= 2 && e1 < e2) e2 = e1;
       ebefore = eprev;
@@ -183,25 +234,26 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
     }
     eprev = e;
   }
+  note_value(D_ARGMIN, s1, e1, e2);
   if (s1 < 0) return;                          // no window inside the reference image
-  if (e1 > (T)p.max_ssd * (T)5) {              // no acceptable match: count a failure
+  if (note(D_MAXSSD, e1, (T)p.max_ssd * (T)5, e1 > (T)p.max_ssd * (T)5)) {  // no acceptable match: count a failure
     ++bl;
     return;
   }
-  if (!(e2 > (T)p.unique_ratio * e1)) return;  // ambiguous
+  if (!note(D_UNIQUE, e2, (T)p.unique_ratio * e1, e2 > (T)p.unique_ratio * e1)) return;  // ambiguous
   T off = (T)0;
   if (ebefore < INF && eafter < INF) {
     const T den = (ebefore - (T)2 * e1) + eafter;
-    if (den > (T)0) {
+    if (note(D_DEN, den, (T)0, den > (T)0)) {
       off = ((T)0.5 * (ebefore - eafter)) / den;
-      if (off > (T)0.5) off = (T)0.5;
-      if (off < (T)-0.5) off = (T)-0.5;
+      if (note(D_CLAMP_HI, off, (T)0.5, off > (T)0.5)) off = (T)0.5;
+      if (note(D_CLAMP_LO, off, (T)-0.5, off < (T)-0.5)) off = (T)-0.5;
     }
   }
   const T sm = (T)s1 + off;
   const T mx = pfx + sm * lrx, my = pfy + sm * lry;
   T dobs, alpha;
-  if (std::fabs(lrx) >= std::fabs(lry)) {
+  if (note(D_AXIS, std::fabs(lrx), std::fabs(lry), std::fabs(lrx) >= std::fabs(lry))) {
     const T den = mx * bz - bx;
     dobs = (ax - mx * az) / den;
     alpha = std::fabs(lrx * (bx * az - ax * bz)) / (den * den);
@@ -210,11 +262,11 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
     dobs = (ay - my * az) / den;
     alpha = std::fabs(lry * (by * az - ay * bz)) / (den * den);
   }
-  if (!(dobs > (T)0)) return;
+  if (!note(D_DOBS, dobs, (T)0, dobs > (T)0)) return;
   const T geo = (T)p.epipolar_var / cos2;
   const T photo = ((T)2 * (T)p.image_var) / (gp * gp);
   const T vobs = (alpha * alpha) * (geo + photo);
-  if (val <= 0) {
+  if (note(D_INIT, (T)val, (T)0, val <= 0)) {
     d = dobs;
     var = vobs;
     val = p.validity_init;
@@ -222,10 +274,10 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
   }
   const T dd = dobs - d;
   const T chi2 = (dd * dd) / (var + vobs);
-  if (chi2 > (T)p.fuse_chi2) {
+  if (note(D_CHI2, chi2, (T)p.fuse_chi2, chi2 > (T)p.fuse_chi2)) {
     ++bl;
     val -= p.validity_penalty;
-    if (val <= 0) {
+    if (note(D_VALDROP, (T)val, (T)0, val <= 0)) {
       val = 0;
       d = (T)-1;
       var = (T)-1;
@@ -279,8 +331,10 @@ static void observe_all(const DepthFrame<T>& K, int n_refs, const float* ref_ima
         const size_t i = (size_t)y * w + x;
         T d = S.d[i], v = S.v[i];
         int val = S.val[i], bl = S.bl[i];
+        t_sink.pixel = (int)i;
         for (int r = 0; r < n_refs; ++r) {
-          if (bl >= p.blacklist_limit) break;
+          t_sink.ref = r;
+          if (note(D_BLLIMIT, (T)bl, (T)p.blacklist_limit, bl >= p.blacklist_limit)) break;
           observe_pixel<T>(x, y, w, h, K.I.data(), K.gx.data(), K.gy.data(), R[r].data(), G[r], fx, fy, cx, cy, p,
                            d, v, val, bl);
         }
@@ -299,31 +353,34 @@ static void observe_all(const DepthFrame<T>& K, int n_refs, const float* ref_ima
 // regularizeDepthMap + hole filling: smoothed planes from the raw hypotheses, then the commit that
 // drops removed hypotheses from the raw state (var_smoothed == -2 marks a removal).
 template <class T>
-static void regularize(int w, int h, const lsdg_params& p, DepthState<T>& S, int threads) {
+static void regularize(int w, int h, const lsdg_params& p, DepthState<T>& S, int threads, int stage) {
   const int R = p.reg_radius;
+  t_sink.stage = stage;
+  t_sink.ref = 0;
   auto rows = [&](int y0, int y1) {
     for (int y = y0; y < y1; ++y)
       for (int x = 0; x < w; ++x) {
         const size_t i = (size_t)y * w + x;
+        t_sink.pixel = (int)i;
         T sw = 0, swd = 0;
         int cnt = 0;
-        if (S.val[i] > 0) {
+        if (note(D_R_HASDEPTH, (T)S.val[i], (T)0, S.val[i] > 0)) {
           const T d = S.d[i], v = S.v[i];
           for (int dy = -R; dy <= R; ++dy)
             for (int dx = -R; dx <= R; ++dx) {
               const int nx = x + dx, ny = y + dy;
               if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
               const size_t j = (size_t)ny * w + nx;
-              if (S.val[j] <= 0) continue;
+              if (!note(D_R_NVAL, (T)S.val[j], (T)0, S.val[j] > 0, (int)j)) continue;
               const T dd = S.d[j] - d;
-              if (dd * dd <= (T)p.reg_chi2 * (S.v[j] + v)) {
+              if (note(D_R_COMPAT, dd * dd, (T)p.reg_chi2 * (S.v[j] + v), dd * dd <= (T)p.reg_chi2 * (S.v[j] + v), (int)j)) {
                 const T wt = (T)1 / S.v[j];
                 sw = sw + wt;
                 swd = swd + wt * S.d[j];
                 if (dx != 0 || dy != 0) ++cnt;
               }
             }
-          if (cnt < p.reg_min_support) {
+          if (note(D_R_SUPPORT, (T)cnt, (T)p.reg_min_support, cnt < p.reg_min_support)) {
             S.sm[i] = (T)-1;
             S.vsm[i] = (T)-2;
           } else {
@@ -336,13 +393,13 @@ static void regularize(int w, int h, const lsdg_params& p, DepthState<T>& S, int
               const int nx = x + dx, ny = y + dy;
               if (nx < 0 || ny < 0 || nx >= w || ny >= h) continue;
               const size_t j = (size_t)ny * w + nx;
-              if (S.val[j] <= 0) continue;
+              if (!note(D_R_NVAL, (T)S.val[j], (T)0, S.val[j] > 0, (int)j)) continue;
               const T wt = (T)1 / S.v[j];
               sw = sw + wt;
               swd = swd + wt * S.d[j];
               ++cnt;
             }
-          if (cnt >= p.fill_min_support) {
+          if (note(D_R_FILL, (T)cnt, (T)p.fill_min_support, cnt >= p.fill_min_support)) {
             S.sm[i] = swd / sw;
             S.vsm[i] = (T)p.fill_var_factor * ((T)cnt / sw);
           } else {
@@ -382,23 +439,31 @@ static void propagate(const DepthFrame<T>& Kold, const DepthFrame<T>& Knew, cons
   }
   std::vector<uint64_t> key((size_t)w * h, ~0ull);
   struct Warp { T zn, izn; int xi, yi; bool ok; };
-  auto warp = [&](int x, int y) {
+  t_sink.stage = 2;
+  t_sink.ref = 0;
+  auto warp = [&](int x, int y, bool rec) {
     Warp r{0, 0, 0, 0, false};
     const size_t i = (size_t)y * w + x;
+    TraceSink keep = t_sink;
+    if (!rec) t_sink.out = nullptr;  // the gather pass repeats the warp of a winner: not traced again
+    t_sink.pixel = (int)i;
+    struct Restore { TraceSink& s; TraceSink k; ~Restore() { s = k; } } restore{t_sink, keep};
     const T z = (T)1 / S.d[i];
     const T X = (((T)x - cx) * fxi) * z, Y = (((T)y - cy) * fyi) * z;
     const T Xn = ((Rm[0] * X + Rm[1] * Y) + Rm[2] * z) + t[0];
     const T Yn = ((Rm[3] * X + Rm[4] * Y) + Rm[5] * z) + t[1];
     const T Zn = ((Rm[6] * X + Rm[7] * Y) + Rm[8] * z) + t[2];
-    if (!(Zn > (T)p.min_z)) return r;
+    if (!note(D_P_Z, Zn, (T)p.min_z, Zn > (T)p.min_z)) return r;
     const T izn = (T)1 / Zn;
     const T un = fx * (Xn * izn) + cx, vn = fy * (Yn * izn) + cy;
     const T fxr = std::floor(un + (T)0.5), fyr = std::floor(vn + (T)0.5);
-    if (!(fxr >= (T)0 && fyr >= (T)0 && fxr <= (T)(w - 1) && fyr <= (T)(h - 1))) return r;
+    note_value(D_P_RX, (int)fxr, un + (T)0.5, fxr);
+    note_value(D_P_RY, (int)fyr, vn + (T)0.5, fyr);
+    if (!note(D_P_BOUND, fxr, fyr, fxr >= (T)0 && fyr >= (T)0 && fxr <= (T)(w - 1) && fyr <= (T)(h - 1))) return r;
     r.xi = (int)fxr;
     r.yi = (int)fyr;
     const T diff = Knew.I[(size_t)r.yi * w + r.xi] - Kold.I[i];
-    if (std::fabs(diff) > (T)p.propagate_max_photo_diff) return r;
+    if (note(D_P_PHOTO, std::fabs(diff), (T)p.propagate_max_photo_diff, std::fabs(diff) > (T)p.propagate_max_photo_diff)) return r;
     r.zn = Zn;
     r.izn = izn;
     r.ok = true;
@@ -408,7 +473,7 @@ static void propagate(const DepthFrame<T>& Kold, const DepthFrame<T>& Knew, cons
     for (int x = 0; x < w; ++x) {
       const size_t i = (size_t)y * w + x;
       if (S.val[i] <= 0) continue;
-      const Warp r = warp(x, y);
+      const Warp r = warp(x, y, true);
       if (!r.ok) continue;
       float zf = (float)r.zn;  // the key orders by the float depth (positive floats order as integers)
       uint32_t zb;
@@ -422,7 +487,7 @@ static void propagate(const DepthFrame<T>& Kold, const DepthFrame<T>& Knew, cons
     if (key[ti] == ~0ull) continue;
     const uint32_t o = (uint32_t)(key[ti] & 0xffffffffu);
     const int x = (int)(o % (uint32_t)w), y = (int)(o / (uint32_t)w);
-    const Warp r = warp(x, y);
+    const Warp r = warp(x, y, false);
     const T d = S.d[o], v = S.v[o];
     const T ratio = r.izn / d;
     const T r2 = ratio * ratio;
@@ -476,15 +541,16 @@ static int pipeline(int w, int h, const lsdg_intrinsics* k, const lsdg_params* p
   DepthState<T> S;
   const size_t n = (size_t)w * h;
   init_state<T>(init_idepth, init_var, n, *p, S);
+  t_sink.stage = 0;
   observe_all<T>(K, n_refs, ref_images, key_to_ref, *p, S, threads);
-  if (flags & 1) regularize<T>(w, h, *p, S, threads);
+  if (flags & 1) regularize<T>(w, h, *p, S, threads, 1);
   if (upd_out) dump(S, upd_out, n);
   if (new_image && key_to_new) {
     DepthFrame<T> Kn;
     make_depth_frame<T>(new_image, w, h, *k, Kn);
     DepthState<T> N;
     propagate<T>(K, Kn, key_to_new, *p, S, N);
-    if (flags & 2) regularize<T>(w, h, *p, N, threads);
+    if (flags & 2) regularize<T>(w, h, *p, N, threads, 3);
     if (prop_out) dump(N, prop_out, n);
   }
   return 0;
@@ -508,6 +574,29 @@ int lsdo_depth_pipeline_d(int w, int h, const lsdg_intrinsics* k, const lsdg_par
                           float* upd_out, float* prop_out, int threads) {
   return lsdo::pipeline<double>(w, h, k, p, key_image, init_idepth, init_var, n_refs, ref_images, key_to_ref,
                                 new_image, key_to_new, flags, upd_out, prop_out, threads);
+}
+
+// The same pipeline with the decision trace on for the pixels where mask[i] != 0 (single-threaded):
+// records in execution order, stage 0 observe (pixel = keyframe pixel, ref = reference index),
+// 1 the update's regularisation, 2 propagation (pixel = old keyframe pixel), 3 the new keyframe's
+// regularisation.  Returns the number of records (more than `cap` means some were dropped).
+long lsdo_depth_trace(int use_double, int w, int h, const lsdg_intrinsics* k, const lsdg_params* p,
+                      const float* key_image, const float* init_idepth, const float* init_var, int n_refs,
+                      const float* ref_images, const double* key_to_ref, const float* new_image,
+                      const double* key_to_new, int flags, const uint8_t* mask, lsdo::DecisionRec* out, long cap) {
+  std::vector<lsdo::DecisionRec> rec;
+  lsdo::t_sink.out = &rec;
+  lsdo::t_sink.mask = mask;
+  if (use_double)
+    lsdo::pipeline<double>(w, h, k, p, key_image, init_idepth, init_var, n_refs, ref_images, key_to_ref, new_image,
+                           key_to_new, flags, nullptr, nullptr, 1);
+  else
+    lsdo::pipeline<float>(w, h, k, p, key_image, init_idepth, init_var, n_refs, ref_images, key_to_ref, new_image,
+                          key_to_new, flags, nullptr, nullptr, 1);
+  lsdo::t_sink = lsdo::TraceSink{};
+  const long n = (long)rec.size();
+  std::memcpy(out, rec.data(), sizeof(lsdo::DecisionRec) * (size_t)(n < cap ? n : cap));
+  return n;
 }
 
 }  // extern "C"
