@@ -296,9 +296,10 @@ DECISION_DTYPE = np.dtype([("pixel", np.int32), ("stage", np.int32), ("ref", np.
 
 
 def depth_trace(seq, mask, double=False, params=None, regularize=True, propagate=True, n_refs=None):
-    """The depth_pipeline of `seq` with every threshold decision recorded for the pixels where
-    `mask` is true (stage 0 observe, 1 the update's regularisation, 2 propagation keyed by the old
-    keyframe pixel, 3 the new keyframe's regularisation), in execution order."""
+    """The depth_pipeline of `seq` with every threshold decision recorded, in execution order, for
+    the pixels where mask[stage] is true: stage 0 observe, 1 the update's regularisation,
+    2 propagation (keyed by the old keyframe pixel), 3 the new keyframe's regularisation.
+    `mask` is bool [4, h, w]."""
     p = params or default_params()
     h, w = seq.h, seq.w
     n = len(seq.ref_images) if n_refs is None else n_refs
@@ -307,7 +308,7 @@ def depth_trace(seq, mask, double=False, params=None, regularize=True, propagate
     nimg = np.ascontiguousarray(seq.next_image, np.float32) if propagate else None
     knew = np.ascontiguousarray(_inv(seq.next_to_key), np.float64).ravel() if propagate else None
     flags = (1 if regularize else 0) | (2 if regularize else 0)
-    m = np.ascontiguousarray(np.asarray(mask, bool).ravel(), np.uint8)
+    m = np.ascontiguousarray(np.asarray(mask, bool).reshape(4, h * w), np.uint8).ravel()
     cap = 1 << 16
     while True:
         out = np.zeros(cap, DECISION_DTYPE)

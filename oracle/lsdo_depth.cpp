@@ -46,7 +46,7 @@ struct DepthState {
 enum DecisionId {
   D_GRAD = 1, D_EPL, D_COS, D_AZ, D_EPLLEN, D_RANGE, D_Z, D_PAD, D_MAXLEN, D_ORIENT, D_NWIN, D_SAMPLE, D_WIN,
   D_ARGMIN, D_MAXSSD, D_UNIQUE, D_DEN, D_CLAMP_HI, D_CLAMP_LO, D_AXIS, D_DOBS, D_INIT, D_CHI2, D_VALDROP,
-  D_BLLIMIT,
+  D_BLLIMIT, D_RUNBEST, D_RUN2,
   D_R_HASDEPTH = 40, D_R_NVAL, D_R_COMPAT, D_R_SUPPORT, D_R_FILL,
   D_P_Z = 60, D_P_RX, D_P_RY, D_P_BOUND, D_P_PHOTO
 };
@@ -58,12 +58,13 @@ struct DecisionRec {
 
 struct TraceSink {
   std::vector<DecisionRec>* out = nullptr;
-  const uint8_t* mask = nullptr;
+  const uint8_t* mask = nullptr;  // [stage][pixel]: which pixels of which stage are traced
+  size_t npix = 0;
   int pixel = 0, stage = 0, ref = 0;
 };
 static thread_local TraceSink t_sink;
 
-static inline bool tracing() { return t_sink.out && t_sink.mask[t_sink.pixel]; }
+static inline bool tracing() { return t_sink.out && t_sink.mask[(size_t)t_sink.stage * t_sink.npix + t_sink.pixel]; }
 
 template <class T>
 static inline bool note(int id, T q, T thr, bool outcome, int aux = 0) {
@@ -222,15 +223,15 @@ static void observe_pixel(int x, int y, int w, int h, const T* Ik, const T* gxk,
       e = (((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3) + d4 * d4;
     }
     note_value(D_WIN, s, e, (T)0);
-    if (e < e1) {
-      if (s1 >= 0 && s - s1 >= 2 && e1 < e2) e2 = e1;
+    if (note(D_RUNBEST, e, e1, e < e1, s)) {
+      if (s1 >= 0 && s - s1 >= 2 && note(D_RUN2, e1, e2, e1 < e2, s)) e2 = e1;
       ebefore = eprev;
       e1 = e;
       s1 = s;
       eafter = INF;
     } else {
       if (s == s1 + 1) eafter = e;
-      if (s - s1 >= 2 && e < e2) e2 = e;
+      if (s - s1 >= 2 && note(D_RUN2, e, e2, e < e2, s)) e2 = e;
     }
     eprev = e;
   }
@@ -576,7 +577,8 @@ int lsdo_depth_pipeline_d(int w, int h, const lsdg_intrinsics* k, const lsdg_par
                                 new_image, key_to_new, flags, upd_out, prop_out, threads);
 }
 
-// The same pipeline with the decision trace on for the pixels where mask[i] != 0 (single-threaded):
+// The same pipeline with the decision trace on for the pixels where mask[stage * w * h + i] != 0
+// (single-threaded):
 // records in execution order, stage 0 observe (pixel = keyframe pixel, ref = reference index),
 // 1 the update's regularisation, 2 propagation (pixel = old keyframe pixel), 3 the new keyframe's
 // regularisation.  Returns the number of records (more than `cap` means some were dropped).
@@ -587,6 +589,7 @@ long lsdo_depth_trace(int use_double, int w, int h, const lsdg_intrinsics* k, co
   std::vector<lsdo::DecisionRec> rec;
   lsdo::t_sink.out = &rec;
   lsdo::t_sink.mask = mask;
+  lsdo::t_sink.npix = (size_t)w * h;
   if (use_double)
     lsdo::pipeline<double>(w, h, k, p, key_image, init_idepth, init_var, n_refs, ref_images, key_to_ref, new_image,
                            key_to_new, flags, nullptr, nullptr, 1);

@@ -58,13 +58,25 @@ def test_update_regularize_propagate_bit_exact_640(ctx, seq640):
 
 
 def test_flags_and_idepth_vs_fp64_oracle(ctx, seq640):
-    got, _ = _gpu_pipeline(ctx, seq640, propagate=False)
-    ref, _ = lsdo.depth_pipeline(seq640, propagate=False, double=True)
-    assert np.mean(got["validity"] == ref["validity"]) >= 0.999
-    assert np.mean(got["blacklist"] == ref["blacklist"]) >= 0.999
-    both = (got["validity"] > 0) & (ref["validity"] > 0) & (ref["var"] < 0.01)
-    rel = np.abs(got["idepth"][both] - ref["idepth"][both]) / ref["idepth"][both]
-    assert np.mean(rel <= 1e-3) >= 0.99, np.mean(rel <= 1e-3)
+    """Against the FP64 oracle: flags agree on >= 99.9 % of pixels, the observed inverse depths
+    within 1e-3 relative on >= 99.9 % of the pixels holding one in both runs, and every pixel whose
+    flags differ -- after the update and after the propagation into the next keyframe -- is
+    explained by a decision at a float threshold boundary (tests/depth_flags.py)."""
+    import depth_flags
+    got_u, got_p = _gpu_pipeline(ctx, seq640)
+    c, upd, prop = depth_flags.classify(seq640)
+    for got, ref in ((got_u, c.upd_d), (got_p, c.prop_d)):
+        assert np.mean(got["validity"] == ref["validity"]) >= 0.999
+        assert np.mean(got["blacklist"] == ref["blacklist"]) >= 0.999
+    moved = got_u["var"] != seq640.init_var
+    both = (got_u["validity"] > 0) & (c.upd_d["validity"] > 0) & moved
+    rel = np.abs(got_u["idepth"][both] - c.upd_d["idepth"][both]) / c.upd_d["idepth"][both]
+    assert np.mean(rel <= 1e-3) >= 0.999, np.mean(rel <= 1e-3)
+    # the GPU's disagreements are the float oracle's (its state is the float oracle's bit for bit)
+    np.testing.assert_array_equal(depth_flags.flags_differ(got_u, c.upd_d), depth_flags.flags_differ(c.upd_f, c.upd_d))
+    np.testing.assert_array_equal(depth_flags.flags_differ(got_p, c.prop_d), depth_flags.flags_differ(c.prop_f, c.prop_d))
+    bad = [{k: v for k, v in r.items() if k != "via"} for r in upd + prop if not r["explained"]]
+    assert not bad, bad
 
 
 def test_depth_output_layout(ctx, seq320):
