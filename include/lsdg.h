@@ -369,12 +369,6 @@ LSDG_API lsdg_status lsdg_batch_shape(lsdg_ctx* ctx, lsdg_batch* batch, int* thr
  * (split = -1: a single launch over all levels). */
 LSDG_API lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* batch, int* split, int* threads, int* minblocks,
                                       int* cluster);
-/* The pool plan of an SE3 batch, when the autotuner chose it (pool = 1; the shapes above then do
- * not apply): one persistent grid of `grid` CTAs of `threads` over all levels, each pass of a pair
- * cut into chunks of `chunk` consecutive points that any CTA may claim; the CTA completing a pass
- * runs its LM step.  pool = 0: the cluster plan above. */
-LSDG_API lsdg_status lsdg_batch_pool_plan(lsdg_ctx* ctx, lsdg_batch* batch, int* pool, int* threads, int* grid,
-                                          int* chunk);
 /* TEST HOOK -- not part of the tracking API; the library's own tests call it, applications never
  * should.  It exercises the batch build's bounded wait: in the following steps band 0 of keyframe
  * `frame` publishes no point counts, so the other bands of that keyframe wait until their limit and

@@ -29,10 +29,6 @@ int track_max_clusters(int threads, int minblocks, int cluster, bool sim3);
 cudaError_t track_prepare();
 int track_shape_count();
 void track_shape(int i, int* threads, int* minblocks);
-cudaError_t launch_pool(const TrackArgs& a, int threads, int minblocks, int grid, cudaStream_t s);
-int pool_shape_count();
-void pool_shape(int i, int* threads, int* minblocks);
-int pool_blocks_per_sm(int threads, int minblocks);
 }  // namespace lsdg
 
 // ============================================================================================
@@ -372,19 +368,7 @@ static void split_args(const TrackArgs& a, int split, double* mid, TrackArgs* a1
   a2->accumulate_stats = 1;
 }
 
-static lsdg_status launch_pool_plan(lsdg_ctx* ctx, const TrackArgs& a, int threads, int minblocks, int grid,
-                                    int chunk) {
-  TrackArgs p = a;
-  p.pool = 1;
-  p.pool_chunk = chunk;
-  CK(ctx, launch_pool(p, threads, minblocks, grid, ctx->stream));
-  ctx->launches += 2;
-  return LSDG_OK;
-}
-
 lsdg_status run_tracker(lsdg_ctx* ctx, const TrackArgs& a, const TuneChoice& tc, bool sim3, double* mid) {
-  if (tc.pool && a.pool_ws && !sim3)
-    return launch_pool_plan(ctx, a, tc.pool_threads, tc.pool_minblocks, tc.pool_grid, tc.pool_chunk);
   if (use_split(a, tc, mid)) {
     TrackArgs a1, a2;
     split_args(a, tc.split, mid, &a1, &a2);
@@ -457,25 +441,6 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
     *out = it->second;
     return LSDG_OK;
   }
-  // LSDG_TRACK_POOL="threads,minblocks,chunk" pins a pool plan (SE3 batches; used to profile one
-  // known configuration); ignored when it does not fit the device or the batch's pool scratch.
-  if (const char* env = std::getenv("LSDG_TRACK_POOL")) {
-    int nt = 0, mb = 0, ch = 0;
-    if (a.pool_ws && !sim3 && std::sscanf(env, "%d,%d,%d", &nt, &mb, &ch) == 3) {
-      const int per_sm = pool_blocks_per_sm(nt, mb);
-      if (per_sm > 0 && ch >= a.pool_chunk && ch % nt == 0) {
-        TuneChoice tc;
-        tc.pool = 1;
-        tc.pool_threads = nt;
-        tc.pool_minblocks = mb;
-        tc.pool_grid = per_sm * ctx->sm_count;
-        tc.pool_chunk = ch;
-        ctx->tune_cache[key] = tc;
-        *out = tc;
-        return LSDG_OK;
-      }
-    }
-  }
   if (const char* env = std::getenv("LSDG_TRACK_SHAPE")) {
     int nt = 0, c = 0, mb = 1;
     if (std::sscanf(env, "%d,%d,%d", &nt, &c, &mb) >= 2) {
@@ -542,36 +507,6 @@ lsdg_status autotune(lsdg_ctx* ctx, const std::string& key, const TrackArgs& a, 
       best.c_minblocks = cmb;
       best.c_cluster = cc;
       best.c_max_clusters = cmc;
-    }
-  }
-  // pool plans (SE3 batches with pool scratch): every (shape, chunk size) over all levels
-  for (int si = 0; st == LSDG_OK && a.pool_ws && !sim3 && si < pool_shape_count(); ++si) {
-    int pnt = 0, pmb = 0;
-    pool_shape(si, &pnt, &pmb);
-    const int per_sm = pool_blocks_per_sm(pnt, pmb);
-    if (per_sm <= 0) continue;
-    const int grid = per_sm * ctx->sm_count;
-    for (int f = 1; f <= 4 && st == LSDG_OK; f *= 2) {
-      const int chunk = a.pool_chunk * f;  // a.pool_chunk: the smallest chunk the scratch allows
-      float ms = 1e30f;
-      for (int rep = 0; rep < 3 && st == LSDG_OK; ++rep) {
-        CK(ctx, cudaEventRecord(e0, ctx->stream));
-        st = launch_pool_plan(ctx, a, pnt, pmb, grid, chunk);
-        if (st != LSDG_OK) break;
-        CK(ctx, cudaEventRecord(e1, ctx->stream));
-        CK(ctx, cudaEventSynchronize(e1));
-        float t = 0;
-        CK(ctx, cudaEventElapsedTime(&t, e0, e1));
-        ms = std::min(ms, t);
-      }
-      if (st == LSDG_OK && ms < best_ms) {
-        best_ms = ms;
-        best.pool = 1;
-        best.pool_threads = pnt;
-        best.pool_minblocks = pmb;
-        best.pool_grid = grid;
-        best.pool_chunk = chunk;
-      }
     }
   }
   cudaEventDestroy(e0);

@@ -34,8 +34,6 @@ size_t frame_build_ws_bytes(int n, int levels, int max_h);
 int launch_frame_build(const FrameDev* frames, int n, int n_point_frames, int levels, int max_h,
                        unsigned long long* ws, cudaStream_t s, int withhold_frame, const uint8_t* u8,
                        const float* plane0, const int* mode);
-size_t pool_ws_bytes(int n_pairs, int max_chunks);
-void pool_sizes(long max_pix, int* chunk_min, int* max_chunks);
 }  // namespace lsdg
 
 #define CK(ctx, expr)                                         \
@@ -60,7 +58,6 @@ struct BatchSlot {
   int* d_mode = nullptr;              // 1: this step's level-0 images are the bytes in d_u8
   int* h_mode = nullptr;              // pinned {0, 1}: the sources of the mode word
   unsigned long long* d_scan = nullptr;  // one-launch build workspace (ticket, error word, band counts)
-  void* d_pool = nullptr;                // pool-plan tracker scratch (SE3 batches)
   unsigned* h_err = nullptr;          // pinned copy of the build's error word
   double* h_out = nullptr;            // pinned staging of the results
   lsdg_track_stats* h_stats = nullptr;
@@ -92,8 +89,6 @@ struct lsdg_batch {
   int next = 0;                 // slot of the next submit
   int launches_per_run = 0;
   int tune_epoch = -1;          // params epoch the shape was tuned for
-  int pool_chunk_min = 0;       // smallest pool chunk the scratch allows (points)
-  int pool_max_chunks = 0;      // pool partial slots per pair
   TuneChoice tc;
   std::string key;
 };
@@ -112,7 +107,6 @@ static void slot_free(BatchSlot& s) {
   if (s.d_mode) cudaFree(s.d_mode);
   if (s.h_mode) cudaFreeHost(s.h_mode);
   if (s.d_scan) cudaFree(s.d_scan);
-  if (s.d_pool) cudaFree(s.d_pool);
   if (s.h_err) cudaFreeHost(s.h_err);
   if (s.h_out) cudaFreeHost(s.h_out);
   if (s.h_stats) cudaFreeHost(s.h_stats);
@@ -161,10 +155,6 @@ static lsdg_status slot_alloc(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_err, sizeof(unsigned));
   if (e == cudaSuccess) *s.h_err = 0;
   if (e == cudaSuccess && !b->sim3) e = cudaMalloc(&s.d_u8, s.fs.pix_total);
-  if (e == cudaSuccess && !b->sim3) {
-    pool_sizes(s.fs.max_pix, &b->pool_chunk_min, &b->pool_max_chunks);
-    e = cudaMalloc(&s.d_pool, pool_ws_bytes(n, b->pool_max_chunks));
-  }
   if (e == cudaSuccess) e = cudaMalloc(&s.d_mode, sizeof(int));
   if (e == cudaSuccess) e = cudaMallocHost(&s.h_mode, 2 * sizeof(int));
   if (e == cudaSuccess) {
@@ -199,10 +189,6 @@ static TrackArgs slot_track_args(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s) {
   a.out_pose = s.d_out;
   a.out_stats = s.d_stats;
   a.out_sums = nullptr;
-  a.pool_ws = s.d_pool;
-  a.pool_chunk = b->pool_chunk_min;
-  a.pool_max_chunks = b->pool_max_chunks;
-  a.error_word = reinterpret_cast<unsigned*>(s.d_scan) + 1;
   return a;
 }
 
@@ -322,10 +308,8 @@ static lsdg_status slot_upload(lsdg_ctx* ctx, lsdg_batch* b, BatchSlot& s, cudaS
 // The step's one-launch build reports a band wait that ran out (its error word, copied back with
 // the results): the poses of that step are not to be trusted.
 static lsdg_status build_error(lsdg_ctx* ctx, const BatchSlot& s) {
-  if (s.h_err && (*s.h_err & 1u))
+  if (s.h_err && *s.h_err)
     return ctx_fail(ctx, LSDG_TIMEOUT, "keyframe build: a band's wait for the point counts of the bands before it ran out");
-  if (s.h_err && (*s.h_err & 2u))
-    return ctx_fail(ctx, LSDG_TIMEOUT, "tracker: a pool CTA's wait for an open chunk ran out");
   return LSDG_OK;
 }
 
@@ -642,15 +626,6 @@ lsdg_status lsdg_batch_split(lsdg_ctx* ctx, lsdg_batch* b, int* split, int* thre
   if (threads) *threads = b->tc.c_threads;
   if (minblocks) *minblocks = b->tc.c_minblocks;
   if (cluster) *cluster = b->tc.c_cluster;
-  return LSDG_OK;
-}
-
-lsdg_status lsdg_batch_pool_plan(lsdg_ctx* ctx, lsdg_batch* b, int* pool, int* threads, int* grid, int* chunk) {
-  if (!ctx || !b) return LSDG_INVALID_ARG;
-  if (pool) *pool = b->tc.pool;
-  if (threads) *threads = b->tc.pool_threads;
-  if (grid) *grid = b->tc.pool_grid;
-  if (chunk) *chunk = b->tc.pool_chunk;
   return LSDG_OK;
 }
 

@@ -21,10 +21,6 @@ struct TuneChoice {
   // with the shape above starting from the coarse poses; split = -1: one launch over all levels
   int split = -1;
   int c_threads = 256, c_minblocks = 2, c_cluster = 1, c_max_clusters = 1;
-  // pool plan (SE3 batches): one persistent grid of pool_grid CTAs over all levels, passes cut into
-  // chunks of pool_chunk points; when set it replaces the cluster plan above
-  int pool = 0;
-  int pool_threads = 256, pool_minblocks = 2, pool_grid = 0, pool_chunk = 0;
 };
 
 struct lsdg_ctx {

@@ -70,12 +70,6 @@ struct TrackArgs {
   float lambda0, lambda_up, lambda_down, step_eps, stall_eps;  // the LM schedule runs in float
   float min_good_ratio, min_usage;
   int accumulate_stats;      // continue the pass counts already in out_stats (second phase of a split run)
-  // pool plan (SE3 batches; see track.cu): a pair that finishes is done (no queue of pairs)
-  int pool;
-  void* pool_ws;             // PoolPair[n] | LMState[n] | PoolPartial[n][pool_max_chunks] | counters
-  int pool_chunk;            // points per work chunk (a multiple of the CTA's threads)
-  int pool_max_chunks;       // partial slots per pair
-  unsigned* error_word;      // OR-ed with 2 when a pool CTA's wait for work runs out (or nullptr)
 };
 
 // Kahan-compensated float sum (value = s - c) and the merge of two of them (an exact TwoSum of the

@@ -442,62 +442,50 @@ __device__ __noinline__ void finish_pair(const TrackArgs& a, LMState& lm) {
     for (int i = 0; i < Md::REC; ++i) a.out_sums[(size_t)Md::REC * p + i] = S[i];
 }
 
-// Sets up pair p's LM state from its initial pose and starts its first level with points
-// (publishing it in ctl); false when the pair has no level to run (its result is written).
-template <bool SIM3>
-__device__ __noinline__ bool begin_pair(const TrackArgs& a, LMState& lm, Ctl& ctl, int p) {
-  using Md = Mode<SIM3>;
-  lm.pair = p;
-  lm.have_final = 0;
-  lm.need_exp = 0;
-  lm.s_src = 1;
-  lm.it = 0;
-  lm.E_num = 0;
-  lm.E_den = 1;
-  lm.lambda = a.lambda0;
-  for (int i = 0; i < kMaxRec; ++i) lm.S[i] = 0;
-  for (int i = 0; i < kMaxSums; ++i) lm.Sf[i] = 0.f;
-  if (a.accumulate_stats) {
-    lm.st = a.out_stats[p];  // the coarse levels' pass counts, from the first phase
-  } else {
-    char* sp = reinterpret_cast<char*>(&lm.st);
-    for (int i = 0; i < (int)sizeof(lsdg_track_stats); ++i) sp[i] = 0;
-  }
-  const double* in = a.init + (size_t)Md::POSE * p;
-  double Tin[12];
-  if (SIM3) {  // {R, t, s} -> [sR | t]
-    for (int i = 0; i < 3; ++i) {
-      for (int j = 0; j < 3; ++j) Tin[4 * i + j] = in[12] * in[3 * i + j];
-      Tin[4 * i + 3] = in[9 + i];
-    }
-  } else {
-    for (int i = 0; i < 12; ++i) Tin[i] = in[i];
-  }
-  if (a.init_is_ref_to_frame) {
-    for (int i = 0; i < 12; ++i) lm.T[i] = Tin[i];
-  } else {
-    se3_inv_d(Tin, lm.T, SIM3);
-  }
-  if (start_level(a, lm, ctl, a.top_level)) return true;
-  finish_pair<SIM3>(a, lm);
-  return false;
-}
-
-// Takes pairs off the queue until one has a level to run; publishes it (or pair = -1).  In a pool
-// launch every pair is set up in advance and a finished pair takes no other: pair = -1.
+// Takes pairs off the queue until one has a level to run; publishes it (or pair = -1).
 template <bool SIM3>
 __device__ __noinline__ void fetch_pair(const TrackArgs& a, LMState& lm, Ctl& ctl) {
-  if (a.pool) {
-    ctl.pair = -1;
-    return;
-  }
+  using Md = Mode<SIM3>;
   for (;;) {
     const int k = atomicAdd(a.work_counter, 1);
     if (k >= a.n_pairs) {
       ctl.pair = -1;
       return;
     }
-    if (begin_pair<SIM3>(a, lm, ctl, a.order ? a.order[k] : k)) return;
+    const int p = a.order ? a.order[k] : k;
+    lm.pair = p;
+    lm.have_final = 0;
+    lm.need_exp = 0;
+    lm.s_src = 1;
+    lm.it = 0;
+    lm.E_num = 0;
+    lm.E_den = 1;
+    lm.lambda = a.lambda0;
+    for (int i = 0; i < kMaxRec; ++i) lm.S[i] = 0;
+    for (int i = 0; i < kMaxSums; ++i) lm.Sf[i] = 0.f;
+    if (a.accumulate_stats) {
+      lm.st = a.out_stats[p];  // the coarse levels' pass counts, from the first phase
+    } else {
+      char* sp = reinterpret_cast<char*>(&lm.st);
+      for (int i = 0; i < (int)sizeof(lsdg_track_stats); ++i) sp[i] = 0;
+    }
+    const double* in = a.init + (size_t)Md::POSE * p;
+    double Tin[12];
+    if (SIM3) {  // {R, t, s} -> [sR | t]
+      for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) Tin[4 * i + j] = in[12] * in[3 * i + j];
+        Tin[4 * i + 3] = in[9 + i];
+      }
+    } else {
+      for (int i = 0; i < 12; ++i) Tin[i] = in[i];
+    }
+    if (a.init_is_ref_to_frame) {
+      for (int i = 0; i < 12; ++i) lm.T[i] = Tin[i];
+    } else {
+      se3_inv_d(Tin, lm.T, SIM3);
+    }
+    if (start_level(a, lm, ctl, a.top_level)) return;
+    finish_pair<SIM3>(a, lm);
   }
 }
 
@@ -647,144 +635,6 @@ __device__ __forceinline__ void speculate(const TrackArgs& a, const LMState& lm,
 }
 
 // ------------------------------------------------------------------------------------------
-// The SE3 residual pass over a range of points (a3/a4): shared by the cluster kernel and the pool
-// kernel.  Points k, k + stride, ... below kend; two per iteration, each evaluated without branches
-// (a point that sits out gathers a clamped in-frame cell and gets zero weight), so both points' 32
-// gathers are in flight together and one add per sum takes both products.  The level's first pass
-// freezes 1/sigma^2 in psig, so later passes divide nothing; inliers take no square root.  A thread
-// sums a few dozen points per pass: the 21 Hessian sums (all terms of one sign on the diagonal, and
-// only the curvature of the step) are plain float sums there, the gradient and the energy (whose
-// terms cancel, and whose differences decide LM steps) stay compensated; every merge across
-// threads, warps and CTAs is compensated.
-// L2PSIG: psig is read through L2 (the pool kernel evaluates a point on different SMs in different
-// passes, and the L1 of one SM does not see another SM's writes).
-// ------------------------------------------------------------------------------------------
-struct Se3Pass {
-  const float4* __restrict__ pts;
-  const float* __restrict__ pvar;
-  float* __restrict__ psig;
-  const float* __restrict__ img;
-  int w;
-  float fx, fy, cx, cy, umax, vmax, ulo, vlo, uhi, vhi;
-  bool first;
-  float R00, R01, R02, R10, R11, R12, R20, R21, R22, t0, t1, t2;
-  float pvr, delta, minz;
-};
-
-template <bool L2PSIG>
-__device__ __forceinline__ void se3_point_loop(const Se3Pass& P, int k, const int n, const int stride, float (&hs)[21],
-                                               float (&gs)[6], float (&gc)[6], float& es, float& ec, int& good,
-                                               int& bad, int& oob) {
-  constexpr int D = 6;
-  const float4* __restrict__ pts = P.pts;
-  const float* __restrict__ pvar = P.pvar;
-  float* __restrict__ psig = P.psig;
-  const float* __restrict__ img = P.img;
-  const int w = P.w;
-  const float fx = P.fx, fy = P.fy, cx = P.cx, cy = P.cy;
-  const float umax = P.umax, vmax = P.vmax, ulo = P.ulo, vlo = P.vlo, uhi = P.uhi, vhi = P.vhi;
-  const bool first = P.first;
-  const float R00 = P.R00, R01 = P.R01, R02 = P.R02, R10 = P.R10, R11 = P.R11, R12 = P.R12;
-  const float R20 = P.R20, R21 = P.R21, R22 = P.R22, t0 = P.t0, t1 = P.t1, t2 = P.t2;
-  const float pvr = P.pvr, delta = P.delta, minz = P.minz;
-  const float d2 = delta * delta;
-  // a point's inputs: its float4 and frozen 1/sigma^2 (index 0 stands in past the end; the level's
-  // arrays are allocated for every pixel, so it is in bounds)
-  auto load = [&](int k, float4& p, float& sig) {
-    const int kk = k < n ? k : 0;
-    sig = first ? 1.f : (L2PSIG ? __ldcg(&psig[kk]) : psig[kk]);
-    p = __ldg(&pts[kk]);
-  };
-  auto eval = [&](int k, const float4 p, const float sig, float (&J)[D], float& wgt, float& res, float& rho) {
-    const bool in = k < n;
-    const int kk = in ? k : 0;
-    const bool act = in && sig > 0.f;
-    const float X = p.x, Y = p.y, Z = p.z, Ik = p.w;
-    const float Rpx = (R00 * X + R01 * Y) + R02 * Z;
-    const float Rpy = (R10 * X + R11 * Y) + R12 * Z;
-    const float Rpz = (R20 * X + R21 * Y) + R22 * Z;
-    const float Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
-    const bool zok = Zp > minz;
-    const float iz = __fdividef(1.0f, zok ? Zp : 1.f);  // ~1 ulp reciprocal
-    const float u = fx * (Xp * iz) + cx;
-    const float v = fy * (Yp * iz) + cy;
-    const bool bok = first ? (u >= ulo && v >= vlo && u < uhi && v < vhi)
-                           : (u >= 1.f && v >= 1.f && u < umax && v < vmax);
-    const bool ok = act && zok && bok;
-    if (act && !ok) {
-      ++oob;
-      if (first) psig[k] = 0.f;
-    }
-    const float uc = ok ? u : 1.f, vc = ok ? v : 1.f;
-    const int ix = (int)uc, iy = (int)vc;
-    const float ax = uc - (float)ix, ay = vc - (float)iy;
-    float wx[4], dxw[4], wy[4], dyw[4];
-    catmull_rom_fma(ax, wx, dxw);
-    catmull_rom_fma(ay, wy, dyw);
-    float rI[4], rD[4];
-    const float* q = img + (size_t)(iy - 1) * w + (ix - 1);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const float i0 = __ldg(q), i1 = __ldg(q + 1), i2 = __ldg(q + 2), i3 = __ldg(q + 3);
-      rI[j] = ((wx[0] * i0 + wx[1] * i1) + wx[2] * i2) + wx[3] * i3;
-      rD[j] = ((dxw[0] * i0 + dxw[1] * i1) + dxw[2] * i2) + dxw[3] * i3;
-      q += w;
-    }
-    const float In = ((wy[0] * rI[0] + wy[1] * rI[1]) + wy[2] * rI[2]) + wy[3] * rI[3];
-    const float Gx = ((wy[0] * rD[0] + wy[1] * rD[1]) + wy[2] * rD[2]) + wy[3] * rD[3];
-    const float Gy = ((dyw[0] * rI[0] + dyw[1] * rI[1]) + dyw[2] * rI[2]) + dyw[3] * rI[3];
-    const float r = In - Ik;
-    const float a0 = (Gx * fx) * iz, a1 = (Gy * fy) * iz;
-    const float a2 = -((a0 * Xp + a1 * Yp) * iz);
-    float isig = sig;
-    if (first) {
-      const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
-      isig = 1.0f / (pvr + (drd * drd) * __ldg(&pvar[kk]));
-      if (ok) psig[k] = isig;
-    }
-    const float e2 = (r * r) * isig;
-    const bool inl = e2 <= d2;
-    const float ir = rsqrtf(e2);
-    good += (ok && inl) ? 1 : 0;
-    bad += (ok && !inl) ? 1 : 0;
-    wgt = ok ? (inl ? isig : (delta * ir) * isig) : 0.f;
-    rho = ok ? (inl ? e2 : delta * (2.f * (e2 * ir) - delta)) : 0.f;
-    res = ok ? r : 0.f;
-    J[0] = ok ? a0 : 0.f;
-    J[1] = ok ? a1 : 0.f;
-    J[2] = ok ? a2 : 0.f;
-    J[3] = ok ? Yp * a2 - Zp * a1 : 0.f;
-    J[4] = ok ? Zp * a0 - Xp * a2 : 0.f;
-    J[5] = ok ? Xp * a1 - Yp * a0 : 0.f;
-  };
-  // the next iteration's two points are loaded while this one's are evaluated
-  float4 pa, pb;
-  float sa, sb;
-  load(k, pa, sa);
-  load(k + stride, pb, sb);
-  for (; k < n; k += 2 * stride) {
-    const float4 ca = pa, cb = pb;
-    const float csa = sa, csb = sb;
-    load(k + 2 * stride, pa, sa);
-    load(k + 3 * stride, pb, sb);
-    float Ja[D], Jb[D], wa, wb, ra, rb, ea, eb;
-    eval(k, ca, csa, Ja, wa, ra, ea);
-    eval(k + stride, cb, csb, Jb, wb, rb, eb);
-    float wJa[D], wJb[D];
-#pragma unroll
-    for (int i = 0; i < D; ++i) { wJa[i] = wa * Ja[i]; wJb[i] = wb * Jb[i]; }
-    int q2 = 0;
-#pragma unroll
-    for (int i = 0; i < D; ++i)
-#pragma unroll
-      for (int j = i; j < D; ++j) { hs[q2] = fmaf(wJb[i], Jb[j], fmaf(wJa[i], Ja[j], hs[q2])); ++q2; }
-#pragma unroll
-    for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJa[i] * ra + wJb[i] * rb);
-    kadd(es, ec, ea + eb);
-  }
-}
-
-// ------------------------------------------------------------------------------------------
 // The persistent cluster kernel
 // ------------------------------------------------------------------------------------------
 constexpr int kMaxCluster = 16;
@@ -890,17 +740,112 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
     for (int i = 0; i < D; ++i) { gs[i] = 0.f; gc[i] = 0.f; }
     int good = 0, bad = 0, oob = 0;
 
-    if constexpr (!SIM3) {
-      Se3Pass P;
-      P.pts = pts; P.pvar = pvar; P.psig = psig; P.img = img;
-      P.w = w; P.fx = fx; P.fy = fy; P.cx = cx; P.cy = cy;
-      P.umax = umax; P.vmax = vmax; P.ulo = ulo; P.vlo = vlo; P.uhi = uhi; P.vhi = vhi;
-      P.first = first;
-      P.R00 = R00; P.R01 = R01; P.R02 = R02; P.R10 = R10; P.R11 = R11; P.R12 = R12;
-      P.R20 = R20; P.R21 = R21; P.R22 = R22; P.t0 = t0; P.t1 = t1; P.t2 = t2;
-      P.pvr = pvr; P.delta = delta; P.minz = minz;
-      // the same thread evaluates a point in every pass of a level, so psig is read back by its writer
-      se3_point_loop<false>(P, (int)rank * NT + tid, n, (int)C * NT, hs, gs, gc, es, ec, good, bad, oob);
+    if (!SIM3) {
+      // SE3: two points per iteration, each evaluated without branches (a point that sits out gathers
+      // a clamped in-frame cell and gets zero weight), so both points' 32 gathers are in flight
+      // together and one add per sum takes both products.  The level's first pass freezes 1/sigma^2
+      // in psig, so later passes divide nothing; inliers take no square root.  A thread sums a few
+      // dozen points per pass: the 21 Hessian sums (all terms of one sign on the diagonal, and only
+      // the curvature of the step) are plain float sums there, the gradient and the energy (whose
+      // terms cancel, and whose differences decide LM steps) stay compensated; every merge across
+      // threads, warps and CTAs is compensated.
+      const int stride = (int)C * NT;
+      const float d2 = delta * delta;
+      // a point's inputs: its float4 and frozen 1/sigma^2 (index 0 stands in past the end; the level's
+      // arrays are allocated for every pixel, so it is in bounds)
+      auto load = [&](int k, float4& p, float& sig) {
+        const int kk = k < n ? k : 0;
+        sig = first ? 1.f : psig[kk];
+        p = __ldg(&pts[kk]);
+      };
+      auto eval = [&](int k, const float4 p, const float sig, float (&J)[D], float& wgt, float& res, float& rho) {
+        const bool in = k < n;
+        const int kk = in ? k : 0;
+        const bool act = in && sig > 0.f;
+        const float X = p.x, Y = p.y, Z = p.z, Ik = p.w;
+        const float Rpx = (R00 * X + R01 * Y) + R02 * Z;
+        const float Rpy = (R10 * X + R11 * Y) + R12 * Z;
+        const float Rpz = (R20 * X + R21 * Y) + R22 * Z;
+        const float Xp = Rpx + t0, Yp = Rpy + t1, Zp = Rpz + t2;
+        const bool zok = Zp > minz;
+        const float iz = __fdividef(1.0f, zok ? Zp : 1.f);  // ~1 ulp reciprocal
+        const float u = fx * (Xp * iz) + cx;
+        const float v = fy * (Yp * iz) + cy;
+        const bool bok = first ? (u >= ulo && v >= vlo && u < uhi && v < vhi)
+                               : (u >= 1.f && v >= 1.f && u < umax && v < vmax);
+        const bool ok = act && zok && bok;
+        if (act && !ok) {
+          ++oob;
+          if (first) psig[k] = 0.f;
+        }
+        const float uc = ok ? u : 1.f, vc = ok ? v : 1.f;
+        const int ix = (int)uc, iy = (int)vc;
+        const float ax = uc - (float)ix, ay = vc - (float)iy;
+        float wx[4], dxw[4], wy[4], dyw[4];
+        catmull_rom_fma(ax, wx, dxw);
+        catmull_rom_fma(ay, wy, dyw);
+        float rI[4], rD[4];
+        const float* q = img + (size_t)(iy - 1) * w + (ix - 1);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float i0 = __ldg(q), i1 = __ldg(q + 1), i2 = __ldg(q + 2), i3 = __ldg(q + 3);
+          rI[j] = ((wx[0] * i0 + wx[1] * i1) + wx[2] * i2) + wx[3] * i3;
+          rD[j] = ((dxw[0] * i0 + dxw[1] * i1) + dxw[2] * i2) + dxw[3] * i3;
+          q += w;
+        }
+        const float In = ((wy[0] * rI[0] + wy[1] * rI[1]) + wy[2] * rI[2]) + wy[3] * rI[3];
+        const float Gx = ((wy[0] * rD[0] + wy[1] * rD[1]) + wy[2] * rD[2]) + wy[3] * rD[3];
+        const float Gy = ((dyw[0] * rI[0] + dyw[1] * rI[1]) + dyw[2] * rI[2]) + dyw[3] * rI[3];
+        const float r = In - Ik;
+        const float a0 = (Gx * fx) * iz, a1 = (Gy * fy) * iz;
+        const float a2 = -((a0 * Xp + a1 * Yp) * iz);
+        float isig = sig;
+        if (first) {
+          const float drd = -(((a0 * Rpx + a1 * Rpy) + a2 * Rpz) * Z);
+          isig = 1.0f / (pvr + (drd * drd) * __ldg(&pvar[kk]));
+          if (ok) psig[k] = isig;
+        }
+        const float e2 = (r * r) * isig;
+        const bool inl = e2 <= d2;
+        const float ir = rsqrtf(e2);
+        good += (ok && inl) ? 1 : 0;
+        bad += (ok && !inl) ? 1 : 0;
+        wgt = ok ? (inl ? isig : (delta * ir) * isig) : 0.f;
+        rho = ok ? (inl ? e2 : delta * (2.f * (e2 * ir) - delta)) : 0.f;
+        res = ok ? r : 0.f;
+        J[0] = ok ? a0 : 0.f;
+        J[1] = ok ? a1 : 0.f;
+        J[2] = ok ? a2 : 0.f;
+        J[3] = ok ? Yp * a2 - Zp * a1 : 0.f;
+        J[4] = ok ? Zp * a0 - Xp * a2 : 0.f;
+        J[5] = ok ? Xp * a1 - Yp * a0 : 0.f;
+      };
+      // the next iteration's two points are loaded while this one's are evaluated
+      int k = (int)rank * NT + tid;
+      float4 pa, pb;
+      float sa, sb;
+      load(k, pa, sa);
+      load(k + stride, pb, sb);
+      for (; k < n; k += 2 * stride) {
+        const float4 ca = pa, cb = pb;
+        const float csa = sa, csb = sb;
+        load(k + 2 * stride, pa, sa);
+        load(k + 3 * stride, pb, sb);
+        float Ja[D], Jb[D], wa, wb, ra, rb, ea, eb;
+        eval(k, ca, csa, Ja, wa, ra, ea);
+        eval(k + stride, cb, csb, Jb, wb, rb, eb);
+        float wJa[D], wJb[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) { wJa[i] = wa * Ja[i]; wJb[i] = wb * Jb[i]; }
+        int q2 = 0;
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+          for (int j = i; j < D; ++j) { hs[q2] = fmaf(wJb[i], Jb[j], fmaf(wJa[i], Ja[j], hs[q2])); ++q2; }
+#pragma unroll
+        for (int i = 0; i < D; ++i) kadd(gs[i], gc[i], wJa[i] * ra + wJb[i] * rb);
+        kadd(es, ec, ea + eb);
+      }
     }
     if (SIM3)
     for (int k = (int)rank * NT + tid; k < n; k += (int)C * NT) {
@@ -1157,332 +1102,6 @@ __global__ void __launch_bounds__(NT, MINB) track_kernel(const TrackArgs a) {
 }
 
 // ------------------------------------------------------------------------------------------
-// The pool kernel (SE3 batches)
-// ------------------------------------------------------------------------------------------
-// The cluster kernel binds a pair to a cluster for all its passes, so the pair's per-pass latency
-// chain (point work -> merges -> cluster barrier -> LM step on one warp -> barrier) idles its SMs
-// at every coarse level and at every LM step, and a batch with more pairs than resident clusters
-// ends with idle SMs.  The pool kernel decouples pairs from SMs: a pass of a pair is cut into
-// chunks of `pool_chunk` consecutive points, and every CTA of a persistent grid repeatedly claims
-// a chunk of whichever pair has one open, evaluates it, and stores its compensated partial sums in
-// the pair's slot for that chunk.  The CTA that completes a pass's last chunk merges the partials
-// in chunk order (so the result does not depend on which CTA took which chunk), runs the LM step
-// with the same warp code as the cluster kernel, and opens the pair's next pass; meanwhile every
-// other CTA works on other pairs' chunks, so LM steps and coarse levels overlap with level-0 work.
-// Claim priority: chunks of coarse levels (the latency-bound part of a pair's chain) first, then
-// level-0 chunks of the lowest pair index (a bounded working set in L2).
-//
-// Per pair a 64-bit claim word: high half = pass sequence << 13 | level << 10 | chunks of the pass
-// (0xffffffff once the pair is done), low half = next chunk.  A CTA claims by atomicAdd on the low
-// half; the finisher publishes the next pass with its pose written first (fence, then atomicExch
-// of the word).  Waits for an open chunk are bounded: a CTA whose wait runs out sets bit 2 of the
-// error word (the batch then reports LSDG_TIMEOUT) and leaves.  No CTA ever waits for a particular
-// other CTA, so the plan needs no co-residency.
-struct PoolPair {
-  unsigned long long claim;
-  int done;  // chunks of the current pass completed
-  int pad;
-  Ctl ctl[2];  // the pose of pass seq lives in ctl[seq & 1]
-};
-
-struct PoolPartial {
-  float s[28];
-  float c[28];
-  int cnt[4];
-};
-
-constexpr unsigned kPoolDone = 0xffffffffu;
-constexpr int kPoolMaxChunks = 1023;
-constexpr long kPoolPolls = 1L << 22;
-
-struct PoolLayout {
-  PoolPair* pairs;
-  LMState* lm;
-  PoolPartial* part;
-  int* counters;  // [0] pairs finished
-};
-
-__host__ __device__ inline size_t pool_align(size_t x) { return (x + 255) & ~(size_t)255; }
-
-__host__ __device__ inline PoolLayout pool_layout(void* ws, int n, int max_chunks) {
-  char* b = static_cast<char*>(ws);
-  PoolLayout L;
-  L.pairs = reinterpret_cast<PoolPair*>(b);
-  b += pool_align(sizeof(PoolPair) * (size_t)n);
-  L.lm = reinterpret_cast<LMState*>(b);
-  b += pool_align(sizeof(LMState) * (size_t)n);
-  L.part = reinterpret_cast<PoolPartial*>(b);
-  b += pool_align(sizeof(PoolPartial) * (size_t)n * max_chunks);
-  L.counters = reinterpret_cast<int*>(b);
-  return L;
-}
-
-// The smallest chunk a frame of max_pix pixels allows (every level's chunk count fits the claim
-// word's 10 bits; a multiple of 512 so that every pool shape's threads divide it) and the partial
-// slots per pair it needs.
-void pool_sizes(long max_pix, int* chunk_min, int* max_chunks) {
-  long c = (max_pix + kPoolMaxChunks - 1) / kPoolMaxChunks;
-  c = (c + 511) / 512 * 512;
-  if (c < 1024) c = 1024;
-  *chunk_min = (int)c;
-  *max_chunks = (int)((max_pix + c - 1) / c);
-}
-
-size_t pool_ws_bytes(int n_pairs, int max_chunks) {
-  return pool_align(sizeof(PoolPair) * (size_t)n_pairs) + pool_align(sizeof(LMState) * (size_t)n_pairs) +
-         pool_align(sizeof(PoolPartial) * (size_t)n_pairs * max_chunks) + 256;
-}
-
-__device__ __forceinline__ unsigned pool_hi(unsigned seq, int level, int nch) {
-  return (seq << 13) | ((unsigned)level << 10) | (unsigned)nch;
-}
-
-__device__ __forceinline__ int pool_chunks(const TrackArgs& a, int p, int level) {
-  const int n = a.pairs[p].ref->pcount[level];
-  return (n + a.pool_chunk - 1) / a.pool_chunk;
-}
-
-// One thread per pair: LM state, first pass and claim word (or the result of a pair with nothing
-// to track).  The counters were zeroed before the launch.
-__global__ void pool_init_kernel(const TrackArgs a) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= a.n_pairs) return;
-  const PoolLayout L = pool_layout(a.pool_ws, a.n_pairs, a.pool_max_chunks);
-  PoolPair& pp = L.pairs[p];
-  Ctl ctl;
-  if (begin_pair<false>(a, L.lm[p], ctl, p)) {
-    pp.ctl[0] = ctl;
-    pp.done = 0;
-    pp.claim = (unsigned long long)pool_hi(0u, ctl.level, pool_chunks(a, p, ctl.level)) << 32;
-  } else {
-    pp.claim = (unsigned long long)kPoolDone << 32;
-    atomicAdd(&L.counters[0], 1);
-  }
-}
-
-// Warp 0: claims an open chunk (true), or finds every pair done / its wait run out (false).
-__device__ __forceinline__ bool pool_claim(const TrackArgs& a, const PoolLayout& L, int lane, int& pair, int& chunk,
-                                           unsigned& hi) {
-  const int n = a.n_pairs;
-  for (long poll = 0; poll < kPoolPolls; ++poll) {
-    if (*reinterpret_cast<volatile int*>(&L.counters[0]) >= n) return false;
-    unsigned best = 0xffffffffu;
-    for (int q = lane; q < n; q += 32) {
-      const unsigned long long w = __ldcg(&L.pairs[q].claim);
-      const unsigned h = (unsigned)(w >> 32), c = (unsigned)w;
-      if (h == kPoolDone || c >= (h & 1023u)) continue;
-      const unsigned key = (((h >> 10) & 7u) == 0u ? (1u << 24) : 0u) | (unsigned)q;
-      best = best < key ? best : key;
-    }
-    best = __reduce_min_sync(0xffffffffu, best);
-    if (best == 0xffffffffu) {
-      __nanosleep(256);
-      continue;
-    }
-    const int q = (int)(best & 0xffffffu);
-    unsigned long long old = 0;
-    if (lane == 0) old = atomicAdd(&L.pairs[q].claim, 1ull);
-    old = __shfl_sync(0xffffffffu, old, 0);
-    const unsigned h = (unsigned)(old >> 32), c = (unsigned)old;
-    if (h != kPoolDone && c < (h & 1023u)) {
-      __threadfence();  // the pass's pose was published before the word: read it after the claim
-      pair = q;
-      chunk = (int)c;
-      hi = h;
-      return true;
-    }
-  }
-  if (lane == 0 && a.error_word) atomicOr(a.error_word, 2u);
-  return false;
-}
-
-template <int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) pool_kernel(const TrackArgs a) {
-  using Md = Mode<false>;
-  constexpr int NW = NT / 32;
-  constexpr int NS = Md::NS, NH = Md::NH, D = Md::DOF;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  const PoolLayout L = pool_layout(a.pool_ws, a.n_pairs, a.pool_max_chunks);
-
-  __shared__ float ws[NW][NS];
-  __shared__ float wc[NW][NS];
-  __shared__ int wn[NW][3];
-  __shared__ Ctl ctl;
-  __shared__ double tot[kMaxRec];
-  __shared__ float totf[kMaxSums];
-  __shared__ LMState lm;
-  __shared__ SolveCache sc;
-  __shared__ int s_pair, s_chunk, s_go, s_last;
-  __shared__ unsigned s_hi;
-
-  for (;;) {
-    if (wid == 0) {
-      int p = -1, c = 0;
-      unsigned h = 0;
-      const bool got = pool_claim(a, L, lane, p, c, h);
-      if (lane == 0) {
-        s_go = got ? 1 : 0;
-        s_pair = p;
-        s_chunk = c;
-        s_hi = h;
-      }
-    }
-    __syncthreads();
-    if (!s_go) break;
-    const int pair = s_pair, chunk = s_chunk;
-    const unsigned hi = s_hi;
-    const unsigned seq = hi >> 13;
-    const int nch = (int)(hi & 1023u);
-    PoolPair* pp = &L.pairs[pair];
-    if (tid < (int)(sizeof(Ctl) / 4))
-      reinterpret_cast<int*>(&ctl)[tid] = __ldcg(reinterpret_cast<const int*>(&pp->ctl[seq & 1u]) + tid);
-    __syncthreads();
-    const int level = ctl.level;
-    const PairDev pd = a.pairs[pair];
-    const FrameDev* __restrict__ R = pd.ref;
-    const FrameDev* __restrict__ Fc = pd.cur;
-    const int n = R->pcount[level];
-    const int w = Fc->w >> level, h = Fc->h >> level;
-    Se3Pass P;
-    P.pts = R->pxyzi[level];
-    P.pvar = R->pvar[level];
-    P.psig = R->psig[level];
-    P.img = Fc->plane[level];
-    P.w = w;
-    P.fx = Fc->fx[level]; P.fy = Fc->fy[level]; P.cx = Fc->cx[level]; P.cy = Fc->cy[level];
-    P.umax = (float)(w - 2); P.vmax = (float)(h - 2);
-    P.ulo = a.border_margin; P.vlo = a.border_margin;
-    P.uhi = (float)(w - 1) - a.border_margin; P.vhi = (float)(h - 1) - a.border_margin;
-    P.first = ctl.first != 0;
-    P.R00 = ctl.R[0]; P.R01 = ctl.R[1]; P.R02 = ctl.R[2];
-    P.R10 = ctl.R[3]; P.R11 = ctl.R[4]; P.R12 = ctl.R[5];
-    P.R20 = ctl.R[6]; P.R21 = ctl.R[7]; P.R22 = ctl.R[8];
-    P.t0 = ctl.t[0]; P.t1 = ctl.t[1]; P.t2 = ctl.t[2];
-    P.pvr = a.photometric_variance; P.delta = a.huber_delta; P.minz = a.min_z;
-
-    float hs[NH], gs[D], gc[D], es = 0.f, ec = 0.f;
-#pragma unroll
-    for (int i = 0; i < NH; ++i) hs[i] = 0.f;
-#pragma unroll
-    for (int i = 0; i < D; ++i) { gs[i] = 0.f; gc[i] = 0.f; }
-    int good = 0, bad = 0, oob = 0;
-    const int k0 = chunk * a.pool_chunk;
-    const int kend = min(n, k0 + a.pool_chunk);
-    se3_point_loop<true>(P, k0 + tid, kend, NT, hs, gs, gc, es, ec, good, bad, oob);
-
-    // warp merge by reduce-scatter (lane l ends with sum l), then the warps in fixed order
-    {
-      float S[32], Cc[32];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        float sv = 0.f, cv = 0.f;
-        if (i < NH) sv = hs[i];
-        else if (i < NH + D) { sv = gs[i - NH]; cv = gc[i - NH]; }
-        else if (i == NH + D) { sv = es; cv = ec; }
-        S[i] = sv;
-        Cc[i] = cv;
-      }
-      warp_reduce_scatter(S, Cc, lane);
-      good = __reduce_add_sync(0xffffffffu, good);
-      bad = __reduce_add_sync(0xffffffffu, bad);
-      oob = __reduce_add_sync(0xffffffffu, oob);
-      if (lane < NS) {
-        ws[wid][lane] = S[0];
-        wc[wid][lane] = Cc[0];
-      }
-      if (lane == 31) {
-        wn[wid][0] = good;
-        wn[wid][1] = bad;
-        wn[wid][2] = oob;
-      }
-    }
-    __syncthreads();
-    PoolPartial* part = L.part + (size_t)pair * a.pool_max_chunks;
-    if (tid < NS) {
-      float s = 0.f, c = 0.f;
-      for (int k = 0; k < NW; ++k) kmerge(s, c, ws[k][tid], wc[k][tid]);
-      __stcg(&part[chunk].s[tid], s);
-      __stcg(&part[chunk].c[tid], c);
-    } else if (tid < NS + 3) {
-      int v = 0;
-      for (int k = 0; k < NW; ++k) v += wn[k][tid - NS];
-      __stcg(&part[chunk].cnt[tid - NS], v);
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&pp->done, 1) == nch - 1 ? 1 : 0;
-    __syncthreads();
-    if (!s_last) continue;
-
-    // this CTA completed the pass: merge the chunks in order, run the LM step, open the next pass
-    __threadfence();
-    if (tid < NS) {
-      float s = 0.f, c = 0.f;
-      for (int k = 0; k < nch; ++k) kmerge(s, c, __ldcg(&part[k].s[tid]), __ldcg(&part[k].c[tid]));
-      tot[tid] = (double)s - (double)c;
-      totf[tid] = s - c;
-    } else if (tid < NS + 3) {
-      int v = 0;
-      for (int k = 0; k < nch; ++k) v += __ldcg(&part[k].cnt[tid - NS]);
-      tot[tid + 1] = (double)v;  // NS+1 inliers, NS+2 outliers, NS+3 left the image
-    }
-    {
-      const int* src = reinterpret_cast<const int*>(&L.lm[pair]);
-      int* dst = reinterpret_cast<int*>(&lm);
-      for (int i = tid; i < (int)(sizeof(LMState) / 4); i += NT) dst[i] = __ldcg(src + i);
-    }
-    __syncthreads();
-    if (wid == 0) {
-      if (lane == 0) tot[NS] = tot[NS + 1] + tot[NS + 2];
-      __syncwarp();
-      speculate<false>(a, lm, tot, totf, sc, lane);
-      __syncwarp();
-      int act = 0;
-      if (lane == 0) act = lm_decide<false>(a, lm, tot);
-      act = __shfl_sync(0xffffffffu, act, 0);
-      __syncwarp();
-      lm_copy<false>(lm, tot, totf, act, lane);
-      __syncwarp();
-      if (lane == 0) lm_continue<false>(a, lm, ctl, sc, act);
-      __syncwarp();
-      if (lm.need_exp) {
-        warp_exp_mul_se3f(lm.dx, lm.T, lm.Ttry, lane);
-        __syncwarp();
-        if (lane < 12) {  // publish the trial pose as float, one element per lane
-          const float f = (float)lm.Ttry[lane];
-          if ((lane & 3) == 3) ctl.t[lane >> 2] = f;
-          else ctl.R[3 * (lane >> 2) + (lane & 3)] = f;
-        }
-        __syncwarp();
-        if (lane == 0) lm.need_exp = 0;
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    {
-      const int* src = reinterpret_cast<const int*>(&lm);
-      int* dst = reinterpret_cast<int*>(&L.lm[pair]);
-      for (int i = tid; i < (int)(sizeof(LMState) / 4); i += NT) __stcg(dst + i, src[i]);
-      if (ctl.pair >= 0 && tid < (int)(sizeof(Ctl) / 4))
-        __stcg(reinterpret_cast<int*>(&pp->ctl[(seq + 1u) & 1u]) + tid, reinterpret_cast<const int*>(&ctl)[tid]);
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) {
-      pp->done = 0;
-      __threadfence();
-      if (ctl.pair >= 0) {
-        atomicExch(&pp->claim, (unsigned long long)pool_hi(seq + 1u, ctl.level, pool_chunks(a, pair, ctl.level)) << 32);
-      } else {
-        atomicExch(&pp->claim, (unsigned long long)kPoolDone << 32);
-        atomicAdd(&L.counters[0], 1);
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// ------------------------------------------------------------------------------------------
 // Host side: launch with a cluster shape.  Shapes are (threads per CTA, CTAs the register budget
 // must leave room for on one SM); the autotuner picks one together with the cluster size.
 // ------------------------------------------------------------------------------------------
@@ -1579,61 +1198,6 @@ int track_max_clusters(int threads, int minblocks, int cluster, bool sim3) {
   LSDG_TRACK_SHAPES(X)
 #undef X
   return 0;
-}
-
-// Pool plan launchers: (threads, CTAs the register budget leaves room for on one SM).
-#define LSDG_POOL_SHAPES(X) X(256, 2) X(512, 1) X(128, 4)
-
-template <int NT, int MINB>
-static cudaError_t launch_pool_nt(const TrackArgs& a, int grid, cudaStream_t s) {
-  pool_init_kernel<<<(a.n_pairs + 127) / 128, 128, 0, s>>>(a);
-  pool_kernel<NT, MINB><<<grid, NT, 0, s>>>(a);
-  return cudaGetLastError();
-}
-
-int pool_shape_count() {
-  int n = 0;
-#define X(nt, mb) ++n;
-  LSDG_POOL_SHAPES(X)
-#undef X
-  return n;
-}
-
-void pool_shape(int i, int* threads, int* minblocks) {
-  int k = 0;
-#define X(nt, mb)       \
-  if (k++ == i) {       \
-    *threads = nt;      \
-    *minblocks = mb;    \
-  }
-  LSDG_POOL_SHAPES(X)
-#undef X
-}
-
-// Resident CTAs of a pool shape per SM (0 if it does not fit).
-int pool_blocks_per_sm(int threads, int minblocks) {
-  int n = 0;
-#define X(nt, mb)                                                                                     \
-  if (threads == nt && minblocks == mb &&                                                           \
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pool_kernel<nt, mb>, nt, 0) != cudaSuccess) { \
-    cudaGetLastError();                                                                             \
-    n = 0;                                                                                          \
-  }
-  LSDG_POOL_SHAPES(X)
-#undef X
-  return n;
-}
-
-// The two launches of a pool run (pair set-up, then the persistent grid), after zeroing the counters.
-cudaError_t launch_pool(const TrackArgs& a, int threads, int minblocks, int grid, cudaStream_t s) {
-  const PoolLayout L = pool_layout(a.pool_ws, a.n_pairs, a.pool_max_chunks);
-  cudaError_t e = cudaMemsetAsync(L.counters, 0, 256, s);
-  if (e != cudaSuccess) return e;
-#define X(nt, mb) \
-  if (threads == nt && minblocks == mb) return launch_pool_nt<nt, mb>(a, grid, s);
-  LSDG_POOL_SHAPES(X)
-#undef X
-  return cudaErrorInvalidValue;
 }
 
 }  // namespace lsdg

@@ -87,7 +87,6 @@ def lib():
     _sig(L, "lsdg_batch_timing", st, [_vp, _vp, C.POINTER(C.c_float), C.POINTER(C.c_float)])
     _sig(L, "lsdg_batch_shape", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 5)
     _sig(L, "lsdg_batch_split", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 4)
-    _sig(L, "lsdg_batch_pool_plan", st, [_vp, _vp] + [C.POINTER(C.c_int)] * 4)
     _sig(L, "lsdg_batch_test_withhold", st, [_vp, _vp, C.c_int])
     _sig(L, "lsdg_batch_get_points", st, [_vp, _vp, C.c_int, C.c_int, _f32p, _f32p, C.c_int, C.POINTER(C.c_int)])
     _sig(L, "lsdg_batch_work", st, [_vp, _vp, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_double)])
@@ -461,12 +460,6 @@ class Batch:
         if sp.value >= 0:
             out["coarse_phase"] = {"levels_from": sp.value, "threads": ct.value, "minblocks": cm.value,
                                    "cluster": cc.value}
-        pl, pt, pg, pc = C.c_int(), C.c_int(), C.c_int(), C.c_int()
-        self.ctx.check(lib().lsdg_batch_pool_plan(self.ctx.handle, self._h, C.byref(pl), C.byref(pt), C.byref(pg),
-                                                  C.byref(pc)))
-        if pl.value:
-            out = {"plan": "pool", "threads": pt.value, "grid": pg.value, "chunk_points": pc.value,
-                   "launches_per_run": k.value}
         return out
 
     def test_withhold(self, frame: int):
