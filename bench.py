@@ -137,6 +137,25 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def measured_l2_copy_gbps(reps: int = 200):
+    """Copy bandwidth of an L2-resident working set on this GPU (torch copy of 24 MB into 24 MB,
+    both inside the 126 MB L2; read + write bytes), the denominator of the L2-side roofline."""
+    import torch
+    n = 24 * 1024 * 1024 // 4
+    a = torch.ones(n, device="cuda")
+    b = torch.empty(n, device="cuda")
+    for _ in range(10):
+        b.copy_(a)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record()
+    e1.synchronize()
+    return 2 * 4 * n * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+
+
 def profiled_traffic(workload_key: str):
     """dram bytes per launch of the tracker kernel from a committed ncu summary, if present."""
     d = os.path.join(ROOT, "profiles")
@@ -342,6 +361,7 @@ def run_ours(args, rank, world, local_rank):
     peak, peak_kind = measured_peak_hbm()
     achieved = pass_bytes / (track_ms / 1e3) / 1e9
     traffic = profiled_traffic("64x640x480")
+    l2_peak = measured_l2_copy_gbps()
 
     # accuracy vs ground truth (the synthetic motion)
     errs = [synth.pose_error(out_e[i], pairs[i].frame_to_ref) for i in range(N_PAIRS)]
@@ -429,6 +449,11 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": "track_kernel",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 16-pair capture of the "
+                                       "pinned 512-thread split plan (profiles/track_kernel_64x640x480.md), scaled "
+                                       "by 64/16 pairs; not measured in this run",
+                     "l2": {"achieved": achieved, "peak": l2_peak, "unit": "GB/s", "frac": achieved / l2_peak,
+                            "peak_how": "torch copy of a 24 MB L2-resident buffer, read + write bytes, this run"},
                      "note": "achieved = algorithmic bytes of all LM residual passes (point float4 + frozen "
                              "variance 20 B, intensity plane 4 B/px, sums; per pass) / tracker kernel time; "
                              "re-reads across passes are L2 "
@@ -517,6 +542,17 @@ def bench_depth(ctx, stream, seq, args):
             prop.append((time.perf_counter() - t0) * 1e3)
     good = (st["validity"] > 0) & (st["var"] < 0.01)
     rel = np.abs(st["idepth"][good] - seq.key_true_idepth[good]) / seq.key_true_idepth[good]
+    # the pixels that search: inside the 3-pixel border with a central-difference gradient of at
+    # least min_grad (the kernels' own test, restated in float32)
+    K = np.asarray(seq.key_image, np.float32)
+    gx = np.zeros_like(K)
+    gy = np.zeros_like(K)
+    gx[:, 1:-1] = (K[:, 2:] - K[:, :-2]) * np.float32(0.5)
+    gy[1:-1, :] = (K[2:, :] - K[:-2, :]) * np.float32(0.5)
+    mg = np.float32(lsdg.default_params().min_grad)
+    inside = np.zeros_like(K, bool)
+    inside[3:-3, 3:-3] = True
+    searched = int((inside & ((gx * gx + gy * gy) >= mg * mg)).sum())
     # the viewer's point cloud of the new keyframe (Keyframe::computeVbo), into a device buffer
     vbuf = torch.empty(seq.w * seq.h * 4, dtype=torch.float32, device="cuda")
     cl = []
@@ -529,8 +565,19 @@ def bench_depth(ctx, stream, seq, args):
         if it >= max(3, args.warmup):
             cl.append(c0.elapsed_time(c1))
     dm.close()
+    n_px, n_refs = seq.w * seq.h, len(seq.ref_images)
+    ms_dev = statistics.median(dev)
+    alg = n_px * (24 + 24 + 12 + 4 * n_refs)
+    peak, peak_kind = measured_peak_hbm()
     return {"workload": "updateKeyframe: 1 keyframe 640x480, 8 references on a 10 cm arc, observe + regularize",
-            "ms_device": statistics.median(dev), "ms_e2e": statistics.median(e2e),
+            "ms_device": ms_dev, "ms_e2e": statistics.median(e2e),
+            "roofline": {"bound": "hbm", "algorithmic_bytes": alg, "achieved": alg / (ms_dev / 1e3) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg / (ms_dev / 1e3) / 1e9 / peak,
+                         "bytes_per_pixel": "24 B state read + 24 B state written + 12 B keyframe {I, gx, gy} + "
+                                            "4 B per reference (%d references)" % n_refs,
+                         "peak_kind": peak_kind},
+            "pixels_searched": searched,
+            "pixel_reference_searches_per_s": searched * n_refs / (ms_dev / 1e3),
             "e2e_api": "lsdg_depth_update_u8 (8 x 8-bit 640x480 references from pinned memory) + lsdg_depth_get "
                        "of the two planes publishKeyframe copies",
             "ms_e2e_float_full_state": statistics.median(e2e_full),

@@ -241,18 +241,42 @@ __device__ void observe_one(const ObserveArgs& A, const RefGeomF& G, const float
   val = val + 1 < A.validity_max ? val + 1 : A.validity_max;
 }
 
-__global__ void __launch_bounds__(256) depth_observe_kernel(const ObserveArgs A) {
-  const int x = blockIdx.x * 32 + (threadIdx.x & 31);
-  const int y = blockIdx.y * 8 + (threadIdx.x >> 5);
-  const int w = A.w, h = A.h;
-  if (x < 3 || y < 3 || x > w - 4 || y > h - 4) return;
-  const size_t i = (size_t)y * w + x;
+// Work list of the observe step: the keyframe pixels a reference can change (inside the 3-pixel
+// border, gradient magnitude at least min_grad; the same test, in the same float operations, that
+// observe_pixel_all repeats).  A warp appends its pixels with one atomic, so the list's order
+// varies from run to run; that is immaterial, every pixel's state depends on that pixel alone.
+// counters[0] receives the list length (zeroed before the launch).
+__global__ void __launch_bounds__(256) depth_worklist_kernel(const float4* __restrict__ key, int w, int h,
+                                                             float min_grad, int* __restrict__ list,
+                                                             int* __restrict__ counters) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  bool ok = false;
+  if (i < w * h) {
+    const int y = i / w, x = i - y * w;
+    if (!(x < 3 || y < 3 || x > w - 4 || y > h - 4)) {
+      const float4 kp = __ldg(&key[i]);
+      const float g2 = kp.y * kp.y + kp.z * kp.z;
+      ok = g2 >= min_grad * min_grad;
+    }
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, ok);
+  int base = 0;
+  if (lane == 0 && m) base = atomicAdd(&counters[0], __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (ok) list[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// observeDepth of keyframe pixel i against every reference in order (its state in registers).
+__device__ __forceinline__ void observe_pixel_all(const ObserveArgs& A, int i) {
+  const int w = A.w;
+  const int y = i / w, x = i - y * w;
   const float4 kp = __ldg(&A.key[i]);
   const float g2 = kp.y * kp.y + kp.z * kp.z;
   if (!(g2 >= A.min_grad * A.min_grad)) return;  // no reference can change this pixel
   float d = A.st.d[i], var = A.st.v[i];
   int val = A.st.val[i], bl = A.st.bl[i];
-  const size_t plane = (size_t)w * h;
+  const size_t plane = (size_t)w * A.h;
   for (int r = 0; r < A.n_refs; ++r) {
     if (bl >= A.blacklist_limit) break;
     observe_one(A, A.geom[r], A.refs + plane * r, x, y, kp.y, kp.z, d, var, val, bl);
@@ -261,6 +285,24 @@ __global__ void __launch_bounds__(256) depth_observe_kernel(const ObserveArgs A)
   A.st.v[i] = var;
   A.st.val[i] = val;
   A.st.bl[i] = bl;
+}
+
+// A persistent grid over the work list: each warp takes the next 32 listed pixels (one atomic),
+// so every lane holds a pixel that searches and warps that draw short epipolar segments come back
+// for more.  counters[0] = list length, counters[1] = next list entry (zeroed before the list
+// kernel).
+__global__ void __launch_bounds__(128) depth_observe_kernel(const ObserveArgs A, const int* __restrict__ list,
+                                                            int* __restrict__ counters) {
+  const int lane = threadIdx.x & 31;
+  const int n = *reinterpret_cast<volatile const int*>(&counters[0]);
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&counters[1], 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const int t = base + lane;
+    if (t < n) observe_pixel_all(A, __ldg(&list[t]));
+  }
 }
 
 struct RegArgs {
@@ -461,6 +503,8 @@ struct lsdg_depthmap {
   float* refs = nullptr;
   uint8_t* refs_u8 = nullptr;  // staging of 8-bit reference frames (lsdg_depth_update_u8)
   unsigned long long* keys = nullptr;
+  int* work = nullptr;      // observe work list: the keyframe pixels that search (one per pixel at most)
+  int* counters = nullptr;  // [0] work list length, [1] next entry
   bool has_key = false;
 };
 
@@ -536,7 +580,7 @@ lsdg_status lsdg_depth_create(lsdg_ctx* ctx, int width, int height, const lsdg_i
     return st;
   }
   const size_t n = (size_t)width * height;
-  const size_t bytes = 2 * 6 * n * 4 + (size_t)LSDG_MAX_REFS * n * 5 + n * 8 + 2048;
+  const size_t bytes = 2 * 6 * n * 4 + (size_t)LSDG_MAX_REFS * n * 5 + n * 8 + n * 4 + 4096;
   cudaError_t e = cudaMalloc(&dm->arena, bytes);
   if (e != cudaSuccess) {
     depth_free(dm);
@@ -552,6 +596,11 @@ lsdg_status lsdg_depth_create(lsdg_ctx* ctx, int width, int height, const lsdg_i
   p += (size_t)LSDG_MAX_REFS * n;
   p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
   dm->keys = (unsigned long long*)p;
+  p += n * 8;
+  dm->work = (int*)p;
+  p += n * 4;
+  p = (char*)(((uintptr_t)p + 255) & ~(uintptr_t)255);
+  dm->counters = (int*)p;
   *out = dm;
   return LSDG_OK;
 }
@@ -624,8 +673,23 @@ lsdg_status lsdg_depth_update_loaded(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_ref
   A.validity_max = p.validity_max;
   A.validity_penalty = p.validity_penalty;
   A.blacklist_limit = p.blacklist_limit;
-  depth_observe_kernel<<<pixel_grid(dm->w, dm->h), 256, 0, ctx->stream>>>(A);
-  ctx->launches += 1;
+  // the pixels that search, then a persistent grid that deals them out 32 at a time
+  const int npix = dm->w * dm->h;
+  CK(ctx, cudaMemsetAsync(dm->counters, 0, 2 * sizeof(int), ctx->stream));
+  depth_worklist_kernel<<<(npix + 255) / 256, 256, 0, ctx->stream>>>(A.key, dm->w, dm->h, p.min_grad, dm->work,
+                                                                       dm->counters);
+  // resident CTAs of the observe kernel per SM (a property of the kernel on this architecture)
+  static const int per_sm = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, depth_observe_kernel, 128, 0) != cudaSuccess) {
+      cudaGetLastError();
+      b = 4;
+    }
+    return b > 0 ? b : 1;
+  }();
+  depth_observe_kernel<<<per_sm * (ctx->sm_count > 0 ? ctx->sm_count : 1), 128, 0, ctx->stream>>>(A, dm->work,
+                                                                                               dm->counters);
+  ctx->launches += 2;
   CK(ctx, cudaGetLastError());
   if (regularize) return enqueue_regularize(ctx, dm);
   return LSDG_OK;
