@@ -872,10 +872,10 @@ def run_profile_energy(args):
 
 
 def run_sequence_bench(args):
-    """The full synthetic sequence: a 20-plane room, cubic-spline path at 0.5 m/s, 30 Hz, every
-    frame tracked and mapped on the GPU (sequence.py), keyframes with batched Sim3 constraint
-    search, own Sim3 pose graph.  Prints one JSON line with frames/s and the trajectory error."""
-    import lsdg
+    """The full synthetic sequence: a 20-plane room, cubic-spline path at 0.5 m/s, 30 Hz, fed frame
+    by frame to the library's SLAM loop (lsdg_slam: tracking and mapping on this thread, batched
+    Sim3 constraint search in both directions and the pose graph on its worker thread).  Prints one
+    JSON line with frames/s and the trajectory error against the ground truth."""
     import sequence
     import synth
 
@@ -884,16 +884,14 @@ def run_sequence_bench(args):
     seq, frames = synth.room_sequence(0, n, W if not args.small else 320, H if not args.small else 240,
                                       workers=min(16, os.cpu_count() or 8))
     render_s = time.time() - t
-    ctx = lsdg.Context()
-    res = sequence.run(ctx, seq, frames)
-    ctx.close()
+    res = sequence.run(seq, frames)
     out = {"metric": "full sequence frames/s and absolute trajectory error", "impl": "ours",
            "workload": "%d frames %dx%d at 30 Hz, 0.5 m/s cubic-spline path through a 20-plane room, "
                        "keyframe every 0.1 m / 6 deg / 55 %% point usage, Sim3 constraint search against <= 10 "
-                       "candidates in one batched launch, own Sim3 pose graph" % (n, seq.w, seq.h),
+                       "candidates in both directions in one batched launch, Sim3 pose graph" % (n, seq.w, seq.h),
            "render_seconds": render_s, **res,
-           "note": "single-threaded Python driver over the C-ABI (tracking, mapping and constraint search in "
-                   "sequence); first keyframe bootstrapped from the synthetic depth; no relocalisation"}
+           "note": "the library's C++ SLAM loop (lsdg_slam_next_image per frame; constraint search on its worker "
+                   "thread); first keyframe bootstrapped from the synthetic depth; no relocalisation"}
     print(json.dumps(out), flush=True)
 
 

@@ -591,6 +591,83 @@ LSDG_API int lsdg_format_pose_row(int id, const double cam_to_world13[13], const
                                   char* buf, int len);
 
 /* ------------------------------------------------------------------------------------------ */
+/* The full SLAM loop (upstream SlamSystem; host C++ over the calls above)                      */
+/* ------------------------------------------------------------------------------------------ */
+
+/* Upstream's SlamSystem is fed by InputThread (lib/App/InputThread.cpp:71
+ * `system->nextImage(runningIdx, imageUndist, camera)`), finalised at the end (tools/LSD.cpp:139)
+ * and publishes a keyframe graph (PangolinOutputIOWrapper::publishKeyframeGraph,
+ * lib/Pangolin_IOWrapper/PangolinOutputIOWrapper.cpp:148-168) and per-frame poses
+ * (TextOutputIOWrapper::publishTrackedFrame, lib/Pangolin_IOWrapper/TextOutputIOWrapper.cpp:100-120).
+ * lsdg_slam is that loop: tracking and mapping on the caller's thread in lsdg_slam_next_image
+ * (trackFrame against the current keyframe, updateKeyframe, keyframe creation by createKeyFrame);
+ * Sim3 constraint search of each new keyframe against its predecessor and nearby keyframes (batched,
+ * optionally in both directions) and the Sim3 pose-graph optimisation on a worker thread with its
+ * own context.  Its policy constants are this project's own (upstream's are not available). */
+typedef struct lsdg_slam lsdg_slam;
+typedef struct lsdg_slam_params {
+  float kf_dist;            /* a new keyframe after this much travel from the current one (m)      */
+  float kf_angle_deg;       /* ... or this much rotation (degrees)                                 */
+  float kf_min_usage;       /* ... or when fewer of the keyframe's points than this stay in view    */
+  int32_t refresh_every;    /* tracking reference refreshed from the depth filter every N frames   */
+  int32_t n_candidates;     /* Sim3 constraint candidates per new keyframe (predecessor included)  */
+  float cand_radius;        /* candidates: earlier keyframes whose centres lie within this (m)     */
+  int32_t optimize_every;   /* pose-graph optimisation after this many keyframes with a loop edge  */
+  int32_t final_iterations; /* Gauss-Newton iterations of lsdg_slam_finalize                      */
+  float max_track_jump;     /* a tracked pose this far from the constant-velocity guess is lost (m) */
+  int32_t both_directions;  /* track every constraint both ways and keep it only when they agree  */
+  float consistency_trans;  /* ... translation of Z_ab Z_ba below this fraction of |t_ab|         */
+  float consistency_rot;    /* ... rotation below this (rad)                                      */
+  float consistency_scale;  /* ... |log scale| below this                                         */
+  int32_t async_constraints; /* constraint search on the worker thread (1) or inline (0)          */
+  int32_t graph_threads;    /* host threads of the pose graph's Cholesky                           */
+  int32_t reserved[8];
+} lsdg_slam_params;
+
+typedef struct lsdg_slam_stats {
+  int32_t frames, keyframes, lost_frames, sim3_edges, sim3_rejected, graph_optimisations;
+  int32_t reserved[6];
+} lsdg_slam_stats;
+
+LSDG_API void lsdg_slam_default_params(lsdg_slam_params* p);
+/* A system for width x height 8-bit frames of camera `intr` on `device` (two contexts, a depth map). */
+LSDG_API lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* sp, int device,
+                                      int width, int height, const lsdg_intrinsics* intr, lsdg_slam** out);
+LSDG_API lsdg_status lsdg_slam_destroy(lsdg_slam* s);
+LSDG_API const char* lsdg_slam_last_error(const lsdg_slam* s);
+/* The first keyframe, with a known inverse depth and variance (idepth <= 0 = none). */
+LSDG_API lsdg_status lsdg_slam_bootstrap(lsdg_slam* s, int id, const uint8_t* image, const float* idepth,
+                                         const float* var);
+/* SlamSystem::nextImage: track, map, and possibly make a keyframe (which starts its constraint
+ * search).  A frame that fails to track keeps the constant-velocity guess and is counted lost. */
+LSDG_API lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image);
+/* SlamSystem::finalize: waits for the constraint search and optimises the pose graph. */
+LSDG_API lsdg_status lsdg_slam_finalize(lsdg_slam* s);
+LSDG_API lsdg_status lsdg_slam_get_stats(const lsdg_slam* s, lsdg_slam_stats* out);
+/* Camera-to-world Sim3 {R, t, s} (13 doubles) of every frame so far (keyframe pose from the graph
+ * times the frame's tracked pose); cam_to_world = NULL returns the count in n. */
+LSDG_API lsdg_status lsdg_slam_get_poses(lsdg_slam* s, double* cam_to_world, int capacity, int* n);
+/* The keyframe graph as publishKeyframeGraph hands it out (GraphFramePose: id + Sophus 7 floats). */
+LSDG_API lsdg_status lsdg_slam_keyframe_graph(lsdg_slam* s, lsdg_graph_frame_pose* out, int capacity, int* n);
+/* One TextOutputIOWrapper pose row per frame (lsdg_format_pose_row) into a file. */
+LSDG_API lsdg_status lsdg_slam_write_pose_file(lsdg_slam* s, const char* path);
+
+/* The Sim3 pose graph alone (host only): nodes are camera-to-world Sim3 poses, an edge (i, j, Z, W)
+ * says "pose j seen from pose i is Z" with 7x7 information W (twist order v, omega, log-scale; row
+ * major); cost sum rho(r^T W r), r = log(Z^-1 T_i^-1 T_j), Huber kernel at 3 sigma; node 0 held. */
+typedef struct lsdg_posegraph lsdg_posegraph;
+LSDG_API lsdg_status lsdg_posegraph_create(lsdg_posegraph** out);
+LSDG_API lsdg_status lsdg_posegraph_destroy(lsdg_posegraph* g);
+LSDG_API int lsdg_posegraph_add_node(lsdg_posegraph* g, const double cam_to_world13[13]);
+LSDG_API lsdg_status lsdg_posegraph_add_edge(lsdg_posegraph* g, int i, int j, const double z13[13],
+                                             const double info[49]);
+LSDG_API lsdg_status lsdg_posegraph_optimize(lsdg_posegraph* g, int iterations, double* cost);
+LSDG_API lsdg_status lsdg_posegraph_get_pose(const lsdg_posegraph* g, int i, double cam_to_world13[13]);
+/* exp / log of sim(3) twists (v, omega, log-scale) <-> 13-double poses. */
+LSDG_API void lsdg_sim3_exp13(const double xi[7], double out13[13]);
+LSDG_API void lsdg_sim3_log13(const double pose13[13], double xi[7]);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                   */
 /* ------------------------------------------------------------------------------------------ */
 

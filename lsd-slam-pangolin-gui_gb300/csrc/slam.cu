@@ -1,0 +1,603 @@
+// slam.cu -- host-only: the full monocular SLAM loop over the GPU hot path (config 4 of the
+// workloads: a 1,000-frame sequence).
+//
+// Upstream this is lsd-slam's SlamSystem (absent from the reference tree; the reference feeds it from
+// InputThread, lib/App/InputThread.cpp:71 `system->nextImage(runningIdx, imageUndist, camera)`, and
+// finalises it at the end, tools/LSD.cpp:139; results leave through OutputIOWrapper:
+// PangolinOutputIOWrapper::publishKeyframeGraph, lib/Pangolin_IOWrapper/PangolinOutputIOWrapper.cpp:148-168,
+// and TextOutputIOWrapper::publishTrackedFrame, lib/Pangolin_IOWrapper/TextOutputIOWrapper.cpp:100-120).
+// Upstream runs three threads around the hot path; this loop keeps that division of work:
+//   * tracking (the caller's thread, lsdg_slam_next_image): every frame is aligned to the current
+//     keyframe (SE3Tracker::trackFrame, constant-velocity initial guess);
+//   * mapping (same thread, after tracking): the frame updates the keyframe's depth
+//     (DepthMap::updateKeyframe, 8-bit frame), the tracking reference is refreshed from the smoothed
+//     depth every few frames, and after kf_dist metres of travel, a kf_angle turn, or when fewer than
+//     kf_min_usage of the keyframe's points stay in view, the frame becomes the new keyframe
+//     (DepthMap::createKeyFrame: propagation + regularisation);
+//   * constraint search (a worker thread with a context of its own): each new keyframe is aligned
+//     with Sim3Tracker::trackFrameSim3 to its predecessor and the nearest earlier keyframes in one
+//     batched launch from device-resident keyframes -- in both directions, a constraint being kept
+//     only when the two alignments agree -- and the Sim3 pose graph is optimised every few loop
+//     constraints.  The worker runs while tracking and mapping go on; it is joined before the next
+//     keyframe is made, so the results do not depend on thread timing.
+// The first keyframe's depth is given (lsdg_slam_bootstrap); upstream starts from a random map.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "lsdg.h"
+#include "slam_math.h"
+
+using lsdg::slam::M4;
+
+namespace {
+
+struct Keyframe {
+  int frame_index = 0;
+  int node = 0;
+  lsdg_frame* frame = nullptr;     // tracking reference (refreshed while it is the current keyframe)
+  lsdg_frame* snapshot = nullptr;  // its state at creation, read by the constraint search of its own job
+};
+
+struct FramePose {
+  int keyframe;  // index into keyframes
+  M4 f2k;        // frame-to-keyframe
+};
+
+}  // namespace
+
+struct lsdg_slam {
+  lsdg_params params{};
+  lsdg_slam_params sp{};
+  int w = 0, h = 0;
+  lsdg_intrinsics intr{};
+  lsdg_ctx* ctx = nullptr;       // tracking and mapping
+  lsdg_ctx* ctx_cons = nullptr;  // constraint search (worker thread)
+  lsdg_depthmap* dm = nullptr;
+  lsdg_frame* pool[2] = {nullptr, nullptr};
+  int pool_next = 0;
+  std::vector<Keyframe> keyframes;
+  std::vector<FramePose> traj;
+  std::vector<int> traj_id;  // the caller's frame ids
+  lsdg::slam::PoseGraph graph;
+  std::map<int, lsdg_batch*> batches;  // Sim3 batches by size (worker context)
+  std::thread worker;
+  bool worker_running = false;
+  lsdg_status worker_status = LSDG_OK;
+  std::string worker_error;
+  int since_refresh = 0;
+  int loops_pending = 0;
+  lsdg_slam_stats stats{};
+  std::vector<float> d_buf, v_buf;
+  std::string err;
+};
+
+namespace {
+
+// The worker thread records its errors in the system's worker_error, the caller's thread in err.
+thread_local std::string* t_err = nullptr;
+
+lsdg_status fail(lsdg_slam* s, lsdg_status st, const char* what, const lsdg_ctx* c = nullptr) {
+  if (s) {
+    std::string& e = t_err ? *t_err : s->err;
+    e = what;
+    if (c) {
+      e += ": ";
+      e += lsdg_last_error(c);
+    }
+  }
+  return st;
+}
+
+#define SLAM_CK(s, expr, ctx)                              \
+  do {                                                     \
+    const lsdg_status st_ = (expr);                        \
+    if (st_ != LSDG_OK) return fail((s), st_, #expr, ctx); \
+  } while (0)
+
+double norm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+double rotation_angle(const M4& T) {
+  const double s = lsdg::slam::sim3_scale(T);
+  double R[9], w[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = T(i, j) / s;
+  lsdg::slam::so3_log(R, w);
+  return norm3(w);
+}
+
+bool finite(const M4& T) {
+  for (double v : T.a)
+    if (!std::isfinite(v)) return false;
+  return true;
+}
+
+// The depth map's smoothed inverse depth and variance (the planes the viewer reads) into a frame.
+lsdg_status reference_depth(lsdg_slam* s, lsdg_frame* f) {
+  SLAM_CK(s, lsdg_depth_get(s->ctx, s->dm, nullptr, nullptr, s->d_buf.data(), s->v_buf.data(), nullptr, nullptr), s->ctx);
+  SLAM_CK(s, lsdg_frame_set_depth(s->ctx, f, s->d_buf.data(), s->v_buf.data()), s->ctx);
+  return LSDG_OK;
+}
+
+lsdg_status new_frame_with_depth(lsdg_slam* s, const uint8_t* image, lsdg_frame** out) {
+  *out = nullptr;
+  SLAM_CK(s, lsdg_frame_create(s->ctx, s->w, s->h, &s->intr, out), s->ctx);
+  SLAM_CK(s, lsdg_frame_upload_u8(s->ctx, *out, image), s->ctx);
+  return reference_depth(s, *out);
+}
+
+void hess_full(const lsdg_track_stats& st, int n, double* H) {  // upper triangle -> n x n
+  int q = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = i; j < n; ++j) {
+      H[n * i + j] = H[n * j + i] = st.hessian[q];
+      ++q;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Constraint search of keyframe `k` (worker thread: its own context, the graph is its own until
+// joined)
+// ------------------------------------------------------------------------------------------
+struct Cand {
+  double dist;
+  int kf;
+};
+
+lsdg_status constraint_job(lsdg_slam* s, int k) {
+  lsdg_ctx* ctx = s->ctx_cons;
+  const Keyframe& kn = s->keyframes[k];
+  const Keyframe& kp = s->keyframes[k - 1];
+  const M4 T_new = s->graph.poses[kn.node];
+  std::vector<Cand> others;
+  for (int c = 0; c + 2 <= k; ++c) {
+    const M4& Tc = s->graph.poses[s->keyframes[c].node];
+    const double d[3] = {Tc(0, 3) - T_new(0, 3), Tc(1, 3) - T_new(1, 3), Tc(2, 3) - T_new(2, 3)};
+    const double dist = norm3(d);
+    if (dist < s->sp.cand_radius) others.push_back({dist, c});
+  }
+  std::stable_sort(others.begin(), others.end(), [](const Cand& a, const Cand& b) { return a.dist < b.dist; });
+  std::vector<int> cands = {k - 1};
+  for (const Cand& c : others) {
+    if ((int)cands.size() >= s->sp.n_candidates) break;
+    cands.push_back(c.kf);
+  }
+  const int nc = (int)cands.size();
+  const bool both = s->sp.both_directions != 0;
+  const int nb = both ? 2 * nc : nc;
+  lsdg_batch*& b = s->batches[nb];
+  if (!b) {
+    std::vector<int> ws(nb, s->w), hs(nb, s->h);
+    std::vector<lsdg_intrinsics> ks(nb, s->intr);
+    SLAM_CK(s, lsdg_batch_create_sim3(ctx, nb, ws.data(), hs.data(), ks.data(), &b), ctx);
+  }
+  // pair i < nc: the new keyframe tracked against candidate i (frame-to-ref = new-in-candidate);
+  // pair nc + i: the candidate tracked against the new keyframe
+  std::vector<const lsdg_frame*> refs(nb), frames(nb);
+  std::vector<double> init(13 * (size_t)nb);
+  std::vector<M4> Zinit(nc);
+  for (int i = 0; i < nc; ++i) {
+    const Keyframe& c = s->keyframes[cands[i]];
+    Zinit[i] = lsdg::slam::mul(lsdg::slam::sim3_inv(s->graph.poses[c.node]), T_new);
+    refs[i] = c.frame;
+    frames[i] = kn.snapshot;
+    lsdg::slam::to13(Zinit[i], &init[13 * i]);
+    if (both) {
+      refs[nc + i] = kn.snapshot;
+      frames[nc + i] = c.frame;
+      lsdg::slam::to13(lsdg::slam::sim3_inv(Zinit[i]), &init[13 * (nc + i)]);
+    }
+  }
+  SLAM_CK(s, lsdg_batch_load_frames(ctx, b, refs.data(), frames.data(), init.data()), ctx);
+  SLAM_CK(s, lsdg_batch_run(ctx, b), ctx);
+  std::vector<double> out(13 * (size_t)nb);
+  std::vector<lsdg_track_stats> st(nb);
+  SLAM_CK(s, lsdg_batch_read(ctx, b, out.data(), st.data()), ctx);
+  bool loop = false;
+  for (int i = 0; i < nc; ++i) {
+    const double* o = &out[13 * i];
+    bool ok = st[i].status == LSDG_OK && std::isfinite(o[12]) && o[12] > 0.5 && o[12] < 2.0;
+    M4 Z = M4::identity();
+    if (ok) {
+      Z = lsdg::slam::from13(o);
+      ok = finite(Z);
+    }
+    if (ok) {  // the result stays near the graph's prediction
+      double dz[7];
+      lsdg::slam::sim3_log(lsdg::slam::mul(lsdg::slam::sim3_inv(Zinit[i]), Z), dz);
+      const double tz[3] = {Z(0, 3), Z(1, 3), Z(2, 3)};
+      ok = norm3(dz) < 0.25 * std::max(1.0, norm3(tz)) && norm3(dz + 3) < 0.15 && std::fabs(dz[6]) < 0.1;
+    }
+    if (ok && both) {  // the reverse alignment agrees: Z_fwd Z_rev ~ identity
+      const double* orv = &out[13 * (nc + i)];
+      ok = st[nc + i].status == LSDG_OK && std::isfinite(orv[12]) && orv[12] > 0.0;
+      if (ok) {
+        double e[7];
+        lsdg::slam::sim3_log(lsdg::slam::mul(Z, lsdg::slam::from13(orv)), e);
+        const double tz[3] = {Z(0, 3), Z(1, 3), Z(2, 3)};
+        ok = std::isfinite(e[0]) && norm3(e) < s->sp.consistency_trans * std::max(0.1, norm3(tz)) &&
+             norm3(e + 3) < s->sp.consistency_rot && std::fabs(e[6]) < s->sp.consistency_scale;
+      }
+    }
+    double H[49];
+    if (ok) {
+      hess_full(st[i], 7, H);
+      for (double v : H) ok = ok && std::isfinite(v);
+    }
+    if (!ok) {
+      s->stats.sim3_rejected++;
+      continue;
+    }
+    for (double& v : H) v *= 1e-3;
+    s->graph.add_edge(s->keyframes[cands[i]].node, kn.node, Z, H);
+    s->stats.sim3_edges++;
+    loop = loop || cands[i] != k - 1;
+    (void)kp;
+  }
+  if (loop && ++s->loops_pending >= s->sp.optimize_every) {
+    const std::vector<M4> keep = s->graph.poses;
+    s->graph.optimize(5);
+    bool good = true;
+    for (const M4& T : s->graph.poses) good = good && finite(T);
+    if (!good) s->graph.poses = keep;
+    s->loops_pending = 0;
+    s->stats.graph_optimisations++;
+  }
+  return LSDG_OK;
+}
+
+lsdg_status join_worker(lsdg_slam* s) {
+  if (s->worker_running) {
+    s->worker.join();
+    s->worker_running = false;
+    // the new keyframe's snapshot was read by its own job only
+    Keyframe& k = s->keyframes.back();
+    if (k.snapshot) {
+      lsdg_frame_destroy(s->ctx, k.snapshot);
+      k.snapshot = nullptr;
+    }
+  }
+  if (s->worker_status != LSDG_OK) {
+    s->err = "constraint search: " + s->worker_error;
+    return s->worker_status;
+  }
+  return LSDG_OK;
+}
+
+lsdg_status start_job(lsdg_slam* s, int k) {
+  auto body = [s, k]() {
+    std::string* keep = t_err;
+    t_err = &s->worker_error;
+    const lsdg_status st = constraint_job(s, k);
+    if (st != LSDG_OK) s->worker_status = st;
+    t_err = keep;
+  };
+  if (s->sp.async_constraints) {
+    try {
+      s->worker = std::thread(body);
+    } catch (...) {
+      return fail(s, LSDG_OUT_OF_MEMORY, "could not start the constraint-search thread");
+    }
+    s->worker_running = true;
+    return LSDG_OK;
+  }
+  body();
+  Keyframe& kn = s->keyframes[k];
+  if (kn.snapshot) {
+    lsdg_frame_destroy(s->ctx, kn.snapshot);
+    kn.snapshot = nullptr;
+  }
+  if (s->worker_status != LSDG_OK) {
+    s->err = "constraint search: " + s->worker_error;
+    return s->worker_status;
+  }
+  return LSDG_OK;
+}
+
+lsdg_status new_keyframe(lsdg_slam* s, int frame_index, const uint8_t* image, const M4& f2k,
+                         const lsdg_track_stats& st) {
+  lsdg_status r = join_worker(s);  // the graph is the caller's again
+  if (r != LSDG_OK) return r;
+  const M4 k2f = lsdg::slam::sim3_inv(f2k);
+  double k2f12[12];
+  lsdg::slam::to12(k2f, k2f12);
+  std::vector<float> img((size_t)s->w * s->h);
+  for (size_t i = 0; i < img.size(); ++i) img[i] = (float)image[i];
+  SLAM_CK(s, lsdg_depth_create_keyframe(s->ctx, s->dm, img.data(), k2f12, 1), s->ctx);
+  const Keyframe& prev = s->keyframes.back();
+  Keyframe kf;
+  kf.frame_index = frame_index;
+  kf.node = s->graph.add_node(lsdg::slam::mul(s->graph.poses[prev.node], f2k));
+  r = new_frame_with_depth(s, image, &kf.frame);
+  if (r == LSDG_OK) r = new_frame_with_depth(s, image, &kf.snapshot);
+  if (r != LSDG_OK) {
+    if (kf.frame) lsdg_frame_destroy(s->ctx, kf.frame);
+    if (kf.snapshot) lsdg_frame_destroy(s->ctx, kf.snapshot);
+    return r;
+  }
+  const int prev_node = prev.node;
+  s->keyframes.push_back(kf);
+  s->traj.back() = {(int)s->keyframes.size() - 1, M4::identity()};
+  s->since_refresh = 0;
+  // odometry edge from the tracking chain (SE3 information; the scale tied by a prior as strong as
+  // the strongest direction)
+  double H6[36], W[49];
+  hess_full(st, 6, H6);
+  bool ok = true;
+  double dmax = 0.0;
+  for (int i = 0; i < 36; ++i) ok = ok && std::isfinite(H6[i]);
+  for (int i = 0; i < 6; ++i) dmax = std::max(dmax, H6[7 * i]);
+  if (ok && dmax > 0) {
+    std::memset(W, 0, sizeof(W));
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) W[7 * i + j] = H6[6 * i + j] * 1e-3;
+    W[48] = dmax * 1e-3;
+    s->graph.add_edge(prev_node, kf.node, f2k, W);
+  }
+  s->stats.keyframes = (int)s->keyframes.size();
+  return start_job(s, (int)s->keyframes.size() - 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+void lsdg_slam_default_params(lsdg_slam_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->kf_dist = 0.1f;
+  p->kf_angle_deg = 6.0f;
+  p->kf_min_usage = 0.55f;
+  p->refresh_every = 4;
+  p->n_candidates = 10;
+  p->cand_radius = 1.2f;
+  p->optimize_every = 5;
+  p->final_iterations = 20;
+  p->max_track_jump = 0.2f;
+  p->both_directions = 1;
+  p->consistency_trans = 0.1f;
+  p->consistency_rot = 0.02f;
+  p->consistency_scale = 0.02f;
+  p->async_constraints = 1;
+  p->graph_threads = 8;
+}
+
+lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* sp, int device, int width, int height,
+                             const lsdg_intrinsics* intr, lsdg_slam** out) {
+  if (!out || !intr) return LSDG_INVALID_ARG;
+  *out = nullptr;
+  lsdg_slam* s = new (std::nothrow) lsdg_slam();
+  if (!s) return LSDG_OUT_OF_MEMORY;
+  if (params) s->params = *params;
+  else lsdg_default_params(&s->params);
+  if (sp) s->sp = *sp;
+  else lsdg_slam_default_params(&s->sp);
+  s->w = width;
+  s->h = height;
+  s->intr = *intr;
+  s->graph.threads = std::max(1, s->sp.graph_threads);
+  s->d_buf.resize((size_t)width * height);
+  s->v_buf.resize((size_t)width * height);
+  lsdg_status st = lsdg_create(&s->ctx, &s->params, device);
+  if (st == LSDG_OK) st = lsdg_create(&s->ctx_cons, &s->params, device);
+  if (st == LSDG_OK) st = lsdg_depth_create(s->ctx, width, height, intr, &s->dm);
+  for (int i = 0; i < 2 && st == LSDG_OK; ++i) st = lsdg_frame_create(s->ctx, width, height, intr, &s->pool[i]);
+  if (st != LSDG_OK) {
+    lsdg_slam_destroy(s);
+    return st;
+  }
+  *out = s;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_destroy(lsdg_slam* s) {
+  if (!s) return LSDG_INVALID_ARG;
+  if (s->worker_running) s->worker.join();
+  for (auto& kv : s->batches)
+    if (kv.second) lsdg_batch_destroy(s->ctx_cons, kv.second);
+  for (Keyframe& k : s->keyframes) {
+    if (k.frame) lsdg_frame_destroy(s->ctx, k.frame);
+    if (k.snapshot) lsdg_frame_destroy(s->ctx, k.snapshot);
+  }
+  for (lsdg_frame* f : s->pool)
+    if (f) lsdg_frame_destroy(s->ctx, f);
+  if (s->dm) lsdg_depth_destroy(s->ctx, s->dm);
+  if (s->ctx_cons) lsdg_destroy(s->ctx_cons);
+  if (s->ctx) lsdg_destroy(s->ctx);
+  delete s;
+  return LSDG_OK;
+}
+
+const char* lsdg_slam_last_error(const lsdg_slam* s) { return s ? s->err.c_str() : "null system"; }
+
+lsdg_status lsdg_slam_bootstrap(lsdg_slam* s, int id, const uint8_t* image, const float* idepth, const float* var) {
+  if (!s || !image || !idepth || !var) return LSDG_INVALID_ARG;
+  if (!s->keyframes.empty()) return fail(s, LSDG_INVALID_ARG, "already bootstrapped");
+  std::vector<float> img((size_t)s->w * s->h);
+  for (size_t i = 0; i < img.size(); ++i) img[i] = (float)image[i];
+  SLAM_CK(s, lsdg_depth_set_keyframe(s->ctx, s->dm, img.data(), idepth, var), s->ctx);
+  Keyframe kf;
+  kf.frame_index = 0;
+  kf.node = s->graph.add_node(M4::identity());
+  const lsdg_status st = new_frame_with_depth(s, image, &kf.frame);
+  if (st != LSDG_OK) return st;
+  s->keyframes.push_back(kf);
+  s->traj.push_back({0, M4::identity()});
+  s->traj_id.push_back(id);
+  s->stats.frames = 1;
+  s->stats.keyframes = 1;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
+  if (!s || !image) return LSDG_INVALID_ARG;
+  if (s->keyframes.empty()) return fail(s, LSDG_INVALID_ARG, "bootstrap the first keyframe first");
+  const int kfi = (int)s->keyframes.size() - 1;
+  const Keyframe& kf = s->keyframes[kfi];
+  // constant-velocity guess in the keyframe's frame
+  const FramePose& last = s->traj.back();
+  const M4 c1 = last.keyframe == kfi ? last.f2k : M4::identity();
+  M4 c0 = c1;
+  if (s->traj.size() > 1 && s->traj[s->traj.size() - 2].keyframe == kfi) c0 = s->traj[s->traj.size() - 2].f2k;
+  M4 guess = lsdg::slam::mul(lsdg::slam::mul(c1, lsdg::slam::sim3_inv(c0)), c1);
+  if (!finite(guess)) guess = c1;
+  lsdg_frame* frame = s->pool[s->pool_next];
+  s->pool_next ^= 1;
+  SLAM_CK(s, lsdg_frame_upload_u8(s->ctx, frame, image), s->ctx);
+  double g12[12], o12[12];
+  lsdg::slam::to12(guess, g12);
+  lsdg_track_stats st{};
+  const lsdg_status ts = lsdg_track_se3(s->ctx, kf.frame, frame, g12, o12, &st);
+  if (ts != LSDG_OK && ts != LSDG_TRACKING_LOST) return fail(s, ts, "lsdg_track_se3", s->ctx);
+  M4 f2k = lsdg::slam::from12(o12);
+  const double jump[3] = {f2k(0, 3) - guess(0, 3), f2k(1, 3) - guess(1, 3), f2k(2, 3) - guess(2, 3)};
+  bool good = st.status == LSDG_OK && finite(f2k) && norm3(jump) <= s->sp.max_track_jump;
+  if (!good) {
+    s->stats.lost_frames++;
+    f2k = guess;
+  }
+  s->traj.push_back({kfi, f2k});
+  s->traj_id.push_back(id);
+  s->stats.frames++;
+  if (!good) return LSDG_OK;
+  // mapping: this frame observes the keyframe's depth
+  const M4 k2f = lsdg::slam::sim3_inv(f2k);
+  double k2f12[12];
+  lsdg::slam::to12(k2f, k2f12);
+  SLAM_CK(s, lsdg_depth_update_u8(s->ctx, s->dm, 1, image, k2f12, 1), s->ctx);
+  if (++s->since_refresh >= s->sp.refresh_every) {
+    lsdg_status r = reference_depth(s, s->keyframes[kfi].frame);
+    if (r != LSDG_OK) return r;
+    s->since_refresh = 0;
+  }
+  const double t[3] = {f2k(0, 3), f2k(1, 3), f2k(2, 3)};
+  if (norm3(t) > s->sp.kf_dist || rotation_angle(f2k) > s->sp.kf_angle_deg * M_PI / 180.0 ||
+      st.usage < s->sp.kf_min_usage)
+    return new_keyframe(s, (int)s->traj.size() - 1, image, f2k, st);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_finalize(lsdg_slam* s) {
+  if (!s) return LSDG_INVALID_ARG;
+  lsdg_status r = join_worker(s);
+  if (r != LSDG_OK) return r;
+  const std::vector<M4> keep = s->graph.poses;
+  s->graph.optimize(s->sp.final_iterations);
+  bool good = true;
+  for (const M4& T : s->graph.poses) good = good && finite(T);
+  if (!good) s->graph.poses = keep;
+  s->stats.graph_optimisations++;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_get_stats(const lsdg_slam* s, lsdg_slam_stats* out) {
+  if (!s || !out) return LSDG_INVALID_ARG;
+  *out = s->stats;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_get_poses(lsdg_slam* s, double* cam_to_world, int capacity, int* n) {
+  if (!s || !n) return LSDG_INVALID_ARG;
+  lsdg_status r = join_worker(s);
+  if (r != LSDG_OK) return r;
+  *n = (int)s->traj.size();
+  if (!cam_to_world) return LSDG_OK;
+  if (capacity < *n) return fail(s, LSDG_INVALID_ARG, "capacity below the frame count");
+  for (size_t i = 0; i < s->traj.size(); ++i) {
+    const M4 T = lsdg::slam::mul(s->graph.poses[s->keyframes[s->traj[i].keyframe].node], s->traj[i].f2k);
+    lsdg::slam::to13(T, cam_to_world + 13 * i);
+  }
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_keyframe_graph(lsdg_slam* s, lsdg_graph_frame_pose* out, int capacity, int* n) {
+  if (!s || !n) return LSDG_INVALID_ARG;
+  lsdg_status r = join_worker(s);
+  if (r != LSDG_OK) return r;
+  *n = (int)s->keyframes.size();
+  if (!out) return LSDG_OK;
+  if (capacity < *n) return fail(s, LSDG_INVALID_ARG, "capacity below the keyframe count");
+  for (int k = 0; k < *n; ++k) {
+    double p13[13];
+    lsdg::slam::to13(s->graph.poses[s->keyframes[k].node], p13);
+    out[k].id = s->traj_id[s->keyframes[k].frame_index];
+    lsdg_sim3_to_sophus7(p13, out[k].cam_to_world);
+  }
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_slam_write_pose_file(lsdg_slam* s, const char* path) {
+  if (!s || !path) return LSDG_INVALID_ARG;
+  lsdg_status r = join_worker(s);
+  if (r != LSDG_OK) return r;
+  FILE* f = std::fopen(path, "w");
+  if (!f) return fail(s, LSDG_INVALID_ARG, "cannot open the pose file");
+  char line[256];
+  for (size_t i = 0; i < s->traj.size(); ++i) {
+    const int kfi = s->traj[i].keyframe;
+    const M4& Tk = s->graph.poses[s->keyframes[kfi].node];
+    double c2w[13], rel[13];
+    lsdg::slam::to13(lsdg::slam::mul(Tk, s->traj[i].f2k), c2w);
+    lsdg::slam::to13(s->traj[i].f2k, rel);  // the frame's pose relative to its parent keyframe
+    const int len = lsdg_format_pose_row(s->traj_id[i], c2w, rel, line, (int)sizeof(line));
+    if (len > 0) std::fwrite(line, 1, (size_t)len, f);
+  }
+  std::fclose(f);
+  return LSDG_OK;
+}
+
+// ---- the pose graph alone (host only), for tests and for callers with their own front end ----
+struct lsdg_posegraph {
+  lsdg::slam::PoseGraph g;
+};
+
+lsdg_status lsdg_posegraph_create(lsdg_posegraph** out) {
+  if (!out) return LSDG_INVALID_ARG;
+  *out = new (std::nothrow) lsdg_posegraph();
+  return *out ? LSDG_OK : LSDG_OUT_OF_MEMORY;
+}
+
+lsdg_status lsdg_posegraph_destroy(lsdg_posegraph* g) {
+  delete g;
+  return LSDG_OK;
+}
+
+int lsdg_posegraph_add_node(lsdg_posegraph* g, const double cam_to_world13[13]) {
+  if (!g || !cam_to_world13) return -1;
+  return g->g.add_node(lsdg::slam::from13(cam_to_world13));
+}
+
+lsdg_status lsdg_posegraph_add_edge(lsdg_posegraph* g, int i, int j, const double z13[13], const double info[49]) {
+  if (!g || !z13 || !info || i < 0 || j < 0 || i >= (int)g->g.poses.size() || j >= (int)g->g.poses.size())
+    return LSDG_INVALID_ARG;
+  g->g.add_edge(i, j, lsdg::slam::from13(z13), info);
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_posegraph_optimize(lsdg_posegraph* g, int iterations, double* cost) {
+  if (!g) return LSDG_INVALID_ARG;
+  const double c = g->g.optimize(iterations);
+  if (cost) *cost = c;
+  return LSDG_OK;
+}
+
+lsdg_status lsdg_posegraph_get_pose(const lsdg_posegraph* g, int i, double cam_to_world13[13]) {
+  if (!g || !cam_to_world13 || i < 0 || i >= (int)g->g.poses.size()) return LSDG_INVALID_ARG;
+  lsdg::slam::to13(g->g.poses[i], cam_to_world13);
+  return LSDG_OK;
+}
+
+void lsdg_sim3_exp13(const double xi[7], double out13[13]) { lsdg::slam::to13(lsdg::slam::sim3_exp(xi), out13); }
+
+void lsdg_sim3_log13(const double pose13[13], double xi[7]) { lsdg::slam::sim3_log(lsdg::slam::from13(pose13), xi); }
+
+}  // extern "C"

@@ -128,6 +128,26 @@ def lib():
     _sig(L, "lsdg_sophus7_to_sim3", None, [_f32p, _f64p])
     _sig(L, "lsdg_format_pose_row", C.c_int, [C.c_int, _f64p, _f64p, C.c_char_p, C.c_int])
     _sig(L, "lsdg_tune_info", st, [_vp, C.c_int, C.c_char_p, C.c_int] + [C.POINTER(C.c_int)] * 4 + [C.POINTER(C.c_float)])
+    _sig(L, "lsdg_slam_default_params", None, [C.POINTER(T.SlamParams)])
+    _sig(L, "lsdg_slam_create", st, [C.POINTER(T.Params), C.POINTER(T.SlamParams), C.c_int, C.c_int, C.c_int,
+                                     C.POINTER(T.Intrinsics), C.POINTER(_vp)])
+    _sig(L, "lsdg_slam_destroy", st, [_vp])
+    _sig(L, "lsdg_slam_last_error", C.c_char_p, [_vp])
+    _sig(L, "lsdg_slam_bootstrap", st, [_vp, C.c_int, _u8p, _f32p, _f32p])
+    _sig(L, "lsdg_slam_next_image", st, [_vp, C.c_int, _u8p])
+    _sig(L, "lsdg_slam_finalize", st, [_vp])
+    _sig(L, "lsdg_slam_get_stats", st, [_vp, C.POINTER(T.SlamStats)])
+    _sig(L, "lsdg_slam_get_poses", st, [_vp, _vp, C.c_int, C.POINTER(C.c_int)])
+    _sig(L, "lsdg_slam_keyframe_graph", st, [_vp, _vp, C.c_int, C.POINTER(C.c_int)])
+    _sig(L, "lsdg_slam_write_pose_file", st, [_vp, C.c_char_p])
+    _sig(L, "lsdg_posegraph_create", st, [C.POINTER(_vp)])
+    _sig(L, "lsdg_posegraph_destroy", st, [_vp])
+    _sig(L, "lsdg_posegraph_add_node", C.c_int, [_vp, _f64p])
+    _sig(L, "lsdg_posegraph_add_edge", st, [_vp, C.c_int, C.c_int, _f64p, _f64p])
+    _sig(L, "lsdg_posegraph_optimize", st, [_vp, C.c_int, C.POINTER(C.c_double)])
+    _sig(L, "lsdg_posegraph_get_pose", st, [_vp, C.c_int, _f64p])
+    _sig(L, "lsdg_sim3_exp13", None, [_f64p, _f64p])
+    _sig(L, "lsdg_sim3_log13", None, [_f64p, _f64p])
     _lib = L
     return L
 
@@ -752,6 +772,125 @@ def cloud_build(ctx: Context, points, w: int, h: int, fx, fy, cx, cy, scale: flo
                                      None if params is None else C.byref(params), pts.ctypes.data, out.ctypes.data,
                                      C.byref(n)))
     return out[:n.value].copy()
+
+
+def slam_default_params() -> T.SlamParams:
+    p = T.SlamParams()
+    lib().lsdg_slam_default_params(C.byref(p))
+    return p
+
+
+class SlamSystem:
+    """Upstream SlamSystem over the C-ABI (lsdg_slam_*): nextImage tracks and maps a frame on the
+    caller's thread; keyframes' Sim3 constraint search and the pose graph run on the library's
+    worker thread."""
+
+    def __init__(self, w: int, h: int, intr, params: T.Params = None, slam_params: T.SlamParams = None,
+                 device: int = 0):
+        self.w, self.h = w, h
+        self._h = _vp()
+        p = params or default_params()
+        sp = slam_params or slam_default_params()
+        rc = lib().lsdg_slam_create(C.byref(p), C.byref(sp), device, w, h, C.byref(intrinsics(intr)), C.byref(self._h))
+        if rc != T.OK:
+            raise LsdgError(rc, "lsdg_slam_create")
+
+    def _check(self, rc):
+        if rc != T.OK:
+            raise LsdgError(rc, lib().lsdg_slam_last_error(self._h).decode())
+
+    def bootstrap(self, frame_id: int, image_u8, idepth, var):
+        self._check(lib().lsdg_slam_bootstrap(self._h, frame_id, np.ascontiguousarray(image_u8, np.uint8),
+                                              np.ascontiguousarray(idepth, np.float32),
+                                              np.ascontiguousarray(var, np.float32)))
+
+    def nextImage(self, frame_id: int, image_u8):
+        self._check(lib().lsdg_slam_next_image(self._h, frame_id, np.ascontiguousarray(image_u8, np.uint8)))
+
+    def finalize(self):
+        self._check(lib().lsdg_slam_finalize(self._h))
+
+    def stats(self) -> dict:
+        st = T.SlamStats()
+        self._check(lib().lsdg_slam_get_stats(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in T.SlamStats._fields_ if k != "reserved"}
+
+    def poses(self) -> np.ndarray:
+        """(n, 13) camera-to-world Sim3 {R, t, s} of every frame."""
+        n = C.c_int()
+        self._check(lib().lsdg_slam_get_poses(self._h, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 13))
+        self._check(lib().lsdg_slam_get_poses(self._h, out.ctypes.data, n.value, C.byref(n)))
+        return out
+
+    def keyframe_graph(self):
+        n = C.c_int()
+        self._check(lib().lsdg_slam_keyframe_graph(self._h, None, 0, C.byref(n)))
+        arr = (T.GraphFramePose * n.value)()
+        self._check(lib().lsdg_slam_keyframe_graph(self._h, C.cast(arr, _vp), n.value, C.byref(n)))
+        return [(g.id, np.array(g.cam_to_world[:], np.float32)) for g in arr]
+
+    def write_pose_file(self, path: str):
+        self._check(lib().lsdg_slam_write_pose_file(self._h, path.encode()))
+
+    def close(self):
+        if self._h:
+            lib().lsdg_slam_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class NativePoseGraph:
+    """The library's Sim3 pose graph (lsdg_posegraph_*), poses as 13-double {R, t, s}."""
+
+    def __init__(self):
+        self._h = _vp()
+        rc = lib().lsdg_posegraph_create(C.byref(self._h))
+        if rc != T.OK:
+            raise LsdgError(rc, "lsdg_posegraph_create")
+
+    def add_node(self, pose13) -> int:
+        return lib().lsdg_posegraph_add_node(self._h, np.ascontiguousarray(pose13, np.float64))
+
+    def add_edge(self, i, j, z13, info):
+        rc = lib().lsdg_posegraph_add_edge(self._h, i, j, np.ascontiguousarray(z13, np.float64),
+                                           np.ascontiguousarray(np.asarray(info, np.float64).reshape(49)))
+        if rc != T.OK:
+            raise LsdgError(rc, "lsdg_posegraph_add_edge")
+
+    def optimize(self, iterations: int) -> float:
+        c = C.c_double()
+        lib().lsdg_posegraph_optimize(self._h, iterations, C.byref(c))
+        return c.value
+
+    def pose(self, i) -> np.ndarray:
+        out = np.zeros(13)
+        rc = lib().lsdg_posegraph_get_pose(self._h, i, out)
+        if rc != T.OK:
+            raise LsdgError(rc, "lsdg_posegraph_get_pose")
+        return out
+
+    def close(self):
+        if self._h:
+            lib().lsdg_posegraph_destroy(self._h)
+            self._h = _vp()
+
+
+def sim3_exp13(xi) -> np.ndarray:
+    out = np.zeros(13)
+    lib().lsdg_sim3_exp13(np.ascontiguousarray(xi, np.float64), out)
+    return out
+
+
+def sim3_log13(pose13) -> np.ndarray:
+    out = np.zeros(7)
+    lib().lsdg_sim3_log13(np.ascontiguousarray(pose13, np.float64), out)
+    return out
 
 
 def pack_pairs(pairs):

@@ -122,3 +122,28 @@ class Calibration(C.Structure):
                 ("f", C.c_double), ("cx", C.c_double), ("cy", C.c_double), ("b1", C.c_double), ("b2", C.c_double),
                 ("k1", C.c_double), ("k2", C.c_double), ("k3", C.c_double), ("k4", C.c_double),
                 ("p1", C.c_double), ("p2", C.c_double)]
+
+
+class SlamParams(C.Structure):
+    """lsdg_slam_params (include/lsdg.h)."""
+    _fields_ = [
+        ("kf_dist", C.c_float), ("kf_angle_deg", C.c_float), ("kf_min_usage", C.c_float),
+        ("refresh_every", C.c_int32), ("n_candidates", C.c_int32), ("cand_radius", C.c_float),
+        ("optimize_every", C.c_int32), ("final_iterations", C.c_int32), ("max_track_jump", C.c_float),
+        ("both_directions", C.c_int32), ("consistency_trans", C.c_float), ("consistency_rot", C.c_float),
+        ("consistency_scale", C.c_float), ("async_constraints", C.c_int32), ("graph_threads", C.c_int32),
+        ("reserved", C.c_int32 * 8),
+    ]
+
+
+class SlamStats(C.Structure):
+    """lsdg_slam_stats (include/lsdg.h)."""
+    _fields_ = [("frames", C.c_int32), ("keyframes", C.c_int32), ("lost_frames", C.c_int32),
+                ("sim3_edges", C.c_int32), ("sim3_rejected", C.c_int32), ("graph_optimisations", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
+
+
+class GraphFramePose(C.Structure):
+    """lsdg_graph_frame_pose: a keyframe id and the Sophus 7-float camToWorld (include/lsdg.h)."""
+    _fields_ = [("id", C.c_int32), ("cam_to_world", C.c_float * 7)]
+

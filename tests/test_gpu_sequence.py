@@ -1,6 +1,9 @@
-"""A short full-system run on the GPU (sequence.py over the C-ABI): 240 frames of the synthetic
-room at 320x240 are tracked, mapped, turned into keyframes with batched Sim3 constraint search and a
-pose graph; the trajectory stays within a few percent of the path length of the ground truth."""
+"""Full-system runs on the GPU through the library's SLAM loop (lsdg_slam over the C-ABI, driven
+by sequence.py): frames of the synthetic room are tracked, mapped, turned into keyframes with
+batched two-way Sim3 constraint search and a Sim3 pose graph; the trajectory stays within a few
+percent of the path length of the ground truth, at 320x240 and at 640x480."""
+import os
+
 import numpy as np
 import pytest
 
@@ -9,12 +12,58 @@ import synth
 pytestmark = pytest.mark.gpu
 
 
-def test_room_sequence_runs_end_to_end(ctx):
+def _check(res, n):
+    assert res["frames"] == n and res["non_finite_frames"] == 0
+    assert res["lost_frames"] <= 5, res
+    assert res["keyframes"] >= 15 and res["sim3_edges"] >= res["keyframes"] - 1, res
+    assert res["keyframe_graph_nodes"] == res["keyframes"]
+
+
+def test_room_sequence_320x240(tmp_path):
     import sequence
-    seq, frames = synth.room_sequence(0, 240, 320, 240, workers=1)
-    res = sequence.run(ctx, seq, frames)
-    assert res["frames"] == 240 and res["non_finite_frames"] == 0
-    assert res["lost_frames"] <= 5
-    assert res["keyframes"] >= 15 and res["sim3_edges"] >= res["keyframes"]
+    seq, frames = synth.room_sequence(0, 240, 320, 240, workers=min(8, os.cpu_count() or 2))
+    res = sequence.run(seq, frames, pose_file=str(tmp_path / "pose.txt"))
+    _check(res, 240)
     assert res["ate_over_path"] < 0.05, res
     assert 0.85 < res["alignment_scale"] < 1.15, res
+    rows = (tmp_path / "pose.txt").read_text().splitlines()
+    assert len(rows) == 240 and rows[0].startswith("0,") and all(len(r.split(",")) == 7 for r in rows)
+
+
+def test_room_sequence_640x480():
+    import sequence
+    seq, frames = synth.room_sequence(0, 240, 640, 480, workers=min(16, os.cpu_count() or 2))
+    res = sequence.run(seq, frames)
+    _check(res, 240)
+    assert res["ate_over_path"] < 0.05, res
+
+
+def test_inline_constraints_equal_worker_thread():
+    """The constraint search on the worker thread (joined before each new keyframe) gives the
+    trajectory of the same search run inline, bit for bit."""
+    seq, frames = synth.room_sequence(1, 90, 320, 240, workers=min(8, os.cpu_count() or 2))
+    out = []
+    # one launch shape for every tracker call of both systems (the autotuner's pick could differ
+    # between them, and with it the summation order)
+    os.environ["LSDG_TRACK_SHAPE"] = "256,8,2"
+    try:
+        _run_both(seq, frames, out)
+    finally:
+        del os.environ["LSDG_TRACK_SHAPE"]
+    np.testing.assert_array_equal(out[0], out[1])
+
+
+def _run_both(seq, frames, out):
+    import lsdg
+    import sequence
+    for inline in (0, 1):
+        sp = lsdg.slam_default_params()
+        sp.async_constraints = 1 - inline
+        sys_ = lsdg.SlamSystem(seq.w, seq.h, seq.intr, slam_params=sp)
+        idepth, var = sequence.bootstrap_depth(seq, image=frames[0])
+        sys_.bootstrap(0, frames[0], idepth, var)
+        for k in range(1, 90):
+            sys_.nextImage(k, frames[k])
+        sys_.finalize()
+        out.append(sys_.poses())
+        sys_.close()

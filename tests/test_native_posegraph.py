@@ -1,0 +1,105 @@
+"""CPU tests of the library's Sim3 pose graph (lsdg_posegraph_*, csrc/slam_math.cu) against the
+independent numpy restatement in tests/posegraph.py: exp / log agree, and the same graphs converge
+to the same poses (consistent chains recovered exactly, drift spread by a loop edge, a bad edge held
+off by the Huber kernel)."""
+import math
+
+import numpy as np
+import pytest
+
+import lsdg
+import posegraph as G
+
+
+def rand_sim3(rng, scale_range=(0.7, 1.4), trans=1.0, angle=0.8):
+    xi = np.concatenate([rng.normal(size=3) * trans, rng.normal(size=3) * angle / math.sqrt(3),
+                         [math.log(rng.uniform(*scale_range))]])
+    return G.sim3_exp(xi), xi
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_exp_log_match_numpy(seed):
+    rng = np.random.default_rng(seed)
+    T, xi = rand_sim3(rng)
+    np.testing.assert_allclose(G.from13(lsdg.sim3_exp13(xi)), T, atol=1e-12)
+    np.testing.assert_allclose(lsdg.sim3_log13(G.to13(T)), xi, atol=1e-10)
+
+
+@pytest.mark.parametrize("xi", [[0.1, 0.2, -0.3, 0, 0, 0, 0], [0.1, 0.2, -0.3, 1e-5, 2e-5, 0, 0.3],
+                                [0.1, 0.2, -0.3, 2e-4, 0, 0, 2.5], [0.1, 0.2, -0.3, 2.5, 0.3, 0.1, 1e-7],
+                                [0.0, 0.0, 0.0, 3.1415, 0.0, 0.0, 0.0]])
+def test_exp_log_branches(xi):
+    T = G.sim3_exp(np.array(xi))
+    np.testing.assert_allclose(G.from13(lsdg.sim3_exp13(xi)), T, atol=1e-11)
+    np.testing.assert_allclose(G.sim3_exp(lsdg.sim3_log13(G.to13(T))), T, atol=1e-9)
+
+
+def _both(truth_nodes, edges):
+    py = G.PoseGraph()
+    cg = lsdg.NativePoseGraph()
+    for T in truth_nodes:
+        py.add_node(T)
+        cg.add_node(G.to13(T))
+    for i, j, Z, W in edges:
+        py.add_edge(i, j, Z, W)
+        cg.add_edge(i, j, G.to13(Z), W)
+    return py, cg
+
+
+def test_consistent_chain_recovered_like_numpy():
+    rng = np.random.default_rng(1)
+    truth = [np.eye(4)]
+    for _ in range(6):
+        truth.append(truth[-1] @ rand_sim3(rng, trans=0.3, angle=0.2)[0])
+    start = [truth[0]] + [truth[k] @ rand_sim3(rng, (0.9, 1.1), 0.1, 0.05)[0] for k in range(1, len(truth))]
+    edges = [(k - 1, k, G.sim3_inv(truth[k - 1]) @ truth[k], np.eye(7)) for k in range(1, len(truth))]
+    edges.append((0, 3, G.sim3_inv(truth[0]) @ truth[3], np.eye(7)))
+    py, cg = _both(start, edges)
+    assert cg.optimize(30) < 1e-16
+    py.optimize(30)
+    for k in range(len(truth)):
+        np.testing.assert_allclose(G.from13(cg.pose(k)), truth[k], atol=1e-7)
+        np.testing.assert_allclose(G.from13(cg.pose(k)), py.poses[k], atol=1e-7)
+    cg.close()
+
+
+def test_loop_edge_and_huber_like_numpy():
+    n = 12
+    truth = [np.eye(4)]
+    step = G.sim3_exp(np.array([0.3, 0, 0, 0, 2 * math.pi / n, 0, 0]))
+    for _ in range(n):
+        truth.append(truth[-1] @ step)
+    drift = G.sim3_exp(np.array([0.01, 0, 0, 0, 0.01, 0, 0.02]))
+    nodes, edges = [truth[0]], []
+    for k in range(1, n + 1):
+        Z = G.sim3_inv(truth[k - 1]) @ truth[k] @ drift
+        nodes.append(nodes[-1] @ Z)
+        edges.append((k - 1, k, Z, np.eye(7)))
+    edges.append((0, n, G.sim3_inv(truth[0]) @ truth[n], 100 * np.eye(7)))
+    edges.append((0, 5, G.sim3_exp(np.array([3.0, 0, 0, 1.0, 0, 0, 0.5])), 1e2 * np.eye(7)))  # wrong
+    py, cg = _both(nodes, edges)
+    c_py = py.optimize(30)
+    c_cg = cg.optimize(30)
+    assert c_cg == pytest.approx(c_py, rel=1e-6)
+    for k in range(n + 1):
+        np.testing.assert_allclose(G.from13(cg.pose(k)), py.poses[k], atol=1e-6)
+    before = np.linalg.norm(nodes[n][:3, 3] - truth[n][:3, 3])
+    after = np.linalg.norm(G.from13(cg.pose(n))[:3, 3] - truth[n][:3, 3])
+    assert after < 0.1 * before
+    cg.close()
+
+
+def test_large_graph_uses_the_threaded_factorisation():
+    """A 200-node graph (1,393 unknowns: several 64-column blocks, threaded trailing updates)."""
+    rng = np.random.default_rng(7)
+    truth = [np.eye(4)]
+    for _ in range(199):
+        truth.append(truth[-1] @ rand_sim3(rng, (0.98, 1.02), 0.1, 0.05)[0])
+    start = [truth[0]] + [T @ rand_sim3(rng, (0.99, 1.01), 0.01, 0.01)[0] for T in truth[1:]]
+    edges = [(k - 1, k, G.sim3_inv(truth[k - 1]) @ truth[k], np.eye(7)) for k in range(1, 200)]
+    edges += [(k - 7, k, G.sim3_inv(truth[k - 7]) @ truth[k], np.eye(7)) for k in range(7, 200, 3)]
+    _, cg = _both(start, edges)
+    assert cg.optimize(20) < 1e-14
+    for k in (50, 120, 199):
+        np.testing.assert_allclose(G.from13(cg.pose(k)), truth[k], atol=1e-6)
+    cg.close()
