@@ -621,7 +621,11 @@ typedef struct lsdg_slam_params {
   float consistency_scale;  /* ... |log scale| below this                                         */
   int32_t async_constraints; /* constraint search on the worker thread (1) or inline (0)          */
   int32_t graph_threads;    /* host threads of the pose graph's Cholesky                           */
-  int32_t reserved[8];
+  float odometry_scale_weight; /* scale information of a keyframe-to-keyframe odometry edge, as a
+                                  fraction of its strongest SE3 direction                          */
+  int32_t ref_min_validity; /* tracking reference: only depth whose validity count reaches this    */
+  float sim3_info_scale;    /* information of a Sim3 constraint = the tracker's J^T W J times this */
+  int32_t reserved[5];
 } lsdg_slam_params;
 
 typedef struct lsdg_slam_stats {

@@ -78,6 +78,7 @@ struct lsdg_slam {
   int loops_pending = 0;
   lsdg_slam_stats stats{};
   std::vector<float> d_buf, v_buf;
+  std::vector<int32_t> val_buf;
   std::string err;
 };
 
@@ -122,8 +123,15 @@ bool finite(const M4& T) {
 }
 
 // The depth map's smoothed inverse depth and variance (the planes the viewer reads) into a frame.
+// With ref_min_validity > 0, hypotheses observed fewer times than that stay out (not applied to the
+// bootstrap keyframe, whose depth has no history).
 lsdg_status reference_depth(lsdg_slam* s, lsdg_frame* f) {
-  SLAM_CK(s, lsdg_depth_get(s->ctx, s->dm, nullptr, nullptr, s->d_buf.data(), s->v_buf.data(), nullptr, nullptr), s->ctx);
+  const bool gate = s->sp.ref_min_validity > 0 && !s->keyframes.empty();
+  SLAM_CK(s, lsdg_depth_get(s->ctx, s->dm, nullptr, nullptr, s->d_buf.data(), s->v_buf.data(),
+                            gate ? s->val_buf.data() : nullptr, nullptr), s->ctx);
+  if (gate)
+    for (size_t i = 0; i < s->d_buf.size(); ++i)
+      if (s->val_buf[i] < s->sp.ref_min_validity) s->d_buf[i] = -1.0f;
   SLAM_CK(s, lsdg_frame_set_depth(s->ctx, f, s->d_buf.data(), s->v_buf.data()), s->ctx);
   return LSDG_OK;
 }
@@ -237,7 +245,7 @@ lsdg_status constraint_job(lsdg_slam* s, int k) {
       s->stats.sim3_rejected++;
       continue;
     }
-    for (double& v : H) v *= 1e-3;
+    for (double& v : H) v *= s->sp.sim3_info_scale;
     s->graph.add_edge(s->keyframes[cands[i]].node, kn.node, Z, H);
     s->stats.sim3_edges++;
     loop = loop || cands[i] != k - 1;
@@ -340,7 +348,7 @@ lsdg_status new_keyframe(lsdg_slam* s, int frame_index, const uint8_t* image, co
     std::memset(W, 0, sizeof(W));
     for (int i = 0; i < 6; ++i)
       for (int j = 0; j < 6; ++j) W[7 * i + j] = H6[6 * i + j] * 1e-3;
-    W[48] = dmax * 1e-3;
+    W[48] = dmax * 1e-3 * s->sp.odometry_scale_weight;
     s->graph.add_edge(prev_node, kf.node, f2k, W);
   }
   s->stats.keyframes = (int)s->keyframes.size();
@@ -369,6 +377,9 @@ void lsdg_slam_default_params(lsdg_slam_params* p) {
   p->consistency_scale = 0.02f;
   p->async_constraints = 1;
   p->graph_threads = 8;
+  p->odometry_scale_weight = 1.0f;
+  p->ref_min_validity = 0;
+  p->sim3_info_scale = 1e-3f;
 }
 
 lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* sp, int device, int width, int height,
@@ -387,6 +398,7 @@ lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* 
   s->graph.threads = std::max(1, s->sp.graph_threads);
   s->d_buf.resize((size_t)width * height);
   s->v_buf.resize((size_t)width * height);
+  s->val_buf.resize((size_t)width * height);
   lsdg_status st = lsdg_create(&s->ctx, &s->params, device);
   if (st == LSDG_OK) st = lsdg_create(&s->ctx_cons, &s->params, device);
   if (st == LSDG_OK) st = lsdg_depth_create(s->ctx, width, height, intr, &s->dm);

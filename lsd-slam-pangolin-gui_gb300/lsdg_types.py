@@ -132,7 +132,8 @@ class SlamParams(C.Structure):
         ("optimize_every", C.c_int32), ("final_iterations", C.c_int32), ("max_track_jump", C.c_float),
         ("both_directions", C.c_int32), ("consistency_trans", C.c_float), ("consistency_rot", C.c_float),
         ("consistency_scale", C.c_float), ("async_constraints", C.c_int32), ("graph_threads", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("odometry_scale_weight", C.c_float), ("ref_min_validity", C.c_int32), ("sim3_info_scale", C.c_float),
+        ("reserved", C.c_int32 * 5),
     ]
 
 
