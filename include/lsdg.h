@@ -672,6 +672,16 @@ LSDG_API void lsdg_sim3_exp13(const double xi[7], double out13[13]);
 LSDG_API void lsdg_sim3_log13(const double pose13[13], double xi[7]);
 
 /* ------------------------------------------------------------------------------------------ */
+/* Measurement                                                                                 */
+/* ------------------------------------------------------------------------------------------ */
+
+/* L2 read bandwidth of an L2-resident working set on the context's GPU (GB/s): a persistent grid
+ * re-reads a `bytes` buffer `reps` times with L2-only loads (no counterpart in the reference; the
+ * denominator of the L2-side roofline of the tracker, whose re-reads across passes L2 serves).
+ * Allocates and frees its buffer; synchronises the context stream. */
+LSDG_API lsdg_status lsdg_measure_l2_read(lsdg_ctx* ctx, long bytes, int reps, double* gbps);
+
+/* ------------------------------------------------------------------------------------------ */
 /* Autotuner                                                                                   */
 /* ------------------------------------------------------------------------------------------ */
 

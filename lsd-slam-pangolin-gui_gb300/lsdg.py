@@ -148,6 +148,7 @@ def lib():
     _sig(L, "lsdg_posegraph_get_pose", st, [_vp, C.c_int, _f64p])
     _sig(L, "lsdg_sim3_exp13", None, [_f64p, _f64p])
     _sig(L, "lsdg_sim3_log13", None, [_f64p, _f64p])
+    _sig(L, "lsdg_measure_l2_read", st, [_vp, C.c_long, C.c_int, C.POINTER(C.c_double)])
     _lib = L
     return L
 
@@ -772,6 +773,13 @@ def cloud_build(ctx: Context, points, w: int, h: int, fx, fy, cx, cy, scale: flo
                                      None if params is None else C.byref(params), pts.ctypes.data, out.ctypes.data,
                                      C.byref(n)))
     return out[:n.value].copy()
+
+
+def measure_l2_read(ctx: "Context", bytes_: int = 32 << 20, reps: int = 50) -> float:
+    """L2 read bandwidth (GB/s) of an L2-resident buffer on the context's GPU."""
+    g = C.c_double()
+    ctx.check(lib().lsdg_measure_l2_read(ctx.handle, bytes_, reps, C.byref(g)))
+    return g.value
 
 
 def slam_default_params() -> T.SlamParams:
