@@ -625,7 +625,8 @@ typedef struct lsdg_slam_params {
                                   fraction of its strongest SE3 direction                          */
   int32_t ref_min_validity; /* tracking reference: only depth whose validity count reaches this    */
   float sim3_info_scale;    /* information of a Sim3 constraint = the tracker's J^T W J times this */
-  int32_t reserved[5];
+  float ref_max_var;        /* tracking reference: only depth whose variance is below this (0 = all) */
+  int32_t reserved[4];
 } lsdg_slam_params;
 
 typedef struct lsdg_slam_stats {

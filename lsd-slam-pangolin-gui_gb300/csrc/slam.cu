@@ -123,8 +123,8 @@ bool finite(const M4& T) {
 }
 
 // The depth map's smoothed inverse depth and variance (the planes the viewer reads) into a frame.
-// With ref_min_validity > 0, hypotheses observed fewer times than that stay out (not applied to the
-// bootstrap keyframe, whose depth has no history).
+// With ref_min_validity > 0, hypotheses observed fewer times than that stay out, and with
+// ref_max_var > 0 those less certain than that (neither applies to the bootstrap keyframe).
 lsdg_status reference_depth(lsdg_slam* s, lsdg_frame* f) {
   const bool gate = s->sp.ref_min_validity > 0 && !s->keyframes.empty();
   SLAM_CK(s, lsdg_depth_get(s->ctx, s->dm, nullptr, nullptr, s->d_buf.data(), s->v_buf.data(),
@@ -132,6 +132,9 @@ lsdg_status reference_depth(lsdg_slam* s, lsdg_frame* f) {
   if (gate)
     for (size_t i = 0; i < s->d_buf.size(); ++i)
       if (s->val_buf[i] < s->sp.ref_min_validity) s->d_buf[i] = -1.0f;
+  if (s->sp.ref_max_var > 0.0f && !s->keyframes.empty())
+    for (size_t i = 0; i < s->d_buf.size(); ++i)
+      if (!(s->v_buf[i] < s->sp.ref_max_var)) s->d_buf[i] = -1.0f;
   SLAM_CK(s, lsdg_frame_set_depth(s->ctx, f, s->d_buf.data(), s->v_buf.data()), s->ctx);
   return LSDG_OK;
 }

@@ -80,9 +80,13 @@ def run(seq, frames, n_frames=None, params=None, slam_params=None, device=0, pos
     bad = np.nonzero(~finite)[0]
     ate, (s, _, _) = ate_rmse(est_c[finite], gt_c[finite]) if finite.sum() >= 3 else (float("nan"), (0.0, 0, 0))
     path = float(np.sum(np.linalg.norm(np.diff(gt_c, axis=0), axis=1)))
+    # the ground truth's own RMS spread about its centroid: a trajectory collapsed to its mean scores
+    # this ATE, so the ATE means something only well below it
+    spread = float(np.sqrt(np.mean(np.sum((gt_c - gt_c.mean(0)) ** 2, axis=1))))
     return {"frames": n, "seconds": wall, "fps": n / wall, "keyframes": stats["keyframes"],
             "sim3_edges": stats["sim3_edges"], "sim3_rejected": stats["sim3_rejected"],
             "lost_frames": stats["lost_frames"], "graph_optimisations": stats["graph_optimisations"],
             "keyframe_graph_nodes": len(graph), "ate_rmse_m": ate, "path_m": path,
-            "ate_over_path": ate / max(path, 1e-9), "alignment_scale": s,
+            "ate_over_path": ate / max(path, 1e-9), "gt_spread_m": spread, "ate_over_gt_spread": ate / max(spread, 1e-9),
+            "alignment_scale": s,
             "non_finite_frames": int(len(bad)), "first_non_finite": int(bad[0]) if len(bad) else -1}
