@@ -25,6 +25,7 @@ def test_room_sequence_320x240(tmp_path):
     res = sequence.run(seq, frames, pose_file=str(tmp_path / "pose.txt"))
     _check(res, 240)
     assert res["ate_over_path"] < 0.05, res
+    assert res["ate_over_gt_spread"] < 0.35, res   # well below a trajectory collapsed to its mean
     assert 0.85 < res["alignment_scale"] < 1.15, res
     rows = (tmp_path / "pose.txt").read_text().splitlines()
     assert len(rows) == 240 and rows[0].startswith("0,") and all(len(r.split(",")) == 7 for r in rows)
@@ -36,6 +37,7 @@ def test_room_sequence_640x480():
     res = sequence.run(seq, frames)
     _check(res, 240)
     assert res["ate_over_path"] < 0.05, res
+    assert res["ate_over_gt_spread"] < 0.35, res
 
 
 def test_inline_constraints_equal_worker_thread():
