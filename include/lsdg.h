@@ -654,6 +654,10 @@ LSDG_API lsdg_status lsdg_slam_get_stats(const lsdg_slam* s, lsdg_slam_stats* ou
 LSDG_API lsdg_status lsdg_slam_get_poses(lsdg_slam* s, double* cam_to_world, int capacity, int* n);
 /* The keyframe graph as publishKeyframeGraph hands it out (GraphFramePose: id + Sophus 7 floats). */
 LSDG_API lsdg_status lsdg_slam_keyframe_graph(lsdg_slam* s, lsdg_graph_frame_pose* out, int capacity, int* n);
+/* Keyframe k's level-0 tracking depth (inverse depth and variance, width x height, idepth <= 0 =
+ * none) and the id of the frame it was made from: what publishKeyframe hands the viewer
+ * (PangolinOutputIOWrapper.cpp:77-89).  The current keyframe's is its latest refresh. */
+LSDG_API lsdg_status lsdg_slam_keyframe_depth(lsdg_slam* s, int k, int* frame_id, float* idepth, float* var);
 /* One TextOutputIOWrapper pose row per frame (lsdg_format_pose_row) into a file. */
 LSDG_API lsdg_status lsdg_slam_write_pose_file(lsdg_slam* s, const char* path);
 

@@ -550,6 +550,16 @@ lsdg_status lsdg_slam_keyframe_graph(lsdg_slam* s, lsdg_graph_frame_pose* out, i
   return LSDG_OK;
 }
 
+lsdg_status lsdg_slam_keyframe_depth(lsdg_slam* s, int k, int* frame_id, float* idepth, float* var) {
+  if (!s || !idepth || !var) return LSDG_INVALID_ARG;
+  lsdg_status r = join_worker(s);
+  if (r != LSDG_OK) return r;
+  if (k < 0 || k >= (int)s->keyframes.size()) return fail(s, LSDG_INVALID_ARG, "keyframe index out of range");
+  if (frame_id) *frame_id = s->traj_id[s->keyframes[k].frame_index];
+  SLAM_CK(s, lsdg_frame_get_depth(s->ctx, s->keyframes[k].frame, 0, idepth, var), s->ctx);
+  return LSDG_OK;
+}
+
 lsdg_status lsdg_slam_write_pose_file(lsdg_slam* s, const char* path) {
   if (!s || !path) return LSDG_INVALID_ARG;
   lsdg_status r = join_worker(s);

@@ -140,6 +140,7 @@ def lib():
     _sig(L, "lsdg_slam_get_poses", st, [_vp, _vp, C.c_int, C.POINTER(C.c_int)])
     _sig(L, "lsdg_slam_keyframe_graph", st, [_vp, _vp, C.c_int, C.POINTER(C.c_int)])
     _sig(L, "lsdg_slam_write_pose_file", st, [_vp, C.c_char_p])
+    _sig(L, "lsdg_slam_keyframe_depth", st, [_vp, C.c_int, C.POINTER(C.c_int), _f32p, _f32p])
     _sig(L, "lsdg_posegraph_create", st, [C.POINTER(_vp)])
     _sig(L, "lsdg_posegraph_destroy", st, [_vp])
     _sig(L, "lsdg_posegraph_add_node", C.c_int, [_vp, _f64p])
@@ -837,6 +838,14 @@ class SlamSystem:
         arr = (T.GraphFramePose * n.value)()
         self._check(lib().lsdg_slam_keyframe_graph(self._h, C.cast(arr, _vp), n.value, C.byref(n)))
         return [(g.id, np.array(g.cam_to_world[:], np.float32)) for g in arr]
+
+    def keyframe_depth(self, k: int):
+        """(frame id, inverse depth [h, w], variance [h, w]) of keyframe k."""
+        fid = C.c_int()
+        d = np.zeros((self.h, self.w), np.float32)
+        v = np.zeros((self.h, self.w), np.float32)
+        self._check(lib().lsdg_slam_keyframe_depth(self._h, k, C.byref(fid), d, v))
+        return fid.value, d, v
 
     def write_pose_file(self, path: str):
         self._check(lib().lsdg_slam_write_pose_file(self._h, path.encode()))
