@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -86,10 +87,148 @@ __device__ __forceinline__ float bilinear_key(const float4* K, int w, float x, f
   return (((bx * by) * __ldg(p).x + (ax * by) * __ldg(p + 1).x) + (bx * ay) * __ldg(p + w).x) + (ax * ay) * __ldg(p + w + 1).x;
 }
 
+// The 5-sample SSD search along the reference epipolar segment: windows s = 0..n centred at
+// pf + s lr, the best (s1, e1), its neighbours' SSDs (ebefore, eafter) and the second best e2 of the
+// online rule (a window counts for e2 when it is at least 2 windows from the best standing when it
+// is met, or when it was the best and a better one appears at least 2 windows later).
+struct SearchResult {
+  float e1, e2, ebefore, eafter;
+  int s1;
+};
+
+__device__ __forceinline__ SearchResult search_seq(const float* __restrict__ Ir, int w, float umax, float vmax,
+                                                   float pfx, float pfy, float lrx, float lry, int n,
+                                                   const float (&tk)[5]) {
+  const float INF = __int_as_float(0x7f800000);
+  float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, r4 = 0.f;
+  bool o0 = false, o1 = false, o2 = false, o3 = false, o4 = false;
+  float e1 = INF, e2 = INF, eprev = INF, ebefore = INF, eafter = INF;
+  int s1 = -1;
+  for (int j = -2; j <= n + 2; ++j) {
+    r0 = r1; r1 = r2; r2 = r3; r3 = r4;
+    o0 = o1; o1 = o2; o2 = o3; o3 = o4;
+    const float sx = pfx + (float)j * lrx, sy = pfy + (float)j * lry;
+    o4 = sx >= 0.f && sy >= 0.f && sx < umax && sy < vmax;
+    r4 = o4 ? bilinear_plane(Ir, w, sx, sy) : 0.f;
+    if (j < 2) continue;
+    const int s = j - 2;
+    float e = INF;
+    if (o0 && o1 && o2 && o3 && o4) {
+      const float d0 = r0 - tk[0], d1 = r1 - tk[1], d2 = r2 - tk[2], d3 = r3 - tk[3], d4 = r4 - tk[4];
+      e = (((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3) + d4 * d4;
+    }
+    if (e < e1) {
+      if (s1 >= 0 && s - s1 >= 2 && e1 < e2) e2 = e1;
+      ebefore = eprev;
+      e1 = e;
+      s1 = s;
+      eafter = INF;
+    } else {
+      if (s == s1 + 1) eafter = e;
+      if (s - s1 >= 2 && e < e2) e2 = e;
+    }
+    eprev = e;
+  }
+  return SearchResult{e1, e2, ebefore, eafter, s1};
+}
+
+// The same search shared by the G lanes of a group (lane u of G, `mask` the group's lanes, `buf`
+// 2 * kSplitCap floats of the group's shared memory), with the same results bit for bit: the samples
+// (INF outside the image) and the window SSDs are computed in parallel with the same operations;
+// then each lane takes a contiguous chunk of windows.  The best standing before a window is a prefix
+// minimum (earliest index on ties, as the strict comparison of the online rule keeps it), so every
+// lane learns the best before its chunk from the lanes before it, walks its chunk with the online
+// rule's two eligibility tests, and e2 is the minimum over the lanes -- a minimum, like the online
+// rule's assignments, so its value does not depend on the order of the candidates.
+constexpr int kSplitCap = 128;  // samples per segment the split search holds (n + 5)
+
+template <int G>
+__device__ __forceinline__ SearchResult search_split(const float* __restrict__ Ir, int w, float umax, float vmax,
+                                                     float pfx, float pfy, float lrx, float lry, int n,
+                                                     const float (&tk)[5], int u, int lane0, unsigned mask,
+                                                     float* __restrict__ buf) {
+  const float INF = __int_as_float(0x7f800000);
+  float* samp = buf;
+  float* es = buf + kSplitCap;
+  for (int j = -2 + u; j <= n + 2; j += G) {
+    const float sx = pfx + (float)j * lrx, sy = pfy + (float)j * lry;
+    const bool ok = sx >= 0.f && sy >= 0.f && sx < umax && sy < vmax;
+    samp[j + 2] = ok ? bilinear_plane(Ir, w, sx, sy) : INF;
+  }
+  __syncwarp(mask);
+  for (int s = u; s <= n; s += G) {
+    const float r0 = samp[s], r1 = samp[s + 1], r2 = samp[s + 2], r3 = samp[s + 3], r4 = samp[s + 4];
+    float e = INF;
+    if (r0 < INF && r1 < INF && r2 < INF && r3 < INF && r4 < INF) {  // all five inside the image
+      const float d0 = r0 - tk[0], d1 = r1 - tk[1], d2 = r2 - tk[2], d3 = r3 - tk[3], d4 = r4 - tk[4];
+      e = (((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3) + d4 * d4;
+    }
+    es[s] = e;
+  }
+  __syncwarp(mask);
+  const int nw = n + 1;
+  const int chunk = (nw + G - 1) / G;
+  const int c0 = min(nw, u * chunk), c1 = min(nw, c0 + chunk);
+  float cm = INF;  // this chunk's best, first occurrence
+  int ci = -1;
+  for (int s = c0; s < c1; ++s) {
+    const float e = es[s];
+    if (e < cm) {
+      cm = e;
+      ci = s;
+    }
+  }
+  float pm = INF, e1 = INF;  // best before this chunk; best overall
+  int pi = -1, s1 = -1;
+#pragma unroll
+  for (int v = 0; v < G; ++v) {
+    const float vm = __shfl_sync(mask, cm, lane0 + v);
+    const int vi = __shfl_sync(mask, ci, lane0 + v);
+    if (v < u && vm < pm) {
+      pm = vm;
+      pi = vi;
+    }
+    if (vm < e1) {
+      e1 = vm;
+      s1 = vi;
+    }
+  }
+  float e2l = INF;
+  float cur = pm;
+  int curi = pi;
+  for (int s = c0; s < c1; ++s) {
+    const float e = es[s];
+    if (e < cur) {
+      if (curi >= 0 && s - curi >= 2 && cur < e2l) e2l = cur;
+      cur = e;
+      curi = s;
+    } else if (s - curi >= 2 && e < e2l) {
+      e2l = e;
+    }
+  }
+  float e2 = INF;
+#pragma unroll
+  for (int v = 0; v < G; ++v) {
+    const float x = __shfl_sync(mask, e2l, lane0 + v);
+    if (x < e2) e2 = x;
+  }
+  SearchResult r;
+  r.e1 = e1;
+  r.e2 = e2;
+  r.s1 = s1;
+  r.ebefore = s1 >= 1 ? es[s1 - 1] : INF;
+  r.eafter = (s1 >= 0 && s1 < n) ? es[s1 + 1] : INF;
+  __syncwarp(mask);  // the buffer is rewritten by the next search
+  return r;
+}
+
 // observeDepth of one pixel against one reference: the same operations, in the same order, as the
-// CPU oracle's observe_pixel.
+// CPU oracle's observe_pixel.  G > 1: the G lanes of a group run it together, each with the whole
+// state, sharing the epipolar search (search_split); G = 1: one lane per pixel.
+template <int NG>
 __device__ void observe_one(const ObserveArgs& A, const RefGeomF& G, const float* __restrict__ Ir, int x, int y,
-                            float gx, float gy, float& d, float& var, int& val, int& bl) {
+                            float gx, float gy, float& d, float& var, int& val, int& bl, int u = 0, int lane0 = 0,
+                            unsigned mask = 0xffffffffu, float* buf = nullptr) {
   const int w = A.w, h = A.h;
   const float g2 = gx * gx + gy * gy;
   const float mg = A.min_grad;
@@ -157,35 +296,11 @@ __device__ void observe_one(const ObserveArgs& A, const RefGeomF& G, const float
   const int n = (int)L;
   const float INF = __int_as_float(0x7f800000);
   const float umax = (float)(w - 1), vmax = (float)(h - 1);
-  float r0 = 0.f, r1 = 0.f, r2 = 0.f, r3 = 0.f, r4 = 0.f;
-  bool o0 = false, o1 = false, o2 = false, o3 = false, o4 = false;
-  float e1 = INF, e2 = INF, eprev = INF, ebefore = INF, eafter = INF;
-  int s1 = -1;
-  for (int j = -2; j <= n + 2; ++j) {
-    r0 = r1; r1 = r2; r2 = r3; r3 = r4;
-    o0 = o1; o1 = o2; o2 = o3; o3 = o4;
-    const float sx = pfx + (float)j * lrx, sy = pfy + (float)j * lry;
-    o4 = sx >= 0.f && sy >= 0.f && sx < umax && sy < vmax;
-    r4 = o4 ? bilinear_plane(Ir, w, sx, sy) : 0.f;
-    if (j < 2) continue;
-    const int s = j - 2;
-    float e = INF;
-    if (o0 && o1 && o2 && o3 && o4) {
-      const float d0 = r0 - tk[0], d1 = r1 - tk[1], d2 = r2 - tk[2], d3 = r3 - tk[3], d4 = r4 - tk[4];
-      e = (((d0 * d0 + d1 * d1) + d2 * d2) + d3 * d3) + d4 * d4;
-    }
-    if (e < e1) {
-      if (s1 >= 0 && s - s1 >= 2 && e1 < e2) e2 = e1;
-      ebefore = eprev;
-      e1 = e;
-      s1 = s;
-      eafter = INF;
-    } else {
-      if (s == s1 + 1) eafter = e;
-      if (s - s1 >= 2 && e < e2) e2 = e;
-    }
-    eprev = e;
-  }
+  SearchResult sr;
+  if (NG > 1 && n + 5 <= kSplitCap) sr = search_split<NG>(Ir, w, umax, vmax, pfx, pfy, lrx, lry, n, tk, u, lane0, mask, buf);
+  else sr = search_seq(Ir, w, umax, vmax, pfx, pfy, lrx, lry, n, tk);
+  const float e1 = sr.e1, e2 = sr.e2, ebefore = sr.ebefore, eafter = sr.eafter;
+  const int s1 = sr.s1;
   if (s1 < 0) return;
   if (e1 > A.max_ssd * 5.f) {
     ++bl;
@@ -267,8 +382,11 @@ __global__ void __launch_bounds__(256) depth_worklist_kernel(const float4* __res
   if (ok) list[base + __popc(m & ((1u << lane) - 1u))] = i;
 }
 
-// observeDepth of keyframe pixel i against every reference in order (its state in registers).
-__device__ __forceinline__ void observe_pixel_all(const ObserveArgs& A, int i) {
+// observeDepth of keyframe pixel i against every reference in order (its state in registers; with
+// NG > 1 every lane of the pixel's group holds it and the writes come from lane u = 0).
+template <int NG>
+__device__ __forceinline__ void observe_pixel_all(const ObserveArgs& A, int i, int u = 0, int lane0 = 0,
+                                                  unsigned mask = 0xffffffffu, float* buf = nullptr) {
   const int w = A.w;
   const int y = i / w, x = i - y * w;
   const float4 kp = __ldg(&A.key[i]);
@@ -279,12 +397,14 @@ __device__ __forceinline__ void observe_pixel_all(const ObserveArgs& A, int i) {
   const size_t plane = (size_t)w * A.h;
   for (int r = 0; r < A.n_refs; ++r) {
     if (bl >= A.blacklist_limit) break;
-    observe_one(A, A.geom[r], A.refs + plane * r, x, y, kp.y, kp.z, d, var, val, bl);
+    observe_one<NG>(A, A.geom[r], A.refs + plane * r, x, y, kp.y, kp.z, d, var, val, bl, u, lane0, mask, buf);
   }
-  A.st.d[i] = d;
-  A.st.v[i] = var;
-  A.st.val[i] = val;
-  A.st.bl[i] = bl;
+  if (u == 0) {
+    A.st.d[i] = d;
+    A.st.v[i] = var;
+    A.st.val[i] = val;
+    A.st.bl[i] = bl;
+  }
 }
 
 // A persistent grid over the work list: each warp takes the next 32 listed pixels (one atomic),
@@ -301,7 +421,29 @@ __global__ void __launch_bounds__(128) depth_observe_kernel(const ObserveArgs A,
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= n) break;
     const int t = base + lane;
-    if (t < n) observe_pixel_all(A, __ldg(&list[t]));
+    if (t < n) observe_pixel_all<1>(A, __ldg(&list[t]));
+  }
+}
+
+// The same over groups of NG lanes per listed pixel: a warp takes 32 / NG pixels at a time and each
+// group shares its pixel's epipolar searches (search_split), so a pixel's chain of dependent samples
+// is NG times shorter.
+template <int NG>
+__global__ void __launch_bounds__(128) depth_observe_split_kernel(const ObserveArgs A, const int* __restrict__ list,
+                                                                  int* __restrict__ counters) {
+  constexpr int PPW = 32 / NG;
+  __shared__ float buf[4][PPW][2 * kSplitCap];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gi = lane / NG, u = lane % NG, lane0 = gi * NG;
+  const unsigned mask = (NG == 32) ? 0xffffffffu : (((1u << NG) - 1u) << lane0);
+  const int n = *reinterpret_cast<volatile const int*>(&counters[0]);
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&counters[1], PPW);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= n) break;
+    const int t = base + gi;
+    if (t < n) observe_pixel_all<NG>(A, __ldg(&list[t]), u, lane0, mask, buf[wid][gi]);
   }
 }
 
@@ -678,17 +820,32 @@ lsdg_status lsdg_depth_update_loaded(lsdg_ctx* ctx, lsdg_depthmap* dm, int n_ref
   CK(ctx, cudaMemsetAsync(dm->counters, 0, 2 * sizeof(int), ctx->stream));
   depth_worklist_kernel<<<(npix + 255) / 256, 256, 0, ctx->stream>>>(A.key, dm->w, dm->h, p.min_grad, dm->work,
                                                                        dm->counters);
+  // Lanes per listed pixel: 4 (a group shares each epipolar search; measured fastest of 1, 2, 4, 8 at
+  // 640x480); LSDG_OBSERVE_GROUP=1|2|4|8 pins another form (used to profile them side by side; results
+  // are the same bit for bit).
+  static const int group = [] {
+    const char* e = std::getenv("LSDG_OBSERVE_GROUP");
+    const int g = e ? std::atoi(e) : 4;
+    return (g == 1 || g == 2 || g == 4 || g == 8) ? g : 4;
+  }();
   // resident CTAs of the observe kernel per SM (a property of the kernel on this architecture)
-  static const int per_sm = [] {
+  auto occupancy = [](const void* k) {
     int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, depth_observe_kernel, 128, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 128, 0) != cudaSuccess) {
       cudaGetLastError();
       b = 4;
     }
     return b > 0 ? b : 1;
-  }();
-  depth_observe_kernel<<<per_sm * (ctx->sm_count > 0 ? ctx->sm_count : 1), 128, 0, ctx->stream>>>(A, dm->work,
-                                                                                               dm->counters);
+  };
+  static const int per_sm1 = occupancy((const void*)depth_observe_kernel);
+  static const int per_sm4 = occupancy((const void*)depth_observe_split_kernel<4>);
+  static const int per_sm8 = occupancy((const void*)depth_observe_split_kernel<8>);
+  static const int per_sm2 = occupancy((const void*)depth_observe_split_kernel<2>);
+  const int sms = ctx->sm_count > 0 ? ctx->sm_count : 1;
+  if (group == 1) depth_observe_kernel<<<per_sm1 * sms, 128, 0, ctx->stream>>>(A, dm->work, dm->counters);
+  else if (group == 2) depth_observe_split_kernel<2><<<per_sm2 * sms, 128, 0, ctx->stream>>>(A, dm->work, dm->counters);
+  else if (group == 4) depth_observe_split_kernel<4><<<per_sm4 * sms, 128, 0, ctx->stream>>>(A, dm->work, dm->counters);
+  else depth_observe_split_kernel<8><<<per_sm8 * sms, 128, 0, ctx->stream>>>(A, dm->work, dm->counters);
   ctx->launches += 2;
   CK(ctx, cudaGetLastError());
   if (regularize) return enqueue_regularize(ctx, dm);
