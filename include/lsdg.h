@@ -555,7 +555,9 @@ LSDG_API lsdg_status lsdg_depth_export_points(lsdg_ctx* ctx, lsdg_depthmap* dm, 
 /* Keyframe::computeVbo (lib/Pangolin_IOWrapper/Keyframe.h:66-143) without OpenGL: the points of a
  * w x h InputPointDense array (host) that pass the variance and neighbour-support filter,
  * back-projected with (fx, fy, cx, cy) and the keyframe's Sim3 scale, in row-major order into `out`
- * (host, capacity w * h vertices); *count = the number of vertices (Keyframe::points). */
+ * (host, capacity w * h vertices); *count = the number of vertices (Keyframe::points).  An array
+ * with fewer than 3 rows or columns has no interior pixel: *count = 0, as computeVbo's loop keeps
+ * nothing. */
 LSDG_API lsdg_status lsdg_cloud_build(lsdg_ctx* ctx, int w, int h, float fx, float fy, float cx, float cy,
                                       float scale, const lsdg_cloud_params* params,
                                       const lsdg_input_point_dense* points, lsdg_cloud_vertex* out,

@@ -248,6 +248,10 @@ lsdg_status lsdg_cloud_build(lsdg_ctx* ctx, int w, int h, float fx, float fy, fl
                              const lsdg_cloud_params* params, const lsdg_input_point_dense* points,
                              lsdg_cloud_vertex* out, int* count) {
   if (!ctx || !points || !out || !count) return ctx_fail(ctx, LSDG_INVALID_ARG, "null argument");
+  if (w > 0 && h > 0 && (w < 3 || h < 3)) {  // no interior pixel: computeVbo's loop keeps nothing
+    *count = 0;
+    return LSDG_OK;
+  }
   lsdg_cloud_params p;
   if (params) p = *params;
   else lsdg_cloud_default_params(&p);

@@ -442,6 +442,44 @@ POINT_DENSE = np.dtype([("idepth", "<f4"), ("idepth_var", "<f4"), ("color", "u1"
 CLOUD_VERTEX = np.dtype([("point", "<f4", (3,)), ("color", "u1", (4,))])
 
 
+_ref_lib = None
+
+
+def ref_lib():
+    """The reference's own Keyframe::computeVbo loop compiled from its source (oracle/_ref, built by
+    oracle/ref_build.py), or None where neither the reference tree nor its generated source is
+    present."""
+    global _ref_lib
+    if _ref_lib is None:
+        sys.path.insert(0, HERE)
+        import ref_build as _rb  # oracle/ref_build.py
+        path = _rb.build()
+        if path is None:
+            return None
+        L = C.CDLL(path)
+        L.ref_compute_vbo.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                      C.c_void_p, C.c_void_p]
+        L.ref_compute_vbo.restype = C.c_int
+        a, b = C.c_int(), C.c_int()
+        L.ref_sizes(C.byref(a), C.byref(b))
+        assert (a.value, b.value) == (POINT_DENSE.itemsize, CLOUD_VERTEX.itemsize)
+        _ref_lib = L
+    return _ref_lib
+
+
+def ref_compute_vbo(points, w, h, fx, fy, cx, cy, scale=1.0):
+    """Vertices computeVbo (the reference's code, its constants) keeps for a w x h InputPointDense
+    array; None without oracle/_ref."""
+    L = ref_lib()
+    if L is None:
+        return None
+    pts = np.ascontiguousarray(points, POINT_DENSE).reshape(-1)
+    assert pts.size == w * h
+    out = np.zeros(w * h, CLOUD_VERTEX)
+    n = L.ref_compute_vbo(w, h, fx, fy, cx, cy, scale, pts.ctypes.data, out.ctypes.data)
+    return out[:n].copy()
+
+
 def cloud_build(points, w, h, fx, fy, cx, cy, scale=1.0, scaled_th=1e-3, abs_th=1e-1, min_near_support=9):
     """Vertices (structured array) of a w x h InputPointDense array (structured, POINT_DENSE)."""
     pts = np.ascontiguousarray(points, POINT_DENSE).reshape(-1)

@@ -1,11 +1,13 @@
 """GPU parity of the keyframe point cloud (Keyframe::computeVbo's filter and back-projection,
-publishKeyframe's export) through the C-ABI, bit for bit against the CPU oracle."""
+publishKeyframe's export) through the C-ABI, bit for bit against the CPU oracle and against the
+reference's own computeVbo loop (the committed fixture of its outputs, and the loop compiled from
+Keyframe.h where oracle/_ref is present)."""
 import numpy as np
 import pytest
 
 import lsdo
 import synth
-from test_oracle_cloud import K, H, W, random_keyframe
+from test_oracle_cloud import K, H, W, _edge_keyframes, random_keyframe, reference_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -19,6 +21,26 @@ def test_cloud_build_matches_oracle(ctx, seed, scale):
     ref = lsdo.cloud_build(pts, W, H, *K, scale=scale)
     assert len(got) == len(ref) > 100
     assert got.tobytes() == ref.tobytes()
+
+
+def test_cloud_build_matches_reference_fixture(ctx):
+    import lsdg
+    for pts, w, h, fx, fy, cx, cy, scale, v in reference_cases():
+        got = lsdg.cloud_build(ctx, pts.reshape(-1), w, h, fx, fy, cx, cy, scale=scale)
+        assert len(got) == len(v) > 500
+        assert got.tobytes() == v.tobytes()
+
+
+def test_cloud_build_matches_reference_code(ctx):
+    import lsdg
+    if lsdo.ref_lib() is None:
+        pytest.skip("oracle/_ref not built: the reference tree is absent")
+    cases = [(f"seed {s}", random_keyframe(s + 200, 160, 120), sc) for s in range(2) for sc in (0.5, 4.0)]
+    for name, pts, scale in cases + list(_edge_keyframes()):
+        h, w = pts.shape
+        ref = lsdo.ref_compute_vbo(pts, w, h, *K, scale=scale)
+        got = lsdg.cloud_build(ctx, pts.reshape(-1), w, h, *K, scale=scale)
+        assert got.tobytes() == ref.tobytes(), name
 
 
 def test_cloud_build_full_frame_and_params(ctx):

@@ -134,3 +134,67 @@ def test_matches_numpy_restatement(seed, scale):
     ref = numpy_cloud(pts, *K, scale)
     assert len(got) == len(ref) and len(got) > 100
     assert got.tobytes() == ref.tobytes()
+
+
+def reference_cases():
+    """(points, w, h, fx, fy, cx, cy, scale, vertices) of tests/golden/cloud_ref.npz: outputs of the
+    reference's own computeVbo loop compiled from Keyframe.h (tests/golden/make_cloud_ref.py)."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "cloud_ref.npz"))
+    k = 0
+    cases = []
+    while f"camera{k}" in z:
+        w, h, fx, fy, cx, cy, scale = z[f"camera{k}"]
+        pts = np.frombuffer(z[f"points{k}"].tobytes(), lsdo.POINT_DENSE).reshape(int(h), int(w))
+        v = np.frombuffer(z[f"vertices{k}"].tobytes(), lsdo.CLOUD_VERTEX)
+        cases.append((pts, int(w), int(h), float(fx), float(fy), float(cx), float(cy), float(scale), v))
+        k += 1
+    return cases
+
+
+def test_oracle_matches_reference_fixture():
+    """The oracle against the reference's own loop, through the committed fixture."""
+    cases = reference_cases()
+    assert len(cases) == 3
+    for pts, w, h, fx, fy, cx, cy, scale, v in cases:
+        got = lsdo.cloud_build(pts, w, h, fx, fy, cx, cy, scale=scale)
+        assert len(got) == len(v) > 500
+        assert got.tobytes() == v.tobytes()
+
+
+def _edge_keyframes():
+    rng = np.random.default_rng(11)
+    yield "all holes", dense(np.full((8, 9), -1.0, np.float32), np.full((8, 9), 1e-6, np.float32)), 1.0
+    yield "3x3", dense(np.full((3, 3), 0.5, np.float32), np.full((3, 3), 1e-6, np.float32)), 1.0
+    yield "2 rows", dense(np.full((2, 7), 0.5, np.float32), np.full((2, 7), 1e-6, np.float32)), 1.0
+    yield "zeros and negatives", dense(rng.choice([0.0, -0.0, -2.0, 0.5], size=(12, 10)).astype(np.float32),
+                                       np.full((12, 10), 1e-6, np.float32)), 1.0
+    flat = np.full((16, 16), 0.25, np.float32)
+    var = np.full((16, 16), 1e-3 / 256, np.float32)  # var * depth^4 == 1e-3 exactly at depth 4
+    yield "scaled threshold boundary", dense(flat, var), 1.0
+    yield "absolute threshold boundary", dense(flat, np.full((16, 16), 1e-6, np.float32)), float(np.sqrt(0.1 / 256e-6))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+@pytest.mark.parametrize("scale", [0.25, 1.0, 12.0])
+def test_oracle_matches_reference_code(seed, scale):
+    """The oracle against the reference's own loop compiled from Keyframe.h (oracle/_ref), where the
+    reference tree or its generated source is present: random keyframes and edge cases."""
+    if lsdo.ref_lib() is None:
+        pytest.skip("oracle/_ref not built: the reference tree is absent")
+    w, h = (64, 48) if seed < 2 else (160, 120)
+    pts = random_keyframe(seed + 100, w, h)
+    ref = lsdo.ref_compute_vbo(pts, w, h, *K, scale=scale)
+    got = lsdo.cloud_build(pts, w, h, *K, scale=scale)
+    assert len(got) == len(ref) > 100
+    assert got.tobytes() == ref.tobytes()
+
+
+def test_oracle_matches_reference_code_edges():
+    if lsdo.ref_lib() is None:
+        pytest.skip("oracle/_ref not built: the reference tree is absent")
+    for name, pts, scale in _edge_keyframes():
+        h, w = pts.shape
+        ref = lsdo.ref_compute_vbo(pts, w, h, *K, scale=scale)
+        got = lsdo.cloud_build(pts, w, h, *K, scale=scale)
+        assert got.tobytes() == ref.tobytes(), name
