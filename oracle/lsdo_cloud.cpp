@@ -1,10 +1,11 @@
 // lsdo_cloud.cpp -- CPU ORACLE (test infrastructure only) of the keyframe point cloud the viewer
 // builds: Keyframe::computeVbo's variance / neighbour-support filter and back-projection
 // (lib/Pangolin_IOWrapper/Keyframe.h:66-143; constants at :78-82, support test :113-132,
-// back-projection :134-141), restated without OpenGL.  Keyframe.h includes GLEW and Sophus, which are
-// absent, so the reference's own loop cannot be compiled here; this restatement follows its steps
-// operation for operation (float arithmetic, the order of the products, the colour swizzle), and is
-// compiled without FP contraction like the kernels.
+// back-projection :134-141), restated without OpenGL.  It follows the loop's steps operation for
+// operation (float arithmetic, the order of the products, the colour swizzle), is compiled without FP
+// contraction like the kernels, and is checked byte for byte against the reference's own loop
+// (oracle/ref_build.py compiles it from Keyframe.h into oracle/_ref; tests/golden/cloud_ref.npz holds
+// its outputs).
 #include <cstdint>
 
 #include "lsdo.h"
