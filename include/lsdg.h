@@ -628,7 +628,11 @@ typedef struct lsdg_slam_params {
   int32_t ref_min_validity; /* tracking reference: only depth whose validity count reaches this    */
   float sim3_info_scale;    /* information of a Sim3 constraint = the tracker's J^T W J times this */
   float ref_max_var;        /* tracking reference: only depth whose variance is below this (0 = all) */
-  int32_t reserved[4];
+  float epipolar_var;       /* sigma_l^2 of the loop's depth filter (px^2), replacing
+                               lsdg_params.epipolar_var (0 = keep it): in the loop the epipolar line
+                               comes from a tracked pose, whose error moves the line by more than the
+                               exact poses lsdg_params' default assumes */
+  int32_t reserved[3];
 } lsdg_slam_params;
 
 typedef struct lsdg_slam_stats {

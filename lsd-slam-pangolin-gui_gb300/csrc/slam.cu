@@ -10,8 +10,9 @@
 //   * tracking (the caller's thread, lsdg_slam_next_image): every frame is aligned to the current
 //     keyframe (SE3Tracker::trackFrame, constant-velocity initial guess);
 //   * mapping (same thread, after tracking): the frame updates the keyframe's depth
-//     (DepthMap::updateKeyframe, 8-bit frame), the tracking reference is refreshed from the smoothed
-//     depth every few frames, and after kf_dist metres of travel, a kf_angle turn, or when fewer than
+//     (DepthMap::updateKeyframe, 8-bit frame; the epipolar line's position variance raised to cover
+//     the tracked pose's error), the tracking reference is refreshed from the smoothed depth (after
+//     every frame by default), and after kf_dist metres of travel, a kf_angle turn, or when fewer than
 //     kf_min_usage of the keyframe's points stay in view, the frame becomes the new keyframe
 //     (DepthMap::createKeyFrame: propagation + regularisation);
 //   * constraint search (a worker thread with a context of its own): each new keyframe is aligned
@@ -368,7 +369,7 @@ void lsdg_slam_default_params(lsdg_slam_params* p) {
   p->kf_dist = 0.1f;
   p->kf_angle_deg = 6.0f;
   p->kf_min_usage = 0.55f;
-  p->refresh_every = 4;
+  p->refresh_every = 1;
   p->n_candidates = 10;
   p->cand_radius = 1.2f;
   p->optimize_every = 5;
@@ -383,6 +384,7 @@ void lsdg_slam_default_params(lsdg_slam_params* p) {
   p->odometry_scale_weight = 1.0f;
   p->ref_min_validity = 0;
   p->sim3_info_scale = 1e-3f;
+  p->epipolar_var = 4.0f;
 }
 
 lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* sp, int device, int width, int height,
@@ -395,6 +397,7 @@ lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* 
   else lsdg_default_params(&s->params);
   if (sp) s->sp = *sp;
   else lsdg_slam_default_params(&s->sp);
+  if (s->sp.epipolar_var > 0.0f) s->params.epipolar_var = s->sp.epipolar_var;
   s->w = width;
   s->h = height;
   s->intr = *intr;

@@ -133,7 +133,7 @@ class SlamParams(C.Structure):
         ("both_directions", C.c_int32), ("consistency_trans", C.c_float), ("consistency_rot", C.c_float),
         ("consistency_scale", C.c_float), ("async_constraints", C.c_int32), ("graph_threads", C.c_int32),
         ("odometry_scale_weight", C.c_float), ("ref_min_validity", C.c_int32), ("sim3_info_scale", C.c_float),
-        ("ref_max_var", C.c_float), ("reserved", C.c_int32 * 4),
+        ("ref_max_var", C.c_float), ("epipolar_var", C.c_float), ("reserved", C.c_int32 * 3),
     ]
 
 
