@@ -86,11 +86,22 @@ __device__ __forceinline__ void band_intensity(const FrameDev& F, int band, cons
   }
 }
 
+// Level-0 staging of the one-launch build: the band's valid level-0 pixels, in row-major order, as
+// {idepth, var, intensity, band-local pixel index}, kept in shared memory from the depth pass to the
+// point writes so that the writes need not read the level-0 planes a second time.  A band with more
+// valid pixels than this keeps the second read (band_points' general path).
+constexpr int kStageCap = 2560;
+
 // Depth pyramid of the band (level 0 sanitised in place: idepth <= 0 or var <= 0 -> -1, written
 // only where the value is not -1 already; level l: inverse-variance weighted mean of the valid 2x2
 // children, variance = n / sum(1/var)) and its valid pixels per level into cnt[l] (shared memory,
 // visible to the whole CTA on return).  Each thread counts its own pixels; one block sum per level.
-__device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt, int* wsum) {
+// stage (or nullptr): shared memory of kStageCap entries that receives the level-0 valid pixels in
+// row-major order (the first kStageCap of them); off: 64 ints of shared memory, total: two (both
+// double-buffered by chunk parity, so a chunk's scan results stay readable while the next chunk
+// publishes its counts: two barriers per chunk).
+__device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt, int* wsum, float4* stage = nullptr,
+                                           int* off = nullptr, int* total = nullptr) {
   const int L = F.levels;
   const int band_rows = 1 << (L - 1);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -100,9 +111,13 @@ __device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt
     if (l == 0) {
       float* D = F.idepth[0] + (size_t)y0 * w;
       float* V = F.ivar[0] + (size_t)y0 * w;
+      const float* P = F.plane[0] + (size_t)y0 * w;
       const int n = rows * w;
-      constexpr int B = 4;
-      for (int base = 0; base < n; base += 256 * B) {
+      constexpr int B = 4, NWARP = 8;  // blockDim.x == 256
+      const unsigned lt = (1u << lane) - 1u;
+      int run = 0;  // staged entries so far (uniform across the CTA)
+      int parity = 0;
+      for (int base = 0; base < n; base += 256 * B, parity ^= 1) {
         float d[B], v[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
@@ -114,15 +129,54 @@ __device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt
             v[u] = V[i];
           }
         }
+        unsigned m[B];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
           const int i = base + u * 256 + (int)threadIdx.x;
           const bool valid = d[u] > 0.f && v[u] > 0.f;
           count += valid ? 1 : 0;
+          m[u] = stage ? __ballot_sync(0xffffffffu, valid) : 0u;
           if (i < n && !valid && !(d[u] == -1.f && v[u] == -1.f)) {
             D[i] = -1.f;
             V[i] = -1.f;
           }
+        }
+        if (stage) {  // same (j, warp) scan as band_points: staged in row-major order
+          int* offp = off + 32 * parity;
+          int* totp = total + parity;
+          float I[B];
+#pragma unroll
+          for (int u = 0; u < B; ++u)
+            I[u] = ((m[u] >> lane) & 1u) ? P[base + u * 256 + (int)threadIdx.x] : 0.f;
+          if (lane < B) {
+            unsigned mm = m[0];
+#pragma unroll
+            for (int u = 1; u < B; ++u)
+              if (lane == u) mm = m[u];
+            offp[lane * NWARP + wid] = __popc(mm);
+          }
+          __syncthreads();
+          if (wid == 0) {
+            const int c = offp[lane];
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+              const int t = __shfl_up_sync(0xffffffffu, incl, o);
+              if (lane >= o) incl += t;
+            }
+            offp[lane] = incl - c;
+            if (lane == 31) *totp = incl;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int u = 0; u < B; ++u) {
+            if ((m[u] >> lane) & 1u) {
+              const int k = run + offp[u * NWARP + wid] + __popc(m[u] & lt);
+              if (k < kStageCap)
+                stage[k] = make_float4(d[u], v[u], I[u], __int_as_float(base + u * 256 + (int)threadIdx.x));
+            }
+          }
+          run += *totp;
         }
       }
     } else {
@@ -190,8 +244,11 @@ __device__ __forceinline__ void band_depth(const FrameDev& F, int band, int* cnt
 // The band's valid pixels of every level as SoA points {X, Y, Z, I} + var, in row-major order,
 // level l starting at pos[l] (shared memory).  A chunk is 4 x 256 pixels (pixel base + 256 j +
 // thread, j = 0..3): one ballot per j and warp, one warp-wide scan of the 32 (j, warp) counts, so
-// three barriers per 1024 pixels.  off: 32 ints of shared memory, total: one.
-__device__ __forceinline__ void band_points(const FrameDev& F, int band, const int* pos, int* off, int* total) {
+// three barriers per 1024 pixels.  off: 32 ints of shared memory, total: one.  stage / n_stage0:
+// level 0's valid pixels as band_depth staged them (n_stage0 of them, all of the level's when
+// n_stage0 <= kStageCap): they are written from shared memory without reading the level-0 planes.
+__device__ __forceinline__ void band_points(const FrameDev& F, int band, const int* pos, int* off, int* total,
+                                            const float4* stage = nullptr, int n_stage0 = 0) {
   const int L = F.levels;
   const int band_rows = 1 << (L - 1);
   constexpr int J = 4, NWARP = 8;  // blockDim.x == 256
@@ -206,6 +263,21 @@ __device__ __forceinline__ void band_points(const FrameDev& F, int band, const i
     const float* P = F.plane[l] + (size_t)y0 * w;
     int pos0 = pos[l];
     const float cx = F.cx[l], cy = F.cy[l], fxi = F.fxi[l], fyi = F.fyi[l];
+    if (l == 0 && stage && n_stage0 <= kStageCap) {
+      for (int k = (int)threadIdx.x; k < n_stage0; k += 256) {
+        const float4 e = stage[k];
+        const int i = __float_as_int(e.w);
+        const int r = rd.row(i), x = i - r * w, y = y0 + r;
+        const int p = pos0 + k;
+        const float z = 1.0f / e.x;
+        const float X = (((float)x - cx) * fxi) * z;
+        const float Y = (((float)y - cy) * fyi) * z;
+        F.pxyzi[0][p] = make_float4(X, Y, z, e.z);
+        F.pvar[0][p] = e.y;
+        if (F.ppix[0]) F.ppix[0][p] = y * w + x;
+      }
+      continue;
+    }
     for (int base = 0; base < npix; base += J * 256) {
       float d[J], v[J];
 #pragma unroll
@@ -361,7 +433,10 @@ constexpr int kBuildSpinLimit = 1 << 20;
 // so the frame's other bands wait until their limit and the error word is set.
 // u8 / plane0 / mode: when *mode is 1 the level-0 images are the bytes at u8 (laid out like the
 // float planes from plane0 on) and the build widens them (band_intensity).
-__global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __restrict__ frames, int n_frames,
+// The level-0 points are staged in shared memory by the depth pass (40 KB a CTA, kStageCap) and
+// written from there after the look-back; four CTAs per SM leave 64 registers a thread (five, at 48,
+// spilled and ran slower).
+__global__ void __launch_bounds__(256, 4) frame_build_kernel(const FrameDev* __restrict__ frames, int n_frames,
                                                              int n_point_frames, int bands,
                                                              unsigned long long* __restrict__ ws, int withhold_frame,
                                                              const uint8_t* __restrict__ u8,
@@ -370,8 +445,9 @@ __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __r
   __shared__ int wsum[8];
   __shared__ int cnt[kMaxLevels];
   __shared__ int pos[kMaxLevels];
-  __shared__ int off[32];
-  __shared__ int total;
+  __shared__ int off[64];
+  __shared__ int total[2];
+  __shared__ float4 stage[kStageCap];
   if (threadIdx.x == 0) s_ticket = (int)atomicAdd(reinterpret_cast<unsigned int*>(ws), 1u);
   __syncthreads();
   const int t = s_ticket;
@@ -384,8 +460,9 @@ __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __r
   const uint8_t* src8 = (mode && *mode == 1) ? u8 + (F.plane[0] - plane0) : nullptr;
   band_intensity(F, band, src8);
   if (!F.has_depth) return;
-  band_depth(F, band, cnt, wsum);
-  if (fi >= n_point_frames) return;
+  const bool points = fi < n_point_frames;
+  band_depth(F, band, cnt, wsum, points ? stage : nullptr, off, total);
+  if (!points) return;
   if ((int)threadIdx.x < L) {
     const int l = threadIdx.x;
     volatile unsigned long long* st = ws + 1 + (size_t)fi * bands * kMaxLevels;
@@ -413,7 +490,7 @@ __global__ void __launch_bounds__(256, 5) frame_build_kernel(const FrameDev* __r
     if (band == nb - 1) F.pcount[l] = (int)(prefix + c);
   }
   __syncthreads();
-  band_points(F, band, pos, off, &total);
+  band_points(F, band, pos, off, total, stage, cnt[0]);
 }
 
 // ------------------------------------------------------------------------------------------
