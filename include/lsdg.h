@@ -632,12 +632,25 @@ typedef struct lsdg_slam_params {
                                lsdg_params.epipolar_var (0 = keep it): in the loop the epipolar line
                                comes from a tracked pose, whose error moves the line by more than the
                                exact poses lsdg_params' default assumes */
-  int32_t reserved[3];
+  int32_t reactivate;       /* before making a keyframe, track the frame against the earlier
+                               keyframes near the camera (SlamSystem's re-positioning); one that
+                               tracks it well becomes the current keyframe again (its depth map is
+                               refined further) and the keyframe left is tied to it in the graph */
+  float react_radius;       /* ... candidates: camera centres within this of the camera (m)        */
+  float react_angle_deg;    /* ... and viewing directions within this angle (degrees)              */
+  float react_min_usage;    /* ... accepted when at least this share of its points stay in view    */
+  float react_max_jump;     /* ... and the tracked pose is this close to the graph's prediction (m) */
+  int32_t react_min_age;    /* ... candidates: keyframes made at least this many keyframes ago     */
+  float react_min_good;     /* ... accepted when at least this share of the points in view are
+                               inliers, and when the frame lies within half of kf_dist and of
+                               kf_angle_deg of the keyframe (so that it is not left at once)      */
+  int32_t reserved[2];
 } lsdg_slam_params;
 
 typedef struct lsdg_slam_stats {
   int32_t frames, keyframes, lost_frames, sim3_edges, sim3_rejected, graph_optimisations;
-  int32_t reserved[6];
+  int32_t reactivations;    /* keyframes made current again instead of a new keyframe */
+  int32_t reserved[5];
 } lsdg_slam_stats;
 
 LSDG_API void lsdg_slam_default_params(lsdg_slam_params* p);

@@ -15,6 +15,10 @@
 //     every frame by default), and after kf_dist metres of travel, a kf_angle turn, or when fewer than
 //     kf_min_usage of the keyframe's points stay in view, the frame becomes the new keyframe
 //     (DepthMap::createKeyFrame: propagation + regularisation);
+//   * re-positioning (caller's thread, before a keyframe would be made): the earlier keyframes whose
+//     camera is near the current one in the graph are tracked against the frame; one that keeps most
+//     of its points in view at a pose close to the graph's prediction becomes the current keyframe
+//     again (its depth map is refined further) and the keyframe left is tied to it in the graph;
 //   * constraint search (a worker thread with a context of its own): each new keyframe is aligned
 //     with Sim3Tracker::trackFrameSim3 to its predecessor and the nearest earlier keyframes in one
 //     batched launch from device-resident keyframes -- in both directions, a constraint being kept
@@ -45,6 +49,7 @@ namespace {
 struct Keyframe {
   int frame_index = 0;
   int node = 0;
+  int parent = -1;                 // the keyframe it was made from (tracked against, propagated from)
   lsdg_frame* frame = nullptr;     // tracking reference (refreshed while it is the current keyframe)
   lsdg_frame* snapshot = nullptr;  // its state at creation, read by the constraint search of its own job
 };
@@ -77,7 +82,9 @@ struct lsdg_slam {
   std::string worker_error;
   int since_refresh = 0;
   int loops_pending = 0;
+  int cur = 0;                 // the current keyframe (tracked against, mapped)
   lsdg_slam_stats stats{};
+  lsdg_slam_stats wstats{};  // counted by the worker's jobs, added to stats when the worker is joined
   std::vector<float> d_buf, v_buf;
   std::vector<int32_t> val_buf;
   std::string err;
@@ -168,17 +175,18 @@ struct Cand {
 lsdg_status constraint_job(lsdg_slam* s, int k) {
   lsdg_ctx* ctx = s->ctx_cons;
   const Keyframe& kn = s->keyframes[k];
-  const Keyframe& kp = s->keyframes[k - 1];
+  const int parent = kn.parent;
   const M4 T_new = s->graph.poses[kn.node];
   std::vector<Cand> others;
-  for (int c = 0; c + 2 <= k; ++c) {
+  for (int c = 0; c < k; ++c) {
+    if (c == parent) continue;
     const M4& Tc = s->graph.poses[s->keyframes[c].node];
     const double d[3] = {Tc(0, 3) - T_new(0, 3), Tc(1, 3) - T_new(1, 3), Tc(2, 3) - T_new(2, 3)};
     const double dist = norm3(d);
     if (dist < s->sp.cand_radius) others.push_back({dist, c});
   }
   std::stable_sort(others.begin(), others.end(), [](const Cand& a, const Cand& b) { return a.dist < b.dist; });
-  std::vector<int> cands = {k - 1};
+  std::vector<int> cands = {parent};
   for (const Cand& c : others) {
     if ((int)cands.size() >= s->sp.n_candidates) break;
     cands.push_back(c.kf);
@@ -246,14 +254,13 @@ lsdg_status constraint_job(lsdg_slam* s, int k) {
       for (double v : H) ok = ok && std::isfinite(v);
     }
     if (!ok) {
-      s->stats.sim3_rejected++;
+      s->wstats.sim3_rejected++;
       continue;
     }
     for (double& v : H) v *= s->sp.sim3_info_scale;
     s->graph.add_edge(s->keyframes[cands[i]].node, kn.node, Z, H);
-    s->stats.sim3_edges++;
-    loop = loop || cands[i] != k - 1;
-    (void)kp;
+    s->wstats.sim3_edges++;
+    loop = loop || cands[i] != parent;
   }
   if (loop && ++s->loops_pending >= s->sp.optimize_every) {
     const std::vector<M4> keep = s->graph.poses;
@@ -262,15 +269,23 @@ lsdg_status constraint_job(lsdg_slam* s, int k) {
     for (const M4& T : s->graph.poses) good = good && finite(T);
     if (!good) s->graph.poses = keep;
     s->loops_pending = 0;
-    s->stats.graph_optimisations++;
+    s->wstats.graph_optimisations++;
   }
   return LSDG_OK;
+}
+
+void merge_worker_stats(lsdg_slam* s) {
+  s->stats.sim3_edges += s->wstats.sim3_edges;
+  s->stats.sim3_rejected += s->wstats.sim3_rejected;
+  s->stats.graph_optimisations += s->wstats.graph_optimisations;
+  s->wstats = lsdg_slam_stats{};
 }
 
 lsdg_status join_worker(lsdg_slam* s) {
   if (s->worker_running) {
     s->worker.join();
     s->worker_running = false;
+    merge_worker_stats(s);
     // the new keyframe's snapshot was read by its own job only
     Keyframe& k = s->keyframes.back();
     if (k.snapshot) {
@@ -285,11 +300,17 @@ lsdg_status join_worker(lsdg_slam* s) {
   return LSDG_OK;
 }
 
+void optimize_graph(lsdg_slam* s, int iterations);
+
+// The worker's next job: the constraint search of keyframe k (k >= 0), or, for k < 0, a few pose-graph
+// iterations after a loop edge (re-positioning).  Inline when async_constraints is 0.
 lsdg_status start_job(lsdg_slam* s, int k) {
   auto body = [s, k]() {
     std::string* keep = t_err;
     t_err = &s->worker_error;
-    const lsdg_status st = constraint_job(s, k);
+    lsdg_status st = LSDG_OK;
+    if (k >= 0) st = constraint_job(s, k);
+    else optimize_graph(s, 5);
     if (st != LSDG_OK) s->worker_status = st;
     t_err = keep;
   };
@@ -303,14 +324,142 @@ lsdg_status start_job(lsdg_slam* s, int k) {
     return LSDG_OK;
   }
   body();
-  Keyframe& kn = s->keyframes[k];
-  if (kn.snapshot) {
-    lsdg_frame_destroy(s->ctx, kn.snapshot);
-    kn.snapshot = nullptr;
+  merge_worker_stats(s);
+  if (k >= 0) {
+    Keyframe& kn = s->keyframes[k];
+    if (kn.snapshot) {
+      lsdg_frame_destroy(s->ctx, kn.snapshot);
+      kn.snapshot = nullptr;
+    }
   }
   if (s->worker_status != LSDG_OK) {
     s->err = "constraint search: " + s->worker_error;
     return s->worker_status;
+  }
+  return LSDG_OK;
+}
+
+// SE3 part {R, t} of a Sim3 [[s R, t], [0, 1]].
+M4 se3_part(const M4& S) {
+  const double sc = lsdg::slam::sim3_scale(S);
+  M4 T = S;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) T(r, c) = S(r, c) / sc;
+  return T;
+}
+
+// SE3 information of a tracking result as a 7x7 graph information (scale tied by a prior as strong
+// as the strongest direction times odometry_scale_weight); false when the Hessian is not usable.
+bool se3_information(const lsdg_slam* s, const lsdg_track_stats& st, double W[49]) {
+  double H6[36];
+  hess_full(st, 6, H6);
+  bool ok = true;
+  double dmax = 0.0;
+  for (int i = 0; i < 36; ++i) ok = ok && std::isfinite(H6[i]);
+  for (int i = 0; i < 6; ++i) dmax = std::max(dmax, H6[7 * i]);
+  if (!ok || !(dmax > 0)) return false;
+  std::memset(W, 0, sizeof(double) * 49);
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) W[7 * i + j] = H6[6 * i + j] * 1e-3;
+  W[48] = dmax * 1e-3 * s->sp.odometry_scale_weight;
+  return true;
+}
+
+// A few pose-graph iterations (worker thread), kept only when every pose stays finite.
+void optimize_graph(lsdg_slam* s, int iterations) {
+  const std::vector<M4> keep = s->graph.poses;
+  s->graph.optimize(iterations);
+  bool good = true;
+  for (const M4& T : s->graph.poses) good = good && finite(T);
+  if (!good) s->graph.poses = keep;
+  s->wstats.graph_optimisations++;
+}
+
+// Re-positioning before a new keyframe (SlamSystem's re-activation of an earlier keyframe): the
+// earlier keyframes whose camera lies within react_radius and react_angle_deg of the current camera
+// in the graph are tracked against `frame` (nearest first, at most three); the first that keeps
+// react_min_usage of its points in view with react_min_good of them inliers, at a pose within
+// react_max_jump of the graph's prediction and within half of kf_dist / kf_angle_deg of the keyframe
+// (so that the keyframe is not left again at the next frame), becomes the current keyframe again.
+// *done: whether one did.
+lsdg_status try_reactivate(lsdg_slam* s, lsdg_frame* frame, const M4& f2k, bool* done) {
+  *done = false;
+  lsdg_status r = join_worker(s);  // the graph is the caller's again
+  if (r != LSDG_OK) return r;
+  const int n_kf = (int)s->keyframes.size();
+  const M4 T_cur = lsdg::slam::mul(s->graph.poses[s->keyframes[s->cur].node], f2k);
+  std::vector<Cand> cands;
+  for (int c = 0; c < n_kf - s->sp.react_min_age; ++c) {
+    if (c == s->cur) continue;
+    const M4& Tc = s->graph.poses[s->keyframes[c].node];
+    const double d[3] = {Tc(0, 3) - T_cur(0, 3), Tc(1, 3) - T_cur(1, 3), Tc(2, 3) - T_cur(2, 3)};
+    const double dist = norm3(d);
+    if (dist > s->sp.react_radius) continue;
+    if (rotation_angle(se3_part(lsdg::slam::mul(lsdg::slam::sim3_inv(Tc), T_cur))) >
+        s->sp.react_angle_deg * M_PI / 180.0)
+      continue;
+    cands.push_back({dist, c});
+  }
+  std::stable_sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) { return a.dist < b.dist; });
+  for (size_t i = 0; i < cands.size() && i < 3; ++i) {
+    const int c = cands[i].kf;
+    const M4 guess = se3_part(lsdg::slam::mul(lsdg::slam::sim3_inv(s->graph.poses[s->keyframes[c].node]), T_cur));
+    double g12[12], o12[12];
+    lsdg::slam::to12(guess, g12);
+    lsdg_track_stats st{};
+    const lsdg_status ts = lsdg_track_se3(s->ctx, s->keyframes[c].frame, frame, g12, o12, &st);
+    if (ts != LSDG_OK && ts != LSDG_TRACKING_LOST) return fail(s, ts, "lsdg_track_se3 (re-positioning)", s->ctx);
+    const M4 f2c = lsdg::slam::from12(o12);
+    const double jump[3] = {f2c(0, 3) - guess(0, 3), f2c(1, 3) - guess(1, 3), f2c(2, 3) - guess(2, 3)};
+    double W[49];
+    const double tc[3] = {f2c(0, 3), f2c(1, 3), f2c(2, 3)};
+    if (st.status != LSDG_OK || !finite(f2c) || st.usage < s->sp.react_min_usage ||
+        st.good_ratio < s->sp.react_min_good || norm3(jump) > s->sp.react_max_jump ||
+        norm3(tc) > 0.5 * s->sp.kf_dist || rotation_angle(f2c) > 0.5 * s->sp.kf_angle_deg * M_PI / 180.0 ||
+        !se3_information(s, st, W))
+      continue;
+    // loop edge: the keyframe left, seen from the re-activated one -- a Sim3 alignment of the two
+    // keyframes (both carry depth, so their relative scale is measured) started from the pose through
+    // this frame; when that alignment fails, the SE3 pose through this frame with its scale prior
+    const M4 z_frame = lsdg::slam::mul(f2c, lsdg::slam::sim3_inv(f2k));
+    double z13[13], zo13[13];
+    lsdg::slam::to13(z_frame, z13);
+    lsdg_track_stats s7{};
+    const lsdg_status ts7 =
+        lsdg_track_sim3(s->ctx, s->keyframes[c].frame, s->keyframes[s->cur].frame, z13, zo13, &s7);
+    if (ts7 != LSDG_OK && ts7 != LSDG_TRACKING_LOST) return fail(s, ts7, "lsdg_track_sim3 (re-positioning)", s->ctx);
+    bool sim3_ok = s7.status == LSDG_OK && std::isfinite(zo13[12]) && zo13[12] > 0.5 && zo13[12] < 2.0;
+    M4 z = z_frame;
+    double H7[49];
+    if (sim3_ok) {
+      z = lsdg::slam::from13(zo13);
+      double dz[7];
+      lsdg::slam::sim3_log(lsdg::slam::mul(lsdg::slam::sim3_inv(z_frame), z), dz);
+      const double tz[3] = {z(0, 3), z(1, 3), z(2, 3)};
+      sim3_ok = finite(z) && norm3(dz) < 0.25 * std::max(1.0, norm3(tz)) && norm3(dz + 3) < 0.15 &&
+                std::fabs(dz[6]) < 0.3;
+      hess_full(s7, 7, H7);
+      for (double v : H7) sim3_ok = sim3_ok && std::isfinite(v);
+    }
+    if (sim3_ok) {
+      for (double& v : H7) v *= s->sp.sim3_info_scale;
+      s->graph.add_edge(s->keyframes[c].node, s->keyframes[s->cur].node, z, H7);
+    } else {
+      s->graph.add_edge(s->keyframes[c].node, s->keyframes[s->cur].node, z_frame, W);
+    }
+    // the depth map takes the re-activated keyframe's state back (image and smoothed depth)
+    const size_t npix = (size_t)s->w * s->h;
+    std::vector<float> lvl(4 * npix), img(npix);  // level 0 comes back as {I, gx, gy, 0} per pixel
+    SLAM_CK(s, lsdg_frame_get_level(s->ctx, s->keyframes[c].frame, 0, lvl.data()), s->ctx);
+    for (size_t i = 0; i < npix; ++i) img[i] = lvl[4 * i];
+    SLAM_CK(s, lsdg_frame_get_depth(s->ctx, s->keyframes[c].frame, 0, s->d_buf.data(), s->v_buf.data()), s->ctx);
+    SLAM_CK(s, lsdg_depth_set_keyframe(s->ctx, s->dm, img.data(), s->d_buf.data(), s->v_buf.data()), s->ctx);
+    s->cur = c;
+    s->traj.back() = {c, f2c};
+    s->since_refresh = 0;
+    s->stats.reactivations++;
+    *done = true;
+    return start_job(s, -1);  // the graph takes the loop edge in on the worker thread
   }
   return LSDG_OK;
 }
@@ -325,9 +474,10 @@ lsdg_status new_keyframe(lsdg_slam* s, int frame_index, const uint8_t* image, co
   std::vector<float> img((size_t)s->w * s->h);
   for (size_t i = 0; i < img.size(); ++i) img[i] = (float)image[i];
   SLAM_CK(s, lsdg_depth_create_keyframe(s->ctx, s->dm, img.data(), k2f12, 1), s->ctx);
-  const Keyframe& prev = s->keyframes.back();
+  const Keyframe& prev = s->keyframes[s->cur];
   Keyframe kf;
   kf.frame_index = frame_index;
+  kf.parent = s->cur;
   kf.node = s->graph.add_node(lsdg::slam::mul(s->graph.poses[prev.node], f2k));
   r = new_frame_with_depth(s, image, &kf.frame);
   if (r == LSDG_OK) r = new_frame_with_depth(s, image, &kf.snapshot);
@@ -338,23 +488,13 @@ lsdg_status new_keyframe(lsdg_slam* s, int frame_index, const uint8_t* image, co
   }
   const int prev_node = prev.node;
   s->keyframes.push_back(kf);
-  s->traj.back() = {(int)s->keyframes.size() - 1, M4::identity()};
+  s->cur = (int)s->keyframes.size() - 1;
+  s->traj.back() = {s->cur, M4::identity()};
   s->since_refresh = 0;
   // odometry edge from the tracking chain (SE3 information; the scale tied by a prior as strong as
   // the strongest direction)
-  double H6[36], W[49];
-  hess_full(st, 6, H6);
-  bool ok = true;
-  double dmax = 0.0;
-  for (int i = 0; i < 36; ++i) ok = ok && std::isfinite(H6[i]);
-  for (int i = 0; i < 6; ++i) dmax = std::max(dmax, H6[7 * i]);
-  if (ok && dmax > 0) {
-    std::memset(W, 0, sizeof(W));
-    for (int i = 0; i < 6; ++i)
-      for (int j = 0; j < 6; ++j) W[7 * i + j] = H6[6 * i + j] * 1e-3;
-    W[48] = dmax * 1e-3 * s->sp.odometry_scale_weight;
-    s->graph.add_edge(prev_node, kf.node, f2k, W);
-  }
+  double W[49];
+  if (se3_information(s, st, W)) s->graph.add_edge(prev_node, kf.node, f2k, W);
   s->stats.keyframes = (int)s->keyframes.size();
   return start_job(s, (int)s->keyframes.size() - 1);
 }
@@ -385,6 +525,13 @@ void lsdg_slam_default_params(lsdg_slam_params* p) {
   p->ref_min_validity = 0;
   p->sim3_info_scale = 1e-3f;
   p->epipolar_var = 4.0f;
+  p->reactivate = 1;
+  p->react_radius = 0.5f;
+  p->react_angle_deg = 20.0f;
+  p->react_min_usage = 0.75f;
+  p->react_max_jump = 0.5f;
+  p->react_min_age = 10;
+  p->react_min_good = 0.9f;
 }
 
 lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* sp, int device, int width, int height,
@@ -449,6 +596,7 @@ lsdg_status lsdg_slam_bootstrap(lsdg_slam* s, int id, const uint8_t* image, cons
   const lsdg_status st = new_frame_with_depth(s, image, &kf.frame);
   if (st != LSDG_OK) return st;
   s->keyframes.push_back(kf);
+  s->cur = 0;
   s->traj.push_back({0, M4::identity()});
   s->traj_id.push_back(id);
   s->stats.frames = 1;
@@ -459,13 +607,16 @@ lsdg_status lsdg_slam_bootstrap(lsdg_slam* s, int id, const uint8_t* image, cons
 lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
   if (!s || !image) return LSDG_INVALID_ARG;
   if (s->keyframes.empty()) return fail(s, LSDG_INVALID_ARG, "bootstrap the first keyframe first");
-  const int kfi = (int)s->keyframes.size() - 1;
+  const int kfi = s->cur;
   const Keyframe& kf = s->keyframes[kfi];
-  // constant-velocity guess in the keyframe's frame
+  // constant-velocity guess in the keyframe's frame; the first frame after a keyframe switch starts
+  // from the switch frame's pose (carrying the velocity across the switch let one poor alignment's
+  // motion grow from keyframe to keyframe: measured, the 640x480 room sequence ran away in 30 frames)
   const FramePose& last = s->traj.back();
   const M4 c1 = last.keyframe == kfi ? last.f2k : M4::identity();
   M4 c0 = c1;
-  if (s->traj.size() > 1 && s->traj[s->traj.size() - 2].keyframe == kfi) c0 = s->traj[s->traj.size() - 2].f2k;
+  const size_t n = s->traj.size();
+  if (n > 1 && s->traj[n - 2].keyframe == kfi) c0 = s->traj[n - 2].f2k;
   M4 guess = lsdg::slam::mul(lsdg::slam::mul(c1, lsdg::slam::sim3_inv(c0)), c1);
   if (!finite(guess)) guess = c1;
   lsdg_frame* frame = s->pool[s->pool_next];
@@ -499,8 +650,14 @@ lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
   }
   const double t[3] = {f2k(0, 3), f2k(1, 3), f2k(2, 3)};
   if (norm3(t) > s->sp.kf_dist || rotation_angle(f2k) > s->sp.kf_angle_deg * M_PI / 180.0 ||
-      st.usage < s->sp.kf_min_usage)
+      st.usage < s->sp.kf_min_usage) {
+    if (s->sp.reactivate) {
+      bool done = false;
+      lsdg_status r = try_reactivate(s, frame, f2k, &done);
+      if (r != LSDG_OK || done) return r;
+    }
     return new_keyframe(s, (int)s->traj.size() - 1, image, f2k, st);
+  }
   return LSDG_OK;
 }
 

@@ -189,10 +189,37 @@ void adjoint(const M4& T, double A[49]) {
   A[48] = 1.0;
 }
 
+// Nearest rotation to a 3x3 matrix that is close to one (polar decomposition by the Newton
+// iteration R <- (R + R^-T) / 2, quadratic near SO(3); Higham 1986).  Poses that arrive from the
+// float tracker, or are composed from such poses, drift off SO(3) by rounding; sim3_inv and the
+// graph's residuals assume a rotation, and a chain of compositions and inverses of a non-rotation
+// amplifies the drift, so every pose is brought back onto SO(3) where it enters.
+void orthonormalize(double R[9]) {
+  for (int it = 0; it < 4; ++it) {
+    // cofactor matrix C: R^-T = C / det(R)
+    double C[9];
+    C[0] = R[4] * R[8] - R[5] * R[7];
+    C[1] = R[5] * R[6] - R[3] * R[8];
+    C[2] = R[3] * R[7] - R[4] * R[6];
+    C[3] = R[2] * R[7] - R[1] * R[8];
+    C[4] = R[0] * R[8] - R[2] * R[6];
+    C[5] = R[1] * R[6] - R[0] * R[7];
+    C[6] = R[1] * R[5] - R[2] * R[4];
+    C[7] = R[2] * R[3] - R[0] * R[5];
+    C[8] = R[0] * R[4] - R[1] * R[3];
+    const double det = R[0] * C[0] + R[1] * C[1] + R[2] * C[2];
+    if (!(det > 0.0)) return;  // not near a rotation: left as it is
+    for (int k = 0; k < 9; ++k) R[k] = 0.5 * (R[k] + C[k] / det);
+  }
+}
+
 M4 from13(const double p[13]) {
+  double R[9];
+  for (int k = 0; k < 9; ++k) R[k] = p[k];
+  orthonormalize(R);
   M4 T = M4::identity();
   for (int i = 0; i < 3; ++i) {
-    for (int j = 0; j < 3; ++j) T(i, j) = p[12] * p[3 * i + j];
+    for (int j = 0; j < 3; ++j) T(i, j) = p[12] * R[3 * i + j];
     T(i, 3) = p[9 + i];
   }
   return T;
@@ -210,6 +237,12 @@ void to13(const M4& T, double p[13]) {
 M4 from12(const double p[12]) {
   M4 T = M4::identity();
   for (int i = 0; i < 12; ++i) T.a[i] = p[i];
+  double R[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = p[4 * i + j];
+  orthonormalize(R);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) T(i, j) = R[3 * i + j];
   return T;
 }
 

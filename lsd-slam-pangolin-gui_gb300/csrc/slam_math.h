@@ -32,9 +32,10 @@ void so3_log(const double R[9], double w[3]);
 M4 sim3_exp(const double xi[7]);
 void sim3_log(const M4& T, double xi[7]);
 void adjoint(const M4& T, double A[49]);
-M4 from13(const double p[13]);             // {R, t, s} -> [[s R, t], [0, 1]]
+void orthonormalize(double R[9]);          // nearest rotation to a near-rotation (row-major 3x3)
+M4 from13(const double p[13]);             // {R, t, s} -> [[s R, t], [0, 1]], R brought onto SO(3)
 void to13(const M4& T, double p[13]);
-M4 from12(const double p[12]);             // [R | t] row-major
+M4 from12(const double p[12]);             // [R | t] row-major, R brought onto SO(3)
 void to12(const M4& T, double p[12]);
 
 struct Edge {

@@ -133,7 +133,10 @@ class SlamParams(C.Structure):
         ("both_directions", C.c_int32), ("consistency_trans", C.c_float), ("consistency_rot", C.c_float),
         ("consistency_scale", C.c_float), ("async_constraints", C.c_int32), ("graph_threads", C.c_int32),
         ("odometry_scale_weight", C.c_float), ("ref_min_validity", C.c_int32), ("sim3_info_scale", C.c_float),
-        ("ref_max_var", C.c_float), ("epipolar_var", C.c_float), ("reserved", C.c_int32 * 3),
+        ("ref_max_var", C.c_float), ("epipolar_var", C.c_float), ("reactivate", C.c_int32),
+        ("react_radius", C.c_float), ("react_angle_deg", C.c_float), ("react_min_usage", C.c_float),
+        ("react_max_jump", C.c_float), ("react_min_age", C.c_int32), ("react_min_good", C.c_float),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -141,7 +144,7 @@ class SlamStats(C.Structure):
     """lsdg_slam_stats (include/lsdg.h)."""
     _fields_ = [("frames", C.c_int32), ("keyframes", C.c_int32), ("lost_frames", C.c_int32),
                 ("sim3_edges", C.c_int32), ("sim3_rejected", C.c_int32), ("graph_optimisations", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("reactivations", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 class GraphFramePose(C.Structure):

@@ -1,7 +1,8 @@
 """Full synthetic sequence runs of the SLAM loop (lsdg_slam, csrc/slam.cu) and their evaluation.
 
-The loop itself -- tracking and mapping of every frame, keyframes, batched Sim3 constraint search
-in both directions on a worker thread, the Sim3 pose graph -- is the library's C++ (lsdg_slam_*);
+The loop itself -- tracking and mapping of every frame, keyframes (or an earlier keyframe made current
+again), batched Sim3 constraint search in both directions on a worker thread, the Sim3 pose graph --
+is the library's C++ (lsdg_slam_*);
 this module feeds it a rendered sequence the way the reference's InputThread feeds SlamSystem
 (lib/App/InputThread.cpp:71), then scores the trajectory against the ground truth: absolute
 trajectory error of the camera centres after the best similarity alignment (Umeyama 1991), as a
@@ -86,6 +87,7 @@ def run(seq, frames, n_frames=None, params=None, slam_params=None, device=0, pos
     return {"frames": n, "seconds": wall, "fps": n / wall, "keyframes": stats["keyframes"],
             "sim3_edges": stats["sim3_edges"], "sim3_rejected": stats["sim3_rejected"],
             "lost_frames": stats["lost_frames"], "graph_optimisations": stats["graph_optimisations"],
+            "reactivations": stats["reactivations"],
             "keyframe_graph_nodes": len(graph), "ate_rmse_m": ate, "path_m": path,
             "ate_over_path": ate / max(path, 1e-9), "gt_spread_m": spread, "ate_over_gt_spread": ate / max(spread, 1e-9),
             "alignment_scale": s,

@@ -1,7 +1,8 @@
 """Full-system runs on the GPU through the library's SLAM loop (lsdg_slam over the C-ABI, driven
-by sequence.py): frames of the synthetic room are tracked, mapped, turned into keyframes with
-batched two-way Sim3 constraint search and a Sim3 pose graph; the trajectory stays within a few
-percent of the path length of the ground truth, at 320x240 and at 640x480."""
+by sequence.py): frames of the synthetic room are tracked, mapped, turned into keyframes (or an
+earlier keyframe is made current again) with batched two-way Sim3 constraint search and a Sim3 pose
+graph; the trajectory stays within a few percent of the path length of the ground truth at 320x240
+and 640x480 over 240 frames, and within 2 % over the full 1,000-frame sequence."""
 import os
 
 import numpy as np
@@ -38,6 +39,21 @@ def test_room_sequence_640x480():
     _check(res, 240)
     assert res["ate_over_path"] < 0.05, res
     assert res["ate_over_gt_spread"] < 0.35, res
+
+
+def test_room_sequence_1000_frames():
+    """The full sequence (1,000 frames 640x480, the path driven 2.2 times): on the second lap earlier
+    keyframes are made current again, which closes the loop; ATE under 2 % of the path and under 0.15
+    of the ground truth's own spread (measured: 0.27 % and 0.036)."""
+    import sequence
+    seq, frames = synth.room_sequence(0, 1000, 640, 480, workers=min(16, os.cpu_count() or 2))
+    res = sequence.run(seq, frames)
+    assert res["frames"] == 1000 and res["non_finite_frames"] == 0
+    assert res["lost_frames"] <= 5, res
+    assert res["reactivations"] > 0, res
+    assert res["ate_over_path"] < 0.02, res
+    assert res["ate_over_gt_spread"] < 0.15, res
+    assert 0.9 < res["alignment_scale"] < 1.1, res
 
 
 def test_keyframe_depth_against_truth():
