@@ -193,28 +193,32 @@ lsdg_status constraint_job(lsdg_slam* s, int k) {
   }
   const int nc = (int)cands.size();
   const bool both = s->sp.both_directions != 0;
-  const int nb = both ? 2 * nc : nc;
+  // one batch size for every job (the unused pairs repeat pair 0 and are not read): a batch is tuned
+  // and captured once, instead of once per candidate count
+  const int ncap = std::max(nc, std::max(1, s->sp.n_candidates));
+  const int nb = both ? 2 * ncap : ncap;
   lsdg_batch*& b = s->batches[nb];
   if (!b) {
     std::vector<int> ws(nb, s->w), hs(nb, s->h);
     std::vector<lsdg_intrinsics> ks(nb, s->intr);
     SLAM_CK(s, lsdg_batch_create_sim3(ctx, nb, ws.data(), hs.data(), ks.data(), &b), ctx);
   }
-  // pair i < nc: the new keyframe tracked against candidate i (frame-to-ref = new-in-candidate);
-  // pair nc + i: the candidate tracked against the new keyframe
+  // pair i < ncap: the new keyframe tracked against candidate i (frame-to-ref = new-in-candidate);
+  // pair ncap + i: the candidate tracked against the new keyframe
   std::vector<const lsdg_frame*> refs(nb), frames(nb);
   std::vector<double> init(13 * (size_t)nb);
   std::vector<M4> Zinit(nc);
-  for (int i = 0; i < nc; ++i) {
-    const Keyframe& c = s->keyframes[cands[i]];
-    Zinit[i] = lsdg::slam::mul(lsdg::slam::sim3_inv(s->graph.poses[c.node]), T_new);
+  for (int i = 0; i < ncap; ++i) {
+    const int ci = i < nc ? i : 0;
+    const Keyframe& c = s->keyframes[cands[ci]];
+    if (i < nc) Zinit[i] = lsdg::slam::mul(lsdg::slam::sim3_inv(s->graph.poses[c.node]), T_new);
     refs[i] = c.frame;
     frames[i] = kn.snapshot;
-    lsdg::slam::to13(Zinit[i], &init[13 * i]);
+    lsdg::slam::to13(Zinit[ci], &init[13 * i]);
     if (both) {
-      refs[nc + i] = kn.snapshot;
-      frames[nc + i] = c.frame;
-      lsdg::slam::to13(lsdg::slam::sim3_inv(Zinit[i]), &init[13 * (nc + i)]);
+      refs[ncap + i] = kn.snapshot;
+      frames[ncap + i] = c.frame;
+      lsdg::slam::to13(lsdg::slam::sim3_inv(Zinit[ci]), &init[13 * (ncap + i)]);
     }
   }
   SLAM_CK(s, lsdg_batch_load_frames(ctx, b, refs.data(), frames.data(), init.data()), ctx);
@@ -238,8 +242,8 @@ lsdg_status constraint_job(lsdg_slam* s, int k) {
       ok = norm3(dz) < 0.25 * std::max(1.0, norm3(tz)) && norm3(dz + 3) < 0.15 && std::fabs(dz[6]) < 0.1;
     }
     if (ok && both) {  // the reverse alignment agrees: Z_fwd Z_rev ~ identity
-      const double* orv = &out[13 * (nc + i)];
-      ok = st[nc + i].status == LSDG_OK && std::isfinite(orv[12]) && orv[12] > 0.0;
+      const double* orv = &out[13 * (ncap + i)];
+      ok = st[ncap + i].status == LSDG_OK && std::isfinite(orv[12]) && orv[12] > 0.0;
       if (ok) {
         double e[7];
         lsdg::slam::sim3_log(lsdg::slam::mul(Z, lsdg::slam::from13(orv)), e);
