@@ -353,11 +353,106 @@ bool cholesky_solve(std::vector<double>& A, int m, std::vector<double>& b, int t
   return true;
 }
 
+// Cholesky factorisation and solve restricted to the lower envelope: row i of A has no entry left
+// of column env[i] (env[i] <= i), and neither has L (fill stays inside the envelope), so the work is
+// the sum over rows of (i - env[i])^2 / 2 instead of m^3 / 6.
+bool envelope_cholesky_solve(std::vector<double>& A, int m, const std::vector<int>& env, std::vector<double>& b) {
+  for (int i = 0; i < m; ++i) {
+    double* Li = &A[(size_t)i * m];
+    for (int j = env[i]; j <= i; ++j) {
+      const double* Lj = &A[(size_t)j * m];
+      double v = Li[j];
+      for (int k = std::max(env[i], env[j]); k < j; ++k) v -= Li[k] * Lj[k];
+      if (j < i) {
+        Li[j] = v / Lj[j];
+      } else {
+        if (!(v > 0.0)) return false;
+        Li[i] = std::sqrt(v);
+      }
+    }
+  }
+  for (int i = 0; i < m; ++i) {  // L y = b
+    const double* Li = &A[(size_t)i * m];
+    double v = b[i];
+    for (int k = env[i]; k < i; ++k) v -= Li[k] * b[k];
+    b[i] = v / Li[i];
+  }
+  for (int i = m - 1; i >= 0; --i) {  // L^T x = y, column-oriented
+    const double* Li = &A[(size_t)i * m];
+    b[i] /= Li[i];
+    for (int k = env[i]; k < i; ++k) b[k] -= Li[k] * b[i];
+  }
+  return true;
+}
+
+// Reverse Cuthill-McKee order of the free nodes (1..n-1; node 0 is held) over the edges' node
+// adjacency: pos[node] = its block position, pos[0] = -1.  Nodes that edges join end up near each
+// other, so the normal equations' envelope stays narrow even when the second lap of a path is tied
+// to the first.  Ties broken by degree, then index: the order depends on the graph alone.
+std::vector<int> rcm_positions(int n, const std::vector<Edge>& edges) {
+  std::vector<std::vector<int>> adj(n);
+  for (const Edge& e : edges)
+    if (e.i != e.j && e.i > 0 && e.j > 0) {
+      adj[e.i].push_back(e.j);
+      adj[e.j].push_back(e.i);
+    }
+  for (auto& a : adj) {
+    std::sort(a.begin(), a.end());
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+  }
+  auto less = [&](int a, int b) { return adj[a].size() != adj[b].size() ? adj[a].size() < adj[b].size() : a < b; };
+  std::vector<int> order;
+  order.reserve(n > 0 ? n - 1 : 0);
+  std::vector<char> seen(n, 0);
+  if (n > 0) seen[0] = 1;
+  for (;;) {
+    int start = -1;
+    for (int k = 1; k < n; ++k)
+      if (!seen[k] && (start < 0 || less(k, start))) start = k;
+    if (start < 0) break;
+    seen[start] = 1;
+    size_t head = order.size();
+    order.push_back(start);
+    while (head < order.size()) {
+      const int v = order[head++];
+      std::vector<int> next;
+      for (int u : adj[v])
+        if (!seen[u]) {
+          seen[u] = 1;
+          next.push_back(u);
+        }
+      std::sort(next.begin(), next.end(), less);
+      order.insert(order.end(), next.begin(), next.end());
+    }
+  }
+  std::reverse(order.begin(), order.end());
+  std::vector<int> pos(n, -1);
+  for (size_t q = 0; q < order.size(); ++q) pos[order[q]] = (int)q;
+  return pos;
+}
+
 double PoseGraph::optimize(int iterations, double lam) {
   const int n = (int)poses.size();
   const int m = 7 * (n - 1);  // node 0 is held
   double c = cost();
   if (m <= 0 || edges.empty()) return c;
+  // block positions (reverse Cuthill-McKee) and the lower envelope of the normal equations
+  const std::vector<int> pos = rcm_positions(n, edges);
+  std::vector<int> envb(n - 1), env(m);
+  for (int q = 0; q < n - 1; ++q) envb[q] = q;
+  for (const Edge& e : edges) {
+    if (e.i <= 0 || e.j <= 0) continue;
+    const int a = pos[e.i], b2 = pos[e.j];
+    const int lo = std::min(a, b2), hi = std::max(a, b2);
+    envb[hi] = std::min(envb[hi], lo);
+  }
+  double env_work = 0.0;
+  for (int r = 0; r < m; ++r) {
+    env[r] = 7 * envb[r / 7];
+    env_work += 0.5 * (double)(r - env[r] + 1) * (double)(r - env[r] + 1);
+  }
+  // the envelope solve when it saves most of the dense work, else the threaded dense one
+  const bool use_env = env_work < 0.25 * (double)m * m * m / 6.0;
   std::vector<double> H((size_t)m * m), b(m), A, x;
   for (int it = 0; it < iterations; ++it) {
     std::fill(H.begin(), H.end(), 0.0);
@@ -376,7 +471,7 @@ double PoseGraph::optimize(int iterations, double lam) {
       static const double Id[49] = {1, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0,
                                     0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1};
       const double* J[2] = {Ji, Id};
-      const int col[2] = {e.i > 0 ? 7 * (e.i - 1) : -1, e.j > 0 ? 7 * (e.j - 1) : -1};
+      const int col[2] = {e.i > 0 ? 7 * pos[e.i] : -1, e.j > 0 ? 7 * pos[e.j] : -1};
       double JtW[2][49];  // J^T W per block
       for (int q = 0; q < 2; ++q)
         for (int a = 0; a < 7; ++a)
@@ -410,9 +505,9 @@ double PoseGraph::optimize(int iterations, double lam) {
       x = b;
       for (double& v : x) v = -v;
       const std::vector<M4> old = poses;
-      bool solved = cholesky_solve(A, m, x, threads);
+      bool solved = use_env ? envelope_cholesky_solve(A, m, env, x) : cholesky_solve(A, m, x, threads);
       if (solved) {
-        for (int k = 1; k < n; ++k) poses[k] = mul(poses[k], sim3_exp(&x[7 * (k - 1)]));
+        for (int k = 1; k < n; ++k) poses[k] = mul(poses[k], sim3_exp(&x[7 * pos[k]]));
         cnew = cost();
       }
       if (solved && std::isfinite(cnew) && cnew <= c) {

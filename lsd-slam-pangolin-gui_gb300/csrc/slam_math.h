@@ -7,8 +7,9 @@
 // says "pose j seen from pose i is Z" with 7x7 information W in the twist order (v, omega,
 // log-scale), the cost is sum rho(r^T W r) with r = log(Z^-1 T_i^-1 T_j) and a Huber kernel rho on
 // the Mahalanobis norm; perturbations act on the right (T <- T exp(d)), so to first order
-// r(d) = r + d_j - Adj(T_j^-1 T_i) d_i.  Damped Gauss-Newton over the dense normal equations,
-// factorised by a blocked Cholesky whose trailing updates run on several host threads.
+// r(d) = r + d_j - Adj(T_j^-1 T_i) d_i.  Damped Gauss-Newton over the normal equations, with the
+// nodes in reverse Cuthill-McKee order and factorised inside their lower envelope (or, when the
+// envelope is wide, by a dense blocked Cholesky whose trailing updates run on several host threads).
 #pragma once
 
 #include <array>
@@ -65,6 +66,10 @@ class PoseGraph {
 // Cholesky factorisation in place of the m x m symmetric positive definite matrix A (row-major,
 // lower triangle used) and the solve A x = b; false when a pivot is not positive.
 bool cholesky_solve(std::vector<double>& A, int m, std::vector<double>& b, int threads);
+// The same restricted to the lower envelope (row i starts at column env[i]); the optimiser orders the
+// nodes by reverse Cuthill-McKee (rcm_positions) and uses it when it saves most of the dense work.
+bool envelope_cholesky_solve(std::vector<double>& A, int m, const std::vector<int>& env, std::vector<double>& b);
+std::vector<int> rcm_positions(int n, const std::vector<Edge>& edges);
 
 
 }  // namespace slam
