@@ -89,8 +89,9 @@ def test_loop_edge_and_huber_like_numpy():
     cg.close()
 
 
-def test_large_graph_uses_the_threaded_factorisation():
-    """A 200-node graph (1,393 unknowns: several 64-column blocks, threaded trailing updates)."""
+def test_large_chain_uses_the_envelope_factorisation():
+    """A 200-node chain with edges that skip 7 nodes (1,393 unknowns): in reverse Cuthill-McKee order
+    its envelope is a few blocks wide, so the envelope factorisation solves it."""
     rng = np.random.default_rng(7)
     truth = [np.eye(4)]
     for _ in range(199):
@@ -165,3 +166,52 @@ def test_branch_kept_when_inputs_drift_off_so3():
     g.optimize(20)
     rel = [g.pose(idx[k])[12] / g.pose(idx[k - 1])[12] for k in range(1, len(idx))]
     np.testing.assert_allclose(rel, 1.0, atol=1e-6)
+
+
+def test_densely_connected_graph_uses_the_threaded_factorisation():
+    """80 nodes each tied to 12 random others (553 unknowns): no order keeps the envelope narrow, so
+    the dense blocked Cholesky with threaded trailing updates solves it; consistent edges give the
+    truth back."""
+    rng = np.random.default_rng(11)
+    n = 80
+    truth = [np.eye(4)] + [rand_sim3(rng, (0.9, 1.1), 1.0, 0.5)[0] for _ in range(n - 1)]
+    start = [truth[0]] + [T @ rand_sim3(rng, (0.99, 1.01), 0.01, 0.01)[0] for T in truth[1:]]
+    edges = [(k - 1, k, G.sim3_inv(truth[k - 1]) @ truth[k], np.eye(7)) for k in range(1, n)]
+    for k in range(n):
+        for j in rng.choice(n, 12, replace=False):
+            if j != k:
+                edges.append((int(k), int(j), G.sim3_inv(truth[k]) @ truth[j], np.eye(7)))
+    _, cg = _both(start, edges)
+    assert cg.optimize(20) < 1e-14
+    for k in (17, 45, 79):
+        np.testing.assert_allclose(G.from13(cg.pose(k)), truth[k], atol=1e-6)
+    cg.close()
+
+
+def test_two_laps_like_numpy():
+    """A path driven twice: the second lap's keyframes tied to the first lap's (far apart in creation
+    order, neighbours in reverse Cuthill-McKee order), with drift on the odometry and a scale
+    disagreement on the ties; the envelope solve converges to the numpy restatement's poses."""
+    rng = np.random.default_rng(13)
+    n = 24
+    step = G.sim3_exp(np.array([0.25, 0, 0, 0, 2 * math.pi / n, 0, 0]))
+    truth = [np.eye(4)]
+    for _ in range(2 * n - 1):
+        truth.append(truth[-1] @ step)
+    drift = G.sim3_exp(np.array([0.004, 0.002, 0, 0.001, 0.003, 0, 0.003]))
+    nodes, edges = [truth[0]], []
+    for k in range(1, 2 * n):
+        Z = G.sim3_inv(truth[k - 1]) @ truth[k] @ drift
+        nodes.append(nodes[-1] @ Z)
+        edges.append((k - 1, k, Z, np.eye(7) * 10))
+    for k in range(n, 2 * n):  # second lap seen from the first, 5 % scale disagreement
+        Z = G.sim3_inv(truth[k - n]) @ truth[k]
+        Z[:3, :3] *= 1.05
+        edges.append((k - n, k, Z, np.eye(7)))
+    py, cg = _both(nodes, edges)
+    c_py = py.optimize(30)
+    c_cg = cg.optimize(30)
+    assert c_cg == pytest.approx(c_py, rel=1e-6)
+    for k in range(0, 2 * n, 5):
+        np.testing.assert_allclose(G.from13(cg.pose(k)), py.poses[k], atol=1e-6)
+    cg.close()
