@@ -644,7 +644,10 @@ typedef struct lsdg_slam_params {
   float react_min_good;     /* ... accepted when at least this share of the points in view are
                                inliers, and when the frame lies within half of kf_dist and of
                                kf_angle_deg of the keyframe (so that it is not left at once)      */
-  int32_t reserved[2];
+  int32_t retrack_iterations; /* when the current keyframe is left: this many rounds of re-tracking
+                                 the frames mapped into it against its refined depth and mapping
+                                 them again from its starting depth with the new poses (0 = off) */
+  int32_t reserved[1];
 } lsdg_slam_params;
 
 typedef struct lsdg_slam_stats {

@@ -15,6 +15,9 @@
 //     every frame by default), and after kf_dist metres of travel, a kf_angle turn, or when fewer than
 //     kf_min_usage of the keyframe's points stay in view, the frame becomes the new keyframe
 //     (DepthMap::createKeyFrame: propagation + regularisation);
+//   * keyframe refinement (caller's thread, when the current keyframe is left): its frames tracked
+//     again against its refined depth and mapped again from its starting depth with the new poses,
+//     a few rounds;
 //   * re-positioning (caller's thread, before a keyframe would be made): the earlier keyframes whose
 //     camera is near the current one in the graph are tracked against the frame; one that keeps most
 //     of its points in view at a pose close to the graph's prediction becomes the current keyframe
@@ -83,6 +86,11 @@ struct lsdg_slam {
   int since_refresh = 0;
   int loops_pending = 0;
   int cur = 0;                 // the current keyframe (tracked against, mapped)
+  // the current keyframe's refinement state: its image and depth when it became current, and the
+  // frames mapped into it since (8-bit images back to back, and their trajectory indices)
+  std::vector<float> kf_image, kf_init_d, kf_init_v;
+  std::vector<uint8_t> hist_images;
+  std::vector<long> hist_traj;
   lsdg_slam_stats stats{};
   lsdg_slam_stats wstats{};  // counted by the worker's jobs, added to stats when the worker is joined
   std::vector<float> d_buf, v_buf;
@@ -379,6 +387,56 @@ void optimize_graph(lsdg_slam* s, int iterations) {
   s->wstats.graph_optimisations++;
 }
 
+// The state a keyframe's refinement starts from when it becomes current: its image (float) and the
+// depth it starts with; no frames mapped yet.
+void begin_keyframe_state(lsdg_slam* s, const float* image, const float* d, const float* v) {
+  const size_t npix = (size_t)s->w * s->h;
+  s->kf_image.assign(image, image + npix);
+  s->kf_init_d.assign(d, d + npix);
+  s->kf_init_v.assign(v, v + npix);
+  s->hist_images.clear();
+  s->hist_traj.clear();
+}
+
+// Refinement of the current keyframe before it is left (a block-coordinate pass over its window of
+// frames): every frame mapped into it is tracked again against its refined depth (from the pose it
+// had), then the depth map restarts from the keyframe's starting depth and maps the frames again with
+// the new poses, and the tracking reference takes the result; retrack_iterations rounds.  Tracking
+// and mapping feed each other inside one keyframe (a small error of the tracked translation tilts
+// the map triangulated from it, and the tilted map biases the next tracked poses); re-estimating the
+// window's poses against the map its own frames built, and the map from those poses, damps that.
+// scratch: a frame to upload into.  Poses that do not track again keep their value.
+lsdg_status refine_keyframe(lsdg_slam* s, lsdg_frame* scratch) {
+  const int nh = (int)s->hist_traj.size();
+  if (s->sp.retrack_iterations <= 0 || nh < 2) return LSDG_OK;
+  const size_t npix = (size_t)s->w * s->h;
+  std::vector<double> k2f12(12 * (size_t)nh);
+  for (int it = 0; it < s->sp.retrack_iterations; ++it) {
+    for (int i = 0; i < nh; ++i) {
+      M4& pose = s->traj[s->hist_traj[i]].f2k;
+      SLAM_CK(s, lsdg_frame_upload_u8(s->ctx, scratch, &s->hist_images[npix * i]), s->ctx);
+      double g12[12], o12[12];
+      lsdg::slam::to12(pose, g12);
+      lsdg_track_stats st{};
+      const lsdg_status ts = lsdg_track_se3(s->ctx, s->keyframes[s->cur].frame, scratch, g12, o12, &st);
+      if (ts != LSDG_OK && ts != LSDG_TRACKING_LOST) return fail(s, ts, "lsdg_track_se3 (keyframe refinement)", s->ctx);
+      const M4 p2 = lsdg::slam::from12(o12);
+      const double d[3] = {p2(0, 3) - pose(0, 3), p2(1, 3) - pose(1, 3), p2(2, 3) - pose(2, 3)};
+      if (st.status == LSDG_OK && finite(p2) && norm3(d) <= 0.25 * s->sp.max_track_jump) pose = p2;
+    }
+    SLAM_CK(s, lsdg_depth_set_keyframe(s->ctx, s->dm, s->kf_image.data(), s->kf_init_d.data(), s->kf_init_v.data()),
+            s->ctx);
+    for (int i = 0; i < nh; ++i) lsdg::slam::to12(lsdg::slam::sim3_inv(s->traj[s->hist_traj[i]].f2k), &k2f12[12 * i]);
+    for (int c0 = 0; c0 < nh; c0 += LSDG_MAX_REFS) {
+      const int nc = std::min(LSDG_MAX_REFS, nh - c0);
+      SLAM_CK(s, lsdg_depth_update_u8(s->ctx, s->dm, nc, &s->hist_images[npix * c0], &k2f12[12 * c0], 1), s->ctx);
+    }
+    lsdg_status r = reference_depth(s, s->keyframes[s->cur].frame);
+    if (r != LSDG_OK) return r;
+  }
+  return LSDG_OK;
+}
+
 // Re-positioning before a new keyframe (SlamSystem's re-activation of an earlier keyframe): the
 // earlier keyframes whose camera lies within react_radius and react_angle_deg of the current camera
 // in the graph are tracked against `frame` (nearest first, at most three); the first that keeps
@@ -458,6 +516,7 @@ lsdg_status try_reactivate(lsdg_slam* s, lsdg_frame* frame, const M4& f2k, bool*
     for (size_t i = 0; i < npix; ++i) img[i] = lvl[4 * i];
     SLAM_CK(s, lsdg_frame_get_depth(s->ctx, s->keyframes[c].frame, 0, s->d_buf.data(), s->v_buf.data()), s->ctx);
     SLAM_CK(s, lsdg_depth_set_keyframe(s->ctx, s->dm, img.data(), s->d_buf.data(), s->v_buf.data()), s->ctx);
+    begin_keyframe_state(s, img.data(), s->d_buf.data(), s->v_buf.data());
     s->cur = c;
     s->traj.back() = {c, f2c};
     s->since_refresh = 0;
@@ -492,6 +551,7 @@ lsdg_status new_keyframe(lsdg_slam* s, int frame_index, const uint8_t* image, co
   }
   const int prev_node = prev.node;
   s->keyframes.push_back(kf);
+  begin_keyframe_state(s, img.data(), s->d_buf.data(), s->v_buf.data());
   s->cur = (int)s->keyframes.size() - 1;
   s->traj.back() = {s->cur, M4::identity()};
   s->since_refresh = 0;
@@ -536,6 +596,7 @@ void lsdg_slam_default_params(lsdg_slam_params* p) {
   p->react_max_jump = 0.5f;
   p->react_min_age = 10;
   p->react_min_good = 0.9f;
+  p->retrack_iterations = 4;
 }
 
 lsdg_status lsdg_slam_create(const lsdg_params* params, const lsdg_slam_params* sp, int device, int width, int height,
@@ -594,6 +655,7 @@ lsdg_status lsdg_slam_bootstrap(lsdg_slam* s, int id, const uint8_t* image, cons
   std::vector<float> img((size_t)s->w * s->h);
   for (size_t i = 0; i < img.size(); ++i) img[i] = (float)image[i];
   SLAM_CK(s, lsdg_depth_set_keyframe(s->ctx, s->dm, img.data(), idepth, var), s->ctx);
+  begin_keyframe_state(s, img.data(), idepth, var);
   Keyframe kf;
   kf.frame_index = 0;
   kf.node = s->graph.add_node(M4::identity());
@@ -647,6 +709,10 @@ lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
   double k2f12[12];
   lsdg::slam::to12(k2f, k2f12);
   SLAM_CK(s, lsdg_depth_update_u8(s->ctx, s->dm, 1, image, k2f12, 1), s->ctx);
+  if (s->sp.retrack_iterations > 0) {
+    s->hist_images.insert(s->hist_images.end(), image, image + (size_t)s->w * s->h);
+    s->hist_traj.push_back((long)s->traj.size() - 1);
+  }
   if (++s->since_refresh >= s->sp.refresh_every) {
     lsdg_status r = reference_depth(s, s->keyframes[kfi].frame);
     if (r != LSDG_OK) return r;
@@ -655,6 +721,10 @@ lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
   const double t[3] = {f2k(0, 3), f2k(1, 3), f2k(2, 3)};
   if (norm3(t) > s->sp.kf_dist || rotation_angle(f2k) > s->sp.kf_angle_deg * M_PI / 180.0 ||
       st.usage < s->sp.kf_min_usage) {
+    // the keyframe is left: refine it (poses of its frames, its depth), the other pool frame as scratch
+    lsdg_status rr = refine_keyframe(s, s->pool[s->pool_next]);
+    if (rr != LSDG_OK) return rr;
+    f2k = s->traj.back().f2k;
     if (s->sp.reactivate) {
       bool done = false;
       lsdg_status r = try_reactivate(s, frame, f2k, &done);

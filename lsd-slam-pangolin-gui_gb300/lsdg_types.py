@@ -136,7 +136,7 @@ class SlamParams(C.Structure):
         ("ref_max_var", C.c_float), ("epipolar_var", C.c_float), ("reactivate", C.c_int32),
         ("react_radius", C.c_float), ("react_angle_deg", C.c_float), ("react_min_usage", C.c_float),
         ("react_max_jump", C.c_float), ("react_min_age", C.c_int32), ("react_min_good", C.c_float),
-        ("reserved", C.c_int32 * 2),
+        ("retrack_iterations", C.c_int32), ("reserved", C.c_int32 * 1),
     ]
 
 
