@@ -91,6 +91,10 @@ struct lsdg_slam {
   std::vector<float> kf_image, kf_init_d, kf_init_v;
   std::vector<uint8_t> hist_images;
   std::vector<long> hist_traj;
+  // the refinement's re-tracking runs as one batch of kRefineBatch pairs (frames uploaded into
+  // hist_frames), created on first use
+  std::vector<lsdg_frame*> hist_frames;
+  lsdg_batch* refine_batch = nullptr;
   lsdg_slam_stats stats{};
   lsdg_slam_stats wstats{};  // counted by the worker's jobs, added to stats when the worker is joined
   std::vector<float> d_buf, v_buf;
@@ -405,24 +409,47 @@ void begin_keyframe_state(lsdg_slam* s, const float* image, const float* d, cons
 // and mapping feed each other inside one keyframe (a small error of the tracked translation tilts
 // the map triangulated from it, and the tilted map biases the next tracked poses); re-estimating the
 // window's poses against the map its own frames built, and the map from those poses, damps that.
-// scratch: a frame to upload into.  Poses that do not track again keep their value.
-lsdg_status refine_keyframe(lsdg_slam* s, lsdg_frame* scratch) {
+// The re-tracking of a round is one batched launch; poses that do not track again keep their value.
+constexpr int kRefineBatch = 16;
+
+lsdg_status refine_keyframe(lsdg_slam* s) {
   const int nh = (int)s->hist_traj.size();
   if (s->sp.retrack_iterations <= 0 || nh < 2) return LSDG_OK;
   const size_t npix = (size_t)s->w * s->h;
   std::vector<double> k2f12(12 * (size_t)nh);
+  // the window's frames on the device, and the batch that re-tracks up to kRefineBatch at once
+  while ((int)s->hist_frames.size() < std::min(nh, kRefineBatch)) {
+    lsdg_frame* f = nullptr;
+    SLAM_CK(s, lsdg_frame_create(s->ctx, s->w, s->h, &s->intr, &f), s->ctx);
+    s->hist_frames.push_back(f);
+  }
+  if (!s->refine_batch) {
+    std::vector<int> ws(kRefineBatch, s->w), hs(kRefineBatch, s->h);
+    std::vector<lsdg_intrinsics> ks(kRefineBatch, s->intr);
+    SLAM_CK(s, lsdg_batch_create(s->ctx, kRefineBatch, ws.data(), hs.data(), ks.data(), &s->refine_batch), s->ctx);
+  }
+  std::vector<const lsdg_frame*> refs(kRefineBatch, s->keyframes[s->cur].frame), frames(kRefineBatch);
+  std::vector<double> init(12 * (size_t)kRefineBatch), out(12 * (size_t)kRefineBatch);
+  std::vector<lsdg_track_stats> st(kRefineBatch);
   for (int it = 0; it < s->sp.retrack_iterations; ++it) {
-    for (int i = 0; i < nh; ++i) {
-      M4& pose = s->traj[s->hist_traj[i]].f2k;
-      SLAM_CK(s, lsdg_frame_upload_u8(s->ctx, scratch, &s->hist_images[npix * i]), s->ctx);
-      double g12[12], o12[12];
-      lsdg::slam::to12(pose, g12);
-      lsdg_track_stats st{};
-      const lsdg_status ts = lsdg_track_se3(s->ctx, s->keyframes[s->cur].frame, scratch, g12, o12, &st);
-      if (ts != LSDG_OK && ts != LSDG_TRACKING_LOST) return fail(s, ts, "lsdg_track_se3 (keyframe refinement)", s->ctx);
-      const M4 p2 = lsdg::slam::from12(o12);
-      const double d[3] = {p2(0, 3) - pose(0, 3), p2(1, 3) - pose(1, 3), p2(2, 3) - pose(2, 3)};
-      if (st.status == LSDG_OK && finite(p2) && norm3(d) <= 0.25 * s->sp.max_track_jump) pose = p2;
+    for (int c0 = 0; c0 < nh; c0 += kRefineBatch) {
+      const int nc = std::min(kRefineBatch, nh - c0);
+      for (int i = 0; i < kRefineBatch; ++i) {
+        const int h = c0 + (i < nc ? i : 0);  // unused pairs repeat the chunk's first and are not read
+        if (it == 0 || nh > kRefineBatch)
+          if (i < nc) SLAM_CK(s, lsdg_frame_upload_u8(s->ctx, s->hist_frames[i], &s->hist_images[npix * h]), s->ctx);
+        frames[i] = s->hist_frames[i < nc ? i : 0];
+        lsdg::slam::to12(s->traj[s->hist_traj[h]].f2k, &init[12 * i]);
+      }
+      SLAM_CK(s, lsdg_batch_load_frames(s->ctx, s->refine_batch, refs.data(), frames.data(), init.data()), s->ctx);
+      SLAM_CK(s, lsdg_batch_run(s->ctx, s->refine_batch), s->ctx);
+      SLAM_CK(s, lsdg_batch_read(s->ctx, s->refine_batch, out.data(), st.data()), s->ctx);
+      for (int i = 0; i < nc; ++i) {
+        M4& pose = s->traj[s->hist_traj[c0 + i]].f2k;
+        const M4 p2 = lsdg::slam::from12(&out[12 * i]);
+        const double d[3] = {p2(0, 3) - pose(0, 3), p2(1, 3) - pose(1, 3), p2(2, 3) - pose(2, 3)};
+        if (st[i].status == LSDG_OK && finite(p2) && norm3(d) <= 0.25 * s->sp.max_track_jump) pose = p2;
+      }
     }
     SLAM_CK(s, lsdg_depth_set_keyframe(s->ctx, s->dm, s->kf_image.data(), s->kf_init_d.data(), s->kf_init_v.data()),
             s->ctx);
@@ -640,6 +667,9 @@ lsdg_status lsdg_slam_destroy(lsdg_slam* s) {
   }
   for (lsdg_frame* f : s->pool)
     if (f) lsdg_frame_destroy(s->ctx, f);
+  for (lsdg_frame* f : s->hist_frames)
+    if (f) lsdg_frame_destroy(s->ctx, f);
+  if (s->refine_batch) lsdg_batch_destroy(s->ctx, s->refine_batch);
   if (s->dm) lsdg_depth_destroy(s->ctx, s->dm);
   if (s->ctx_cons) lsdg_destroy(s->ctx_cons);
   if (s->ctx) lsdg_destroy(s->ctx);
@@ -721,8 +751,8 @@ lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
   const double t[3] = {f2k(0, 3), f2k(1, 3), f2k(2, 3)};
   if (norm3(t) > s->sp.kf_dist || rotation_angle(f2k) > s->sp.kf_angle_deg * M_PI / 180.0 ||
       st.usage < s->sp.kf_min_usage) {
-    // the keyframe is left: refine it (poses of its frames, its depth), the other pool frame as scratch
-    lsdg_status rr = refine_keyframe(s, s->pool[s->pool_next]);
+    // the keyframe is left: refine it (poses of its frames, its depth)
+    lsdg_status rr = refine_keyframe(s);
     if (rr != LSDG_OK) return rr;
     f2k = s->traj.back().f2k;
     if (s->sp.reactivate) {
