@@ -411,6 +411,7 @@ void begin_keyframe_state(lsdg_slam* s, const float* image, const float* d, cons
 // window's poses against the map its own frames built, and the map from those poses, damps that.
 // The re-tracking of a round is one batched launch; poses that do not track again keep their value.
 constexpr int kRefineBatch = 16;
+constexpr int kMaxWindow = 32;  // frames a keyframe's refinement keeps (the most recent)
 
 lsdg_status refine_keyframe(lsdg_slam* s) {
   const int nh = (int)s->hist_traj.size();
@@ -740,7 +741,14 @@ lsdg_status lsdg_slam_next_image(lsdg_slam* s, int id, const uint8_t* image) {
   lsdg::slam::to12(k2f, k2f12);
   SLAM_CK(s, lsdg_depth_update_u8(s->ctx, s->dm, 1, image, k2f12, 1), s->ctx);
   if (s->sp.retrack_iterations > 0) {
-    s->hist_images.insert(s->hist_images.end(), image, image + (size_t)s->w * s->h);
+    // the refinement window: the keyframe's most recent kMaxWindow frames (a keyframe that is never
+    // left, under a still camera, keeps a bounded window)
+    const size_t npix = (size_t)s->w * s->h;
+    if ((int)s->hist_traj.size() >= kMaxWindow) {
+      s->hist_images.erase(s->hist_images.begin(), s->hist_images.begin() + (long)npix);
+      s->hist_traj.erase(s->hist_traj.begin());
+    }
+    s->hist_images.insert(s->hist_images.end(), image, image + npix);
     s->hist_traj.push_back((long)s->traj.size() - 1);
   }
   if (++s->since_refresh >= s->sp.refresh_every) {
