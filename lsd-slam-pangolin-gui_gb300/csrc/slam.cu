@@ -23,11 +23,12 @@
 //     of its points in view at a pose close to the graph's prediction becomes the current keyframe
 //     again (its depth map is refined further) and the keyframe left is tied to it in the graph;
 //   * constraint search (a worker thread with a context of its own): each new keyframe is aligned
-//     with Sim3Tracker::trackFrameSim3 to its predecessor and the nearest earlier keyframes in one
+//     with Sim3Tracker::trackFrameSim3 to its parent and the nearest earlier keyframes in one
 //     batched launch from device-resident keyframes -- in both directions, a constraint being kept
 //     only when the two alignments agree -- and the Sim3 pose graph is optimised every few loop
-//     constraints.  The worker runs while tracking and mapping go on; it is joined before the next
-//     keyframe is made, so the results do not depend on thread timing.
+//     constraints (and after each re-positioning's loop edge).  The worker runs while tracking and
+//     mapping go on; it is joined before the graph is read or changed on the caller's thread (a
+//     keyframe decision, the outputs), so the results do not depend on thread timing.
 // The first keyframe's depth is given (lsdg_slam_bootstrap); upstream starts from a random map.
 #include <cuda_runtime.h>
 
