@@ -1,8 +1,8 @@
 """Full synthetic sequence runs of the SLAM loop (lsdg_slam, csrc/slam.cu) and their evaluation.
 
-The loop itself -- tracking and mapping of every frame, keyframes (or an earlier keyframe made current
-again), batched Sim3 constraint search in both directions on a worker thread, the Sim3 pose graph --
-is the library's C++ (lsdg_slam_*);
+The loop itself -- tracking and mapping of every frame, keyframes (refined before they are left, or an
+earlier keyframe made current again), batched Sim3 constraint search in both directions on a worker
+thread, the Sim3 pose graph -- is the library's C++ (lsdg_slam_*);
 this module feeds it a rendered sequence the way the reference's InputThread feeds SlamSystem
 (lib/App/InputThread.cpp:71), then scores the trajectory against the ground truth: absolute
 trajectory error of the camera centres after the best similarity alignment (Umeyama 1991), as a
